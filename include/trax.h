@@ -1,0 +1,292 @@
+/*
+ * trax.h -- C-ABI of the GB300 triplet-seeding path.
+ *
+ * Replaces the C++ operator surface of trax's seeding chain, which the
+ * reference calls in this order from buildTriplets
+ * (src/triplet_builder/TripletBuilder.cpp:240-263):
+ *
+ *   GridBuilder::run              src/algorithms/GridBuilder.h:42, GridBuilder.cpp:6
+ *   PairGeneratorBeamspot::run    src/algorithms/PairGeneratorBeamspot.h:40-41, .cpp:5
+ *   TripletThetaPhiPredictor::run src/algorithms/TripletThetaPhiPredictor.h:43-44, .cpp:10
+ *   TripletThetaPhiFilter::run    src/algorithms/TripletThetaPhiFilter.h:46-48, .cpp:10
+ *
+ * Conventions
+ *  - Plain C types only; every pointer documents whether it is host or device.
+ *  - Every call returns a trax_status and never throws.  Kernel-side faults
+ *    (hits outside the grid, a bounded wait that gave up, an output larger
+ *    than its capacity) are recorded in a device status word that
+ *    trax_read_counts() and trax_ctx_synchronize() return.
+ *  - Stage calls are asynchronous and stream ordered on the context's stream.
+ *    One context per host thread; contexts are independent.
+ *  - Output buffers are caller allocated with an explicit capacity.  When a
+ *    result does not fit, nothing is written out of bounds and the status
+ *    word reports TRAX_ERR_CAPACITY; the true size is still reported.
+ *  - Hit indices in pairs, candidates and tracklets are indices into the
+ *    cell-sorted hit columns written by trax_grid_build, as in the reference.
+ *    The sorted `orig` column maps them back to input positions.
+ */
+#ifndef TRAX_H
+#define TRAX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TRAX_ABI_VERSION 1
+#define TRAX_MAX_LAYER_TRIPLETS 16
+#define TRAX_MAX_LAYERS 16
+
+typedef enum trax_status {
+    TRAX_OK = 0,
+    TRAX_ERR_BAD_ARG = 1,   /* invalid argument or configuration */
+    TRAX_ERR_OOM = 2,       /* device allocation failed / memory budget exceeded */
+    TRAX_ERR_TIMEOUT = 3,   /* a bounded device-side wait gave up */
+    TRAX_ERR_DEVICE = 4,    /* CUDA runtime error */
+    TRAX_ERR_CAPACITY = 5,  /* an output did not fit its capacity */
+    TRAX_ERR_BAD_INPUT = 6, /* hit outside the grid, NaN, or layout mismatch */
+    TRAX_ERR_NO_DEVICE = 7  /* no CUDA device / CUDA unavailable */
+} trax_status;
+
+typedef struct trax_ctx trax_ctx;
+
+/* GridConfig (src/datastructures/Grid.h:5-39).  The z and phi extents are the
+ * reference's fixed -300..300 cm and -pi..pi. */
+typedef struct trax_grid_cfg {
+    uint32_t n_events;
+    uint32_t n_layers;      /* layers 1..n_layers are gridded */
+    uint32_t n_sectors_z;
+    uint32_t n_sectors_phi;
+} trax_grid_cfg;
+
+/* One row of TripletConfigurations
+ * (src/datastructures/TripletConfiguration.h:33, values as parsed by
+ * TripletConfiguration.cpp:191-207; z0 is parsed as an unsigned integer). */
+typedef struct trax_layer_triplet {
+    uint32_t layer1, layer2, layer3;
+    float dtheta_cut;
+    float sigma_z;
+    float dphi_cut;
+    float sigma_phi;
+    float tip_cut;
+    uint32_t pair_spread_z;
+    float z0;
+    uint32_t pair_spread_phi;
+    uint32_t n_candidates;
+} trax_layer_triplet;
+
+/* Everything on the path that is not per event.
+ * Layer triplet i must have layer1 == i + 1: the reference's predictor and
+ * filter derive the triplet index from the innermost hit's layer
+ * (TripletThetaPhiPredictor.h:79, TripletThetaPhiFilter.h:73). */
+typedef struct trax_config {
+    uint32_t n_layer_triplets;
+    trax_layer_triplet triplets[TRAX_MAX_LAYER_TRIPLETS];
+    /* GeometrySupplement (GeometrySupplement.h:21-43), index = layer - 1 */
+    uint32_t n_geom_layers;
+    float min_radius[TRAX_MAX_LAYERS];
+    float max_radius[TRAX_MAX_LAYERS];
+    float min_pt;  /* GeV; TripletConfigurations::minPt_ */
+    float bz;      /* Tesla; 0 selects the reference's IDEAL_BZ 3.8112 */
+} trax_config;
+
+/* HitCollection columns (HitCollection.h:23, HIT_COLLECTION_ITEMS), device
+ * pointers.  Input order: event-major, then layer-major, exactly as
+ * HitCollection::addEvent produces it (HitCollection.cpp:121-146). */
+typedef struct trax_hits {
+    const float *x, *y, *z;
+    const uint32_t *layer;       /* 1-based detector layer */
+    const uint32_t *detector_id;
+    const uint32_t *hit_id;      /* the reference stores the sim-track id here */
+    const uint32_t *event;       /* event index within the batch */
+    uint32_t n;
+} trax_hits;
+
+/* Cell-sorted hit columns written by trax_grid_build (device pointers).  The
+ * seven reference columns plus `phi` (atan2(y,x), used by the later stages)
+ * and `orig` (input position of the hit). */
+typedef struct trax_sorted_hits {
+    float *x, *y, *z, *phi;
+    uint32_t *layer, *detector_id, *hit_id, *event, *orig;
+    uint32_t n;
+} trax_sorted_hits;
+
+/* EventSupplement / LayerSupplement (EventSupplement.h:8-32,
+ * LayerSupplement.h:7-31): host arrays. */
+typedef struct trax_layout {
+    uint32_t n_events;
+    uint32_t n_layers;
+    const uint32_t *event_nhits;   /* [n_events] */
+    const uint32_t *event_offset;  /* [n_events] */
+    const uint32_t *layer_nhits;   /* [n_events * n_layers] */
+    const uint32_t *layer_offset;  /* [n_events * n_layers], within the event */
+} trax_layout;
+
+/* Pairing (src/datastructures/Pairings.h:9-59): uint2 records plus
+ * per-(event, layer triplet) offsets.  Device pointers. */
+typedef struct trax_pairs {
+    uint32_t *pairs;    /* 2 * capacity uint32: (x, y) records */
+    uint32_t *offsets;  /* n_events * n_layer_triplets + 1 */
+    uint32_t capacity;  /* records */
+} trax_pairs;
+
+/* TrackletCollection (src/datastructures/TrackletCollection.h:32-77):
+ * TrackletHit1/2/3 columns plus per-(event, layer triplet) offsets. */
+typedef struct trax_tracklets {
+    uint32_t *hit1, *hit2, *hit3;
+    uint32_t *offsets;  /* n_events * n_layer_triplets + 1 */
+    uint32_t capacity;
+} trax_tracklets;
+
+/* Device counters accumulated since the last trax_reset_counts(). */
+typedef struct trax_counts {
+    uint64_t n_hits;
+    uint64_t n_pairs;          /* distinct accepted (inner, outer) pairs */
+    uint64_t pair_slots;       /* pairCount total: slots the reference allocates */
+    uint64_t n_candidates;     /* candidates stored by the predictor */
+    uint64_t cand_slots;       /* predictCount total: slots the reference allocates */
+    uint64_t cand_truncated;   /* store-window accepts dropped at the count cap */
+    uint64_t n_tracklets;
+    uint32_t status;           /* trax_status of the first device-side fault */
+    uint32_t error_detail;     /* which check raised it (TRAX_DETAIL_*) */
+} trax_counts;
+
+#define TRAX_DETAIL_HIT_OUTSIDE_GRID 1u
+#define TRAX_DETAIL_HIT_LAYER_MISMATCH 2u
+#define TRAX_DETAIL_WINDOW_OUTSIDE_GRID 3u
+#define TRAX_DETAIL_PAIR_CAPACITY 4u
+#define TRAX_DETAIL_CAND_CAPACITY 5u
+#define TRAX_DETAIL_TRACKLET_CAPACITY 6u
+#define TRAX_DETAIL_SCAN_TIMEOUT 7u
+#define TRAX_DETAIL_BAD_TRIPLET_INDEX 8u
+
+/* ---- context ---------------------------------------------------------- */
+
+const char *trax_version(void);
+trax_status trax_ctx_create(trax_ctx **out, int device);
+void trax_ctx_destroy(trax_ctx *ctx);
+/* cudaStream_t passed as void*; NULL selects the context's own stream. */
+trax_status trax_ctx_set_stream(trax_ctx *ctx, void *stream);
+void *trax_ctx_get_stream(trax_ctx *ctx);
+const char *trax_ctx_last_error(const trax_ctx *ctx);
+/* Waits for the stream; returns the device status word (or a CUDA error). */
+trax_status trax_ctx_synchronize(trax_ctx *ctx);
+/* Number of streaming multiprocessors of the context's device. */
+int trax_ctx_sm_count(const trax_ctx *ctx);
+
+/* Host-only checks (no device needed).  trax_config_validate enforces the
+ * reference's implicit preconditions: triplet i starts on layer i+1, every
+ * layer used has geometry, and (when grid is given) lies inside the grid.
+ * trax_layout_validate checks that the supplements describe hits bucketed
+ * event-major then layer-major with running offsets covering n_hits. */
+trax_status trax_config_validate(const trax_config *cfg, const trax_grid_cfg *grid);
+trax_status trax_layout_validate(const trax_layout *layout, uint32_t n_hits);
+/* sizeof of an ABI struct by name ("trax_config", ...); 0 if unknown. */
+size_t trax_abi_sizeof(const char *type_name);
+
+/* Validates and stores the per-run parameters; computes minRadiusCurvature
+ * (TripletConfiguration.cpp:145-152). */
+trax_status trax_configure(trax_ctx *ctx, const trax_config *cfg);
+/* TripletConfigurations::minRadiusCurvature(minPt, Bz) in cm. */
+float trax_min_radius_curvature(float min_pt, float bz);
+
+/* ---- device memory helpers (for hosts without their own CUDA binding) -- */
+
+trax_status trax_dev_alloc(trax_ctx *ctx, void **ptr, size_t bytes);
+trax_status trax_dev_free(trax_ctx *ctx, void *ptr);
+trax_status trax_host_alloc_pinned(trax_ctx *ctx, void **ptr, size_t bytes);
+trax_status trax_host_free_pinned(trax_ctx *ctx, void *ptr);
+trax_status trax_memcpy_h2d(trax_ctx *ctx, void *dst, const void *src, size_t bytes);
+trax_status trax_memcpy_d2h(trax_ctx *ctx, void *dst, const void *src, size_t bytes);
+trax_status trax_memset_d(trax_ctx *ctx, void *dst, int value, size_t bytes);
+/* CUDA-event timing on the context stream: record marks, read elapsed ms. */
+trax_status trax_timer_record(trax_ctx *ctx, int slot);
+trax_status trax_timer_elapsed_ms(trax_ctx *ctx, int slot_begin, int slot_end, float *ms);
+
+/* ---- the four stages -------------------------------------------------- */
+
+/* GridBuilder::run (GridBuilder.cpp:6-160): per (event, layer) counting sort
+ * of the hits into (z, phi) cells.  Writes the exclusive-scanned grid
+ * (n_events * n_layers * (nZ+1)(nPhi+1) uint32, device) and the sorted hit
+ * columns.  Within a cell hits keep their input order (the reference's order
+ * there is racy, GridBuilder.h:243-244). */
+trax_status trax_grid_build(trax_ctx *ctx, const trax_hits *in, const trax_layout *layout,
+                            const trax_grid_cfg *grid, trax_sorted_hits *out,
+                            uint32_t *d_grid);
+
+/* PairGeneratorBeamspot::run (PairGeneratorBeamspot.cpp:5-177): for every
+ * (event, layer triplet) and every hit on layer2, the beam-spot z/phi window
+ * on layer1; writes distinct accepted pairs (inner, outer) ordered by outer
+ * hit, then inner hit. */
+trax_status trax_pair_gen(trax_ctx *ctx, const trax_sorted_hits *hits, const uint32_t *d_grid,
+                          const trax_grid_cfg *grid, trax_pairs *out);
+
+/* TripletThetaPhiPredictor::run (TripletThetaPhiPredictor.cpp:10-131):
+ * per pair, the theta/phi window on layer3; writes candidates
+ * (pair index, hit3) with the reference's count/store semantics. */
+trax_status trax_triplet_predict(trax_ctx *ctx, const trax_sorted_hits *hits,
+                                 const uint32_t *d_grid, const trax_grid_cfg *grid,
+                                 const trax_pairs *pairs, trax_pairs *candidates);
+
+/* TripletThetaPhiFilter::run (TripletThetaPhiFilter.cpp:10-164): dTheta,
+ * dPhi, circle-fit TIP and minimum-radius cuts; writes tracklets in candidate
+ * order. */
+trax_status trax_triplet_filter(trax_ctx *ctx, const trax_sorted_hits *hits,
+                                const trax_grid_cfg *grid, const trax_pairs *pairs,
+                                const trax_pairs *candidates, trax_tracklets *out);
+
+trax_status trax_read_counts(trax_ctx *ctx, trax_counts *out);  /* synchronises */
+
+/* Diagnostic: evaluates the path's FP32 math on the device for n inputs
+ * (fn 0: atan2(a, b), 1: acos(a), 2: atan(a)); device pointers. */
+trax_status trax_eval_math(trax_ctx *ctx, int fn, const float *d_a, const float *d_b,
+                           float *d_out, uint32_t n);
+trax_status trax_reset_counts(trax_ctx *ctx);
+
+/* ---- batched pipeline ------------------------------------------------- */
+
+/* Host-side batch of events, bucketed as HitCollection::addEvent does. */
+typedef struct trax_event_batch {
+    uint32_t n_events;
+    uint32_t n_layers;
+    uint32_t n_hits;
+    const float *x, *y, *z;
+    const uint32_t *layer, *detector_id, *hit_id, *event;
+    const uint32_t *layer_nhits;  /* [n_events * n_layers] */
+} trax_event_batch;
+
+/* Host-side result.  Tracklet hit indices are input positions of the hits
+ * (the reference's sorted indices mapped through `orig`) when
+ * `input_indices` is non-zero, else sorted indices. */
+typedef struct trax_batch_result {
+    uint32_t *hit1, *hit2, *hit3;  /* host, capacity entries */
+    uint32_t *offsets;             /* host, n_events * n_layer_triplets + 1 */
+    uint32_t capacity;
+    int input_indices;
+    uint32_t n_tracklets;          /* out */
+    trax_counts counts;            /* out */
+} trax_batch_result;
+
+/* Pre-sizes every device buffer of the batched pipeline so that later
+ * trax_seed_batch calls allocate nothing and replay one CUDA graph. */
+trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers,
+                         uint32_t max_hits, const trax_grid_cfg *grid,
+                         uint32_t max_pairs, uint32_t max_candidates,
+                         uint32_t max_tracklets);
+
+/* Uploads the batch, runs grid build -> pairs -> predict -> filter as one
+ * CUDA graph and downloads the tracklets.  Synchronous. */
+trax_status trax_seed_batch(trax_ctx *ctx, const trax_event_batch *in, trax_batch_result *out);
+
+/* Device-resident variant for throughput measurement: the batch was uploaded
+ * by trax_stage_batch; runs the graph only (asynchronous). */
+trax_status trax_stage_batch(trax_ctx *ctx, const trax_event_batch *in);
+trax_status trax_run_staged(trax_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TRAX_H */

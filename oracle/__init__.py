@@ -1,0 +1,128 @@
+"""ctypes driver for the CPU oracle (trax_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and the CPU-baseline
+leg of bench.py use it as the checker.  Parity status: parity unpinned (see
+trax_oracle.h).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+from trax_gb300._abi import TraxConfig, TraxGridCfg
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libtrax_oracle.so")
+
+ITEMS = ("sorted_x", "sorted_y", "sorted_z", "sorted_phi", "sorted_layer", "sorted_det",
+         "sorted_hitid", "sorted_event", "sorted_orig", "grid", "pairs", "pair_valid",
+         "pair_offsets", "cands", "cand_valid", "cand_offsets", "trk_h1", "trk_h2", "trk_h3",
+         "trk_offsets", "stats")
+_DTYPES = {"sorted_x": np.float32, "sorted_y": np.float32, "sorted_z": np.float32,
+           "sorted_phi": np.float32, "pair_valid": np.uint8, "cand_valid": np.uint8,
+           "stats": np.uint64}
+STATS = ("status", "detail", "pair_slots", "pairs", "cand_slots", "cands", "cand_truncated",
+         "tracklets")
+
+_lib = None
+_lock = threading.Lock()
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-C", HERE])
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                build()
+            L = C.CDLL(LIB_PATH)
+            L.or_run.restype = C.c_void_p
+            L.or_run.argtypes = [C.POINTER(TraxConfig), C.POINTER(TraxGridCfg)] + [C.c_void_p] * 7 + \
+                [C.c_uint32] + [C.c_void_p] * 3 + [C.c_int, C.c_uint32, C.c_int]
+            L.or_size.restype = C.c_uint64
+            L.or_size.argtypes = [C.c_void_p, C.c_int]
+            L.or_data.restype = C.c_void_p
+            L.or_data.argtypes = [C.c_void_p, C.c_int]
+            L.or_free.argtypes = [C.c_void_p]
+            L.or_prefix_sum.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32]
+            for f in ("or_atan2f",):
+                getattr(L, f).restype = C.c_float
+                getattr(L, f).argtypes = [C.c_float, C.c_float]
+            for f in ("or_acosf", "or_atanf"):
+                getattr(L, f).restype = C.c_float
+                getattr(L, f).argtypes = [C.c_float]
+            L.or_math_batch.restype = None
+            L.or_math_batch.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64]
+            L.or_min_radius_curvature.restype = C.c_float
+            L.or_min_radius_curvature.argtypes = [C.c_float, C.c_float]
+            _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def math_batch(fn, a, b=None):
+    """fn 0: atan2(a, b), 1: acos(a), 2: atan(a) with the project FP32 math."""
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    bb = np.ascontiguousarray(b if b is not None else a, dtype=np.float32)
+    out = np.empty_like(a)
+    lib().or_math_batch(fn, _ptr(a), _ptr(bb), _ptr(out), a.size)
+    return out
+
+
+def prefix_sum(values, wg):
+    a = np.ascontiguousarray(values, dtype=np.uint32).copy()
+    lib().or_prefix_sum(_ptr(a), a.size, wg)
+    return a
+
+
+def run(batch, cfg: TraxConfig, grid: TraxGridCfg, n_stages=4, n_threads=256, omp_threads=1):
+    """Runs the oracle on an EventBatch; returns a dict of numpy arrays."""
+    L = lib()
+    cols = [np.ascontiguousarray(c) for c in batch.columns()]
+    eo = np.ascontiguousarray(batch.event_offset, dtype=np.uint32)
+    ln = np.ascontiguousarray(batch.layer_nhits.reshape(-1), dtype=np.uint32)
+    lo = np.ascontiguousarray(batch.layer_offset.reshape(-1), dtype=np.uint32)
+    h = L.or_run(C.byref(cfg), C.byref(grid), *[_ptr(c) for c in cols], batch.n_hits,
+                 _ptr(eo), _ptr(ln), _ptr(lo), n_stages, n_threads, omp_threads)
+    if not h:
+        raise MemoryError("oracle allocation failed")
+    out = {}
+    try:
+        for i, name in enumerate(ITEMS):
+            n = int(L.or_size(h, i))
+            p = L.or_data(h, i)
+            dt = _DTYPES.get(name, np.uint32)
+            if not p or n == 0:
+                out[name] = np.zeros(0, dtype=dt)
+                continue
+            buf = (C.c_char * (n * np.dtype(dt).itemsize)).from_address(p)
+            out[name] = np.frombuffer(bytes(buf), dtype=dt).copy()
+    finally:
+        L.or_free(h)
+    out["stats"] = dict(zip(STATS, (int(v) for v in out["stats"])))
+    for k in ("pairs", "cands"):
+        out[k] = out[k].reshape(-1, 2)
+    return out
+
+
+def canonical(res):
+    """Drops unwritten slots; candidates become (hit1, hit2, hit3) rows."""
+    pv = res["pair_valid"].astype(bool)
+    pairs = res["pairs"][pv] if res["pairs"].size else res["pairs"]
+    cv = res["cand_valid"].astype(bool)
+    cands = res["cands"][cv] if res["cands"].size else res["cands"]
+    full = res["pairs"]
+    trip = np.stack([full[cands[:, 0], 0], full[cands[:, 0], 1], cands[:, 1]], axis=1) \
+        if cands.size else np.zeros((0, 3), np.uint32)
+    trk = np.stack([res["trk_h1"], res["trk_h2"], res["trk_h3"]], axis=1)
+    return {"pairs": pairs, "cand_hits": trip, "tracklets": trk}

@@ -1,0 +1,92 @@
+/*
+ * trax_oracle.h -- CPU restatement of trax's triplet-seeding path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
+ * CPU-baseline leg of bench.py may load this library; the product path never
+ * calls it.  It follows the reference kernels loop by loop (file:line cited
+ * at each function in trax_oracle.c), using the same project FP32 math
+ * (trax_gb300/csrc/trax_math.h) as the CUDA kernels.
+ *
+ * Parity status: parity unpinned.  The reference cannot be built or run in
+ * this environment (empty `clever` submodule, no OpenCL headers or device,
+ * no Boost, no protobuf-2.4 runtime) and its own tests hold no golden
+ * vectors for this path.  The oracle is pinned only by the reference's two
+ * self-checks -- the all-ones scan (src/trax_test/trax_test.cpp:473-479) and
+ * the GridBuilder::verifyGrid invariants (GridBuilder.cpp:187-224) -- and by
+ * hand-derived known-answer events in tests/.
+ */
+#ifndef TRAX_ORACLE_H
+#define TRAX_ORACLE_H
+
+#include <stdint.h>
+#include "../include/trax.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum or_item {
+    OR_SORTED_X = 0, OR_SORTED_Y, OR_SORTED_Z, OR_SORTED_PHI,
+    OR_SORTED_LAYER, OR_SORTED_DET, OR_SORTED_HITID, OR_SORTED_EVENT, OR_SORTED_ORIG,
+    OR_GRID,
+    OR_PAIRS,          /* uint32[2*slots] in the reference's slot layout */
+    OR_PAIR_VALID,     /* uint8[slots]: 0 marks a slot pairStore leaves unwritten */
+    OR_PAIR_OFFSETS,   /* uint32[E*T+1] */
+    OR_CANDS,
+    OR_CAND_VALID,
+    OR_CAND_OFFSETS,
+    OR_TRK_H1, OR_TRK_H2, OR_TRK_H3,
+    OR_TRK_OFFSETS,
+    OR_STATS,          /* uint64[OR_NSTATS] */
+    OR_NITEMS
+};
+
+enum or_stat {
+    ORS_STATUS = 0,        /* trax_status of the first fault */
+    ORS_DETAIL,            /* TRAX_DETAIL_* */
+    ORS_PAIR_SLOTS,        /* pairCount total (reference Pairing size) */
+    ORS_PAIRS,             /* distinct pairs written */
+    ORS_CAND_SLOTS,        /* predictCount total */
+    ORS_CANDS,             /* candidates written */
+    ORS_CAND_TRUNCATED,    /* store-window accepts beyond the count */
+    ORS_TRACKLETS,
+    OR_NSTATS
+};
+
+typedef struct or_result or_result;
+
+/*
+ * Runs stages 1..n_stages (1 grid, 2 pairs, 3 predict, 4 filter) on host
+ * arrays.  n_threads is the reference's work-group size (exec.threads), which
+ * fixes the pair slot layout and the scan blocking.  n_omp_threads > 1
+ * parallelises over segments, groups and candidates with identical results.
+ * Returns NULL only on allocation failure.
+ */
+or_result *or_run(const trax_config *cfg, const trax_grid_cfg *grid,
+                  const float *x, const float *y, const float *z,
+                  const uint32_t *layer, const uint32_t *det, const uint32_t *hitid,
+                  const uint32_t *event, uint32_t n_hits,
+                  const uint32_t *event_offset, const uint32_t *layer_nhits,
+                  const uint32_t *layer_offset, int n_stages, uint32_t n_threads,
+                  int n_omp_threads);
+uint64_t or_size(const or_result *r, int item);  /* elements */
+const void *or_data(const or_result *r, int item);
+void or_free(or_result *r);
+
+/* PrefixSum::run restated (PrefixSum.cpp:35-126, PrefixSum.h:55-245):
+ * in-place exclusive scan by recursive work-group scans. */
+void or_prefix_sum(uint32_t *data, uint32_t n, uint32_t wg);
+
+/* Project math, exported so tests can compare against libm / CUDA. */
+float or_atan2f(float y, float x);
+float or_acosf(float x);
+float or_atanf(float x);
+float or_min_radius_curvature(float min_pt, float bz);
+/* fn 0: atan2(a, b), 1: acos(a), 2: atan(a), over n floats. */
+void or_math_batch(int fn, const float *a, const float *b, float *out, uint64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

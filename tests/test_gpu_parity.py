@@ -1,0 +1,191 @@
+"""GPU parity: the sm_103a path through the C-ABI against the CPU oracle.
+
+Bar: bit-exact.  Grid, sorted hit columns (float bits), pairs, candidates
+(as hit triples), tracklets and all per-(event, layer triplet) offsets must
+equal the oracle's, element for element; the reference's slot counts
+(pairCount / predictCount totals) must match too.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from trax_gb300 import gen
+from trax_gb300.ops import build_triplets, Pipeline
+
+pytestmark = pytest.mark.gpu
+
+CASES = [("single-muon-100trk", 1), ("single-muon-100trk", 5), ("multimuon-1000trk", 1),
+         ("multimuon-1000trk", 3), ("pileup50-batch100", 3)]
+
+
+def gpu_stages(ctx, b, w):
+    hits, grid, pairs, cands, trk = build_triplets(ctx, b, w.config(), w.n_sectors_z,
+                                                   w.n_sectors_phi)
+    out = {"grid": grid.download(), "sorted": hits.download(), "pairs": pairs.get_pairings(),
+           "pair_offsets": pairs.get_pairing_offsets(), "cands": cands.get_pairings(),
+           "cand_offsets": cands.get_pairing_offsets(), "trk": trk.hits(),
+           "trk_offsets": trk.get_tracklet_offsets(), "pair_counts": pairs_counts(pairs),
+           "counts": None}
+    return out
+
+
+def pairs_counts(p):
+    return p.count
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def cand_hits(pairs, cands):
+    if cands.size == 0:
+        return np.zeros((0, 3), np.uint32)
+    return np.stack([pairs[cands[:, 0], 0], pairs[cands[:, 0], 1], cands[:, 1]], axis=1)
+
+
+@pytest.mark.parametrize("name,n_ev", CASES)
+def test_stage_parity_bit_exact(gpu_ctx, name, n_ev):
+    w = gen.WORKLOADS[name]
+    b = gen.generate_batch(w, n_ev)
+    cfg, g = w.config(), w.grid(n_ev)
+    r = oracle.run(b, cfg, g, 4, n_threads=1)
+    assert r["stats"]["status"] == 0
+    oc = oracle.canonical(r)
+    d = gpu_stages(gpu_ctx, b, w)
+
+    assert np.array_equal(d["grid"], r["grid"])
+    srt = d["sorted"]
+    for col, key in (("x", "sorted_x"), ("y", "sorted_y"), ("z", "sorted_z"),
+                     ("phi", "sorted_phi")):
+        assert np.array_equal(bits(srt[col]), bits(r[key])), col
+    for col, key in (("layer", "sorted_layer"), ("detector_id", "sorted_det"),
+                     ("hit_id", "sorted_hitid"), ("event", "sorted_event"),
+                     ("orig", "sorted_orig")):
+        assert np.array_equal(srt[col], r[key]), col
+
+    assert np.array_equal(d["pairs"], oc["pairs"])
+    st = r["stats"]
+    assert st["pairs"] == st["pair_slots"]
+    assert np.array_equal(d["pair_offsets"], r["pair_offsets"])
+
+    assert np.array_equal(cand_hits(d["pairs"], d["cands"]), oc["cand_hits"])
+    if st["cands"] == st["cand_slots"]:
+        assert np.array_equal(d["cand_offsets"], r["cand_offsets"])
+
+    assert np.array_equal(d["trk"], oc["tracklets"])
+    assert np.array_equal(d["trk_offsets"], r["trk_offsets"])
+    assert len(d["trk"]) > 0
+
+
+@pytest.mark.parametrize("name,n_ev", [("multimuon-1000trk", 2), ("pileup50-batch100", 2)])
+def test_sets_equal_reference_thread_layout(gpu_ctx, name, n_ev):
+    """Against the reference's default work-group size (256 threads, strided
+    pair slots) the GPU's pair, candidate and tracklet sets are equal."""
+    w = gen.WORKLOADS[name]
+    b = gen.generate_batch(w, n_ev)
+    r = oracle.run(b, w.config(), w.grid(n_ev), 4, n_threads=256)
+    oc = oracle.canonical(r)
+    d = gpu_stages(gpu_ctx, b, w)
+    as_set = lambda a: set(map(tuple, np.asarray(a).tolist()))
+    assert as_set(d["pairs"]) == as_set(oc["pairs"])
+    assert as_set(cand_hits(d["pairs"], d["cands"])) == as_set(oc["cand_hits"])
+    assert as_set(d["trk"]) == as_set(oc["tracklets"])
+    assert np.array_equal(d["trk_offsets"], r["trk_offsets"])
+
+
+def test_device_math_bit_exact(gpu_ctx):
+    """The device evaluates trax_math.h to the same bits as the host."""
+    import ctypes as C
+    rng = np.random.default_rng(5)
+    n = 1 << 20
+    a = np.concatenate([rng.normal(0, 10, n - 12).astype(np.float32),
+                        np.array([0, -0.0, 1, -1, np.inf, -np.inf, np.nan, 1e-40, -1e-40,
+                                  3e38, -3e38, 0.5], np.float32)])
+    bb = rng.normal(0, 10, n).astype(np.float32)
+    u = rng.uniform(-1.05, 1.05, n).astype(np.float32)
+    da, db, du = gpu_ctx.upload(a), gpu_ctx.upload(bb), gpu_ctx.upload(u)
+    out = gpu_ctx.alloc(n, np.float32)
+    for fn, x, y in ((0, da, db), (1, du, du), (2, da, da)):
+        gpu_ctx._check(gpu_ctx.lib.trax_eval_math(gpu_ctx.h, fn, x.ptr, y.ptr, out.ptr, n))
+        got = out.download(n)
+        host = oracle.math_batch(fn, a if fn != 1 else u, bb if fn == 0 else None)
+        assert np.array_equal(bits(got), bits(host)), fn
+
+
+def test_batched_pipeline_equals_stages(gpu_ctx):
+    w = gen.WORKLOADS["pileup50-batch100"]
+    b = gen.generate_batch(w, 4)
+    d = gpu_stages(gpu_ctx, b, w)
+    p = Pipeline(gpu_ctx, w.config(), w.grid(8), max_events=8, max_hits=b.n_hits * 2,
+                 max_pairs=4 * len(d["pairs"]) + 1024, max_candidates=4 * len(d["cands"]) + 1024,
+                 max_tracklets=4 * len(d["trk"]) + 1024)
+    for _ in range(2):  # second call replays the captured graph
+        trk, off, counts = p.seed(b)
+        assert counts["status"] == 0
+        assert np.array_equal(trk, d["trk"])
+        assert np.array_equal(off, d["trk_offsets"])
+    trk_in, _, _ = p.seed(b, input_indices=True)
+    assert np.array_equal(trk_in, d["sorted"]["orig"][d["trk"]])
+
+
+def test_event_alone_equals_event_in_batch(gpu_ctx):
+    """Serving determinism: an event's tracklets (as input hit positions
+    within the event) are the same alone and inside a batch."""
+    w = gen.WORKLOADS["multimuon-1000trk"]
+    b = gen.generate_batch(w, 4)
+    T = w.n_triplets
+    p = Pipeline(gpu_ctx, w.config(), w.grid(4), max_events=4, max_hits=b.n_hits,
+                 max_pairs=200_000, max_candidates=200_000, max_tracklets=50_000)
+    trk, off, _ = p.seed(b, input_indices=True)
+    eoff = b.event_offset
+    for e in range(4):
+        one = b.slice_events(e, 1)
+        t1, off1, _ = p.seed(one, input_indices=True)
+        lo, hi = off[e * T], off[(e + 1) * T]
+        assert np.array_equal(trk[lo:hi] - eoff[e], t1)
+        assert np.array_equal(off[e * T:(e + 1) * T + 1] - off[e * T], off1)
+
+
+def test_empty_batch(gpu_ctx):
+    w = gen.WORKLOADS["single-muon-100trk"]
+    b = gen.generate_batch(w, 2)
+    empty = gen.EventBatch(b.x[:0], b.y[:0], b.z[:0], b.layer[:0], b.detector_id[:0],
+                           b.hit_id[:0], b.event[:0], np.zeros((2, 3), np.uint32))
+    d = gpu_stages(gpu_ctx, empty, w)
+    assert len(d["trk"]) == 0 and len(d["pairs"]) == 0
+    assert d["trk_offsets"].tolist() == [0, 0, 0]
+
+
+def test_capacity_overflow_is_reported_not_written(gpu_ctx):
+    from trax_gb300.ops import PairGeneratorBeamspot, HitCollection, Grid, GridBuilder, supplements
+    w = gen.WORKLOADS["multimuon-1000trk"]
+    b = gen.generate_batch(w, 1)
+    cfg = w.config()
+    gpu_ctx.configure(cfg)
+    hits = HitCollection(gpu_ctx, b)
+    es, ls = supplements(b)
+    grid = Grid(gpu_ctx, 1, w.n_layers, w.n_sectors_z, w.n_sectors_phi)
+    GridBuilder(gpu_ctx).run(hits, 256, es, ls, grid)
+    op = PairGeneratorBeamspot(gpu_ctx)
+    pairs = op.run(hits, cfg, 256, cfg, grid, capacity=100)  # grows after overflow
+    r = oracle.run(b, cfg, w.grid(1), 2, n_threads=1)
+    assert pairs.capacity >= pairs.count == r["stats"]["pairs"]
+    assert np.array_equal(pairs.get_pairings(), oracle.canonical(r)["pairs"])
+
+
+def test_bad_hit_flagged_without_fault(gpu_ctx):
+    w = gen.WORKLOADS["single-muon-100trk"]
+    b = gen.generate_batch(w, 1)
+    b.z[5] = np.float32(400.0)  # outside the -300..300 cm grid
+    d_ctx = gpu_ctx
+    from trax_gb300.ops import HitCollection, Grid, GridBuilder, supplements
+    d_ctx.configure(w.config())
+    d_ctx.reset_counts()
+    hits = HitCollection(d_ctx, b)
+    es, ls = supplements(b)
+    grid = Grid(d_ctx, 1, w.n_layers, w.n_sectors_z, w.n_sectors_phi)
+    GridBuilder(d_ctx).run(hits, 256, es, ls, grid)
+    c = d_ctx.counts()
+    assert c["status"] == 6 and c["error_detail"] == 1
+    d_ctx.reset_counts()
+    assert d_ctx.counts()["status"] == 0

@@ -1,0 +1,966 @@
+/*
+ * trax_capi.cu -- the C-ABI of include/trax.h over the sm_103a kernels.
+ *
+ * The four stage entry points mirror the reference's operator methods
+ * (GridBuilder::run, PairGeneratorBeamspot::run, TripletThetaPhiPredictor::run,
+ * TripletThetaPhiFilter::run) but never synchronise: every size the
+ * reference downloads to the host to allocate the next buffer
+ * (PairGeneratorBeamspot.cpp:120, TripletThetaPhiPredictor.cpp:59,
+ * TripletThetaPhiFilter.cpp:82) stays on the device, and outputs are bounded
+ * by caller capacities.  The batched pipeline runs the same kernels from one
+ * CUDA graph.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "trax_kernels.cuh"
+
+using namespace trax;
+
+namespace {
+
+constexpr int kTimerSlots = 64;
+constexpr int kScanItems = 8;       /* items per thread in k_scan */
+constexpr int kScanThreads = 256;
+constexpr int kFilterItems = 4;
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct trax_ctx {
+    int device = 0;
+    int sm_count = 0;
+    size_t smem_optin = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    bool configured = false;
+    trax_config cfg{};
+    KParams kp{};
+    DevState *d_state = nullptr;
+    DevState *h_state = nullptr;          /* pinned mirror */
+    uint32_t *h_stage = nullptr;          /* pinned staging for small uploads */
+    size_t h_stage_words = 0;
+    cudaEvent_t stage_free = nullptr;     /* last upload from h_stage done */
+    DevBuf seg, g_start, g_base, slots, pcnt, pexcl, ccnt, cexcl, st0, st1, st2;
+    cudaEvent_t timers[kTimerSlots] = {};
+    int blk_pair = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
+
+    /* batched pipeline */
+    bool reserved = false;
+    uint32_t r_events = 0, r_layers = 0, r_hits = 0, r_pairs = 0, r_cands = 0, r_trk = 0;
+    trax_grid_cfg r_grid{};
+    DevBuf in_cols[7], srt_cols[9], grid_buf, pairs_buf, pair_off, cands_buf, cand_off;
+    DevBuf trk_cols[3], trk_off, trk_map[3], r_seg;
+    uint32_t gb_C = 0;                    /* cached k_grid_build launch plan */
+    int gb_warps = 0, gb_per_sm = 0;
+    cudaGraphExec_t graph = nullptr;
+    uint32_t staged_events = 0, staged_hits = 0;
+};
+
+namespace {
+
+trax_status fail(trax_ctx *c, trax_status s, const std::string &msg)
+{
+    if (c) c->err = msg;
+    return s;
+}
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return fail(ctx, TRAX_ERR_DEVICE, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+trax_status ensure(trax_ctx *ctx, DevBuf &b, size_t bytes)
+{
+    if (bytes == 0) bytes = 16;
+    if (b.bytes >= bytes) return TRAX_OK;
+    if (ctx->reserved && ctx->graph) {
+        /* buffers captured in the graph must not move */
+        return fail(ctx, TRAX_ERR_OOM, "scratch beyond the reserved size");
+    }
+    if (b.p) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        CK(cudaFree(b.p));
+        b.p = nullptr;
+        b.bytes = 0;
+    }
+    size_t want = bytes + bytes / 4;
+    cudaError_t e = cudaMalloc(&b.p, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, TRAX_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    b.bytes = want;
+    return TRAX_OK;
+}
+
+trax_status ensure_stage(trax_ctx *ctx, size_t words)
+{
+    if (ctx->stage_free) CK(cudaEventSynchronize(ctx->stage_free));
+    if (ctx->h_stage_words >= words) return TRAX_OK;
+    if (ctx->h_stage) CK(cudaFreeHost(ctx->h_stage));
+    ctx->h_stage = nullptr;
+    size_t want = std::max<size_t>(words + words / 4, 1024);
+    CK(cudaMallocHost(&ctx->h_stage, want * 4));
+    ctx->h_stage_words = want;
+    return TRAX_OK;
+}
+
+uint32_t tiles_for(uint32_t n, uint32_t per) { return (n + per - 1) / per + 1; }
+
+void fill_grid_params(KParams &kp, const trax_grid_cfg *g)
+{
+    kp.n_layers = g->n_layers;
+    kp.nz = g->n_sectors_z;
+    kp.nphi = g->n_sectors_phi;
+    kp.C = (g->n_sectors_z + 1) * (g->n_sectors_phi + 1);
+    kp.sz_z = trax_sector_size_z(g->n_sectors_z);
+    kp.sz_phi = trax_sector_size_phi(g->n_sectors_phi);
+}
+
+trax_status check_grid(trax_ctx *ctx, const trax_grid_cfg *g)
+{
+    if (!ctx->configured) return fail(ctx, TRAX_ERR_BAD_ARG, "trax_configure not called");
+    if (!g || g->n_sectors_z == 0 || g->n_sectors_phi == 0 || g->n_layers == 0 ||
+        g->n_layers > TRAX_MAX_LAYERS)
+        return fail(ctx, TRAX_ERR_BAD_ARG, "bad grid configuration");
+    if ((uint64_t)(g->n_sectors_z + 1) * (g->n_sectors_phi + 1) > 65536)
+        return fail(ctx, TRAX_ERR_BAD_ARG, "grid has more than 65536 cells per layer");
+    for (uint32_t i = 0; i < ctx->cfg.n_layer_triplets; ++i) {
+        const trax_layer_triplet &t = ctx->cfg.triplets[i];
+        if (t.layer1 > g->n_layers || t.layer2 > g->n_layers || t.layer3 > g->n_layers)
+            return fail(ctx, TRAX_ERR_BAD_ARG, "layer triplet uses a layer outside the grid");
+    }
+    return TRAX_OK;
+}
+
+/* Dynamic shared memory plan of k_grid_build: W warps with (W+1)*C words. */
+int grid_build_warps(const trax_ctx *ctx, uint32_t C)
+{
+    const size_t budget = std::min<size_t>(ctx->smem_optin, 200 * 1024);
+    long w = (long)(budget / (4ull * C)) - 1;
+    if (w > 32) w = 32;
+    if (w > 16 && C > 2048) w = 16;
+    return (int)w;
+}
+
+/* Warps and resident CTAs of k_grid_build for C cells; computed outside
+ * any stream capture and cached. */
+trax_status grid_plan(trax_ctx *ctx, uint32_t C)
+{
+    if (ctx->gb_C == C && ctx->gb_warps > 0) return TRAX_OK;
+    const int W = grid_build_warps(ctx, C);
+    if (W < 1) return fail(ctx, TRAX_ERR_BAD_ARG, "grid too large for shared memory");
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_grid_build, W * 32,
+                                                     (size_t)(W + 1) * C * 4));
+    ctx->gb_C = C;
+    ctx->gb_warps = W;
+    ctx->gb_per_sm = per_sm < 1 ? 1 : per_sm;
+    return TRAX_OK;
+}
+
+trax_status set_sizes(trax_ctx *ctx, uint32_t n_events, uint32_t n_hits)
+{
+    trax_status s = ensure_stage(ctx, 2);
+    if (s != TRAX_OK) return s;
+    ctx->h_stage[0] = n_events;
+    ctx->h_stage[1] = n_hits;
+    CK(cudaMemcpyAsync(ctx->d_state, ctx->h_stage, 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaEventRecord(ctx->stage_free, ctx->stream));
+    return TRAX_OK;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Stage enqueue functions shared by the stage API and the graph pipeline. */
+
+trax_status enqueue_grid(trax_ctx *ctx, const InCols &in, const SortedCols &out,
+                         const uint32_t *seg_start, const uint32_t *seg_n, uint32_t *grid,
+                         uint32_t max_segs)
+{
+    const KParams &kp = ctx->kp;
+    trax_status s = grid_plan(ctx, kp.C);
+    if (s != TRAX_OK) return s;
+    const int W = ctx->gb_warps, per_sm = ctx->gb_per_sm;
+    const size_t smem = (size_t)(W + 1) * kp.C * 4;
+    uint32_t blocks = std::min<uint32_t>(max_segs, (uint32_t)(ctx->sm_count * per_sm));
+    if (blocks == 0) blocks = 1;
+    k_grid_build<<<blocks, W * 32, smem, ctx->stream>>>(kp, in, out, seg_start, seg_n, grid,
+                                                        ctx->d_state);
+    CK(cudaGetLastError());
+    return TRAX_OK;
+}
+
+trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *grid, uint2 *pairs,
+                          uint32_t *pair_offsets, uint32_t pair_cap, uint32_t slot_cap,
+                          uint32_t max_groups)
+{
+    const KParams &kp = ctx->kp;
+    trax_status s;
+    if ((s = ensure(ctx, ctx->g_start, (size_t)max_groups * 4)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->g_base, (size_t)(max_groups + 1) * 4)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->slots, (size_t)slot_cap * 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->pcnt, (size_t)slot_cap * 4)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->pexcl, (size_t)(slot_cap + 1) * 4)) != TRAX_OK) return s;
+    const uint32_t ntile = tiles_for(slot_cap, kScanThreads * kScanItems);
+    if ((s = ensure(ctx, ctx->st0, (size_t)ntile * 8)) != TRAX_OK) return s;
+    uint32_t *g_start = (uint32_t *)ctx->g_start.p, *g_base = (uint32_t *)ctx->g_base.p;
+    uint2 *slots = (uint2 *)ctx->slots.p;
+    uint32_t *pcnt = (uint32_t *)ctx->pcnt.p, *pexcl = (uint32_t *)ctx->pexcl.p;
+    DevState *st = ctx->d_state;
+
+    k_pair_groups<<<1, 1024, 0, ctx->stream>>>(kp, grid, g_start, g_base, st);
+    k_pair_slots<<<ctx->blk_small, 256, 0, ctx->stream>>>(kp, g_start, g_base, slots, slot_cap, st);
+    k_pair<false><<<ctx->blk_pair, 256, 0, ctx->stream>>>(kp, grid, h.x, h.y, h.z, h.phi, slots,
+                                                          slot_cap, pcnt, nullptr, nullptr, 0, st);
+    CK(cudaMemsetAsync(&st->tile_ctr[0], 0, 4, ctx->stream));
+    CK(cudaMemsetAsync(ctx->st0.p, 0, (size_t)ntile * 8, ctx->stream));
+    k_scan<kScanItems><<<ctx->blk_scan, kScanThreads, 0, ctx->stream>>>(
+        pcnt, pexcl, &st->n_outer, slot_cap, &st->n_pairs, 0,
+        (unsigned long long *)ctx->st0.p, st);
+    k_group_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(g_base, pexcl, pair_offsets, kp.n_lt,
+                                                             slot_cap, &st->n_pairs, pair_cap,
+                                                             TRAX_DETAIL_PAIR_CAPACITY, st);
+    k_pair<true><<<ctx->blk_pair, 256, 0, ctx->stream>>>(kp, grid, h.x, h.y, h.z, h.phi, slots,
+                                                         slot_cap, nullptr, pexcl, pairs, pair_cap,
+                                                         st);
+    CK(cudaGetLastError());
+    return TRAX_OK;
+}
+
+trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *grid,
+                            const uint2 *pairs, const uint32_t *pair_offsets, uint32_t pair_cap,
+                            uint2 *cands, uint32_t *cand_offsets, uint32_t cand_cap,
+                            uint32_t max_groups)
+{
+    const KParams &kp = ctx->kp;
+    trax_status s;
+    if ((s = ensure(ctx, ctx->ccnt, (size_t)pair_cap * 4)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->cexcl, (size_t)(pair_cap + 1) * 4)) != TRAX_OK) return s;
+    const uint32_t ntile = tiles_for(pair_cap, kScanThreads * kScanItems);
+    if ((s = ensure(ctx, ctx->st1, (size_t)ntile * 8)) != TRAX_OK) return s;
+    uint32_t *ccnt = (uint32_t *)ctx->ccnt.p, *cexcl = (uint32_t *)ctx->cexcl.p;
+    DevState *st = ctx->d_state;
+    /* the pair total is st->n_pairs: written by the pair scan, or copied
+     * from pair_offsets[G] by trax_triplet_predict */
+    k_predict<false><<<ctx->blk_pred, 256, 0, ctx->stream>>>(
+        kp, grid, h.x, h.y, h.z, h.phi, h.event, h.layer, pairs, &st->n_pairs, pair_cap, ccnt,
+        nullptr, nullptr, 0, st);
+    CK(cudaMemsetAsync(&st->tile_ctr[1], 0, 4, ctx->stream));
+    CK(cudaMemsetAsync(ctx->st1.p, 0, (size_t)ntile * 8, ctx->stream));
+    k_scan<kScanItems><<<ctx->blk_scan, kScanThreads, 0, ctx->stream>>>(
+        ccnt, cexcl, &st->n_pairs, pair_cap, &st->n_cands, 1,
+        (unsigned long long *)ctx->st1.p, st);
+    k_cand_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(pair_offsets, cexcl, cand_offsets,
+                                                            kp.n_lt, pair_cap, &st->n_cands,
+                                                            cand_cap, st);
+    k_predict<true><<<ctx->blk_pred, 256, 0, ctx->stream>>>(
+        kp, grid, h.x, h.y, h.z, h.phi, h.event, h.layer, pairs, &st->n_pairs, pair_cap, nullptr,
+        cexcl, cands, cand_cap, st);
+    CK(cudaGetLastError());
+    return TRAX_OK;
+}
+
+trax_status enqueue_filter(trax_ctx *ctx, const SortedCols &h, const uint2 *pairs,
+                           const uint2 *cands, uint32_t cand_cap, uint32_t *t1, uint32_t *t2,
+                           uint32_t *t3, uint32_t *trk_offsets, uint32_t trk_cap,
+                           uint32_t max_groups)
+{
+    const KParams &kp = ctx->kp;
+    trax_status s;
+    const uint32_t ntile = tiles_for(cand_cap, 256 * kFilterItems);
+    if ((s = ensure(ctx, ctx->st2, (size_t)ntile * 8)) != TRAX_OK) return s;
+    DevState *st = ctx->d_state;
+    CK(cudaMemsetAsync(&st->tile_ctr[2], 0, 4, ctx->stream));
+    CK(cudaMemsetAsync(ctx->st2.p, 0, (size_t)ntile * 8, ctx->stream));
+    CK(cudaMemsetAsync(trk_offsets, 0, (size_t)(max_groups + 1) * 4, ctx->stream));
+    k_filter<<<ctx->blk_filter, 256, 0, ctx->stream>>>(kp, h.x, h.y, h.z, h.layer, pairs, cands,
+                                                       &st->n_cands, cand_cap, t1, t2, t3, trk_cap,
+                                                       (unsigned long long *)ctx->st2.p, st);
+    k_trk_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(t1, h.event, h.layer, trk_offsets,
+                                                           kp.n_lt, trk_cap, st);
+    k_monotonize<<<1, 1024, 0, ctx->stream>>>(trk_offsets, kp.n_lt, st);
+    CK(cudaGetLastError());
+    return TRAX_OK;
+}
+
+SortedCols sorted_from(const trax_sorted_hits *o)
+{
+    SortedCols s;
+    s.x = o->x; s.y = o->y; s.z = o->z; s.phi = o->phi;
+    s.layer = o->layer; s.det = o->detector_id; s.hitid = o->hit_id; s.event = o->event;
+    s.orig = o->orig;
+    return s;
+}
+
+trax_status build_segments(trax_ctx *ctx, const trax_layout *lay, uint32_t n_hits,
+                           uint32_t **d_start, uint32_t **d_n)
+{
+    const uint32_t E = lay->n_events, L = lay->n_layers;
+    const size_t nseg = (size_t)E * L;
+    trax_status s = ensure_stage(ctx, 2 * nseg + 2);
+    if (s != TRAX_OK) return s;
+    uint32_t *hs = ctx->h_stage, *hn = ctx->h_stage + nseg;
+    uint64_t run = 0;
+    for (uint32_t e = 0; e < E; ++e) {
+        if (lay->event_offset && lay->event_offset[e] != run)
+            return fail(ctx, TRAX_ERR_BAD_INPUT, "event offsets are not the running hit count");
+        uint64_t in_event = 0;
+        for (uint32_t l = 0; l < L; ++l) {
+            const uint32_t n = lay->layer_nhits[(size_t)e * L + l];
+            if (lay->layer_offset && lay->layer_offset[(size_t)e * L + l] != in_event)
+                return fail(ctx, TRAX_ERR_BAD_INPUT, "layer offsets are not the running hit count");
+            hs[(size_t)e * L + l] = (uint32_t)run;
+            hn[(size_t)e * L + l] = n;
+            run += n;
+            in_event += n;
+        }
+        if (lay->event_nhits && lay->event_nhits[e] != in_event)
+            return fail(ctx, TRAX_ERR_BAD_INPUT, "event hit count differs from its layers' sum");
+    }
+    if (run != n_hits) return fail(ctx, TRAX_ERR_BAD_INPUT, "layout does not cover the hits");
+    if ((s = ensure(ctx, ctx->seg, nseg * 8 + 8)) != TRAX_OK) return s;
+    CK(cudaMemcpyAsync(ctx->seg.p, ctx->h_stage, nseg * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaEventRecord(ctx->stage_free, ctx->stream));
+    *d_start = (uint32_t *)ctx->seg.p;
+    *d_n = (uint32_t *)ctx->seg.p + nseg;
+    return TRAX_OK;
+}
+
+}  // namespace
+
+/* ====================================================================== */
+
+namespace {
+
+__global__ void k_eval_math(int fn, const float *a, const float *b, float *out, uint32_t n)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = fn == 0 ? trax_atan2f(a[i], b[i]) : fn == 1 ? trax_acosf(a[i]) : trax_atanf(a[i]);
+}
+
+std::string g_validate_msg;
+
+}  // namespace
+
+extern "C" {
+
+const char *trax_version(void) { return "trax-gb300 1 (sm_103a)"; }
+
+trax_status trax_config_validate(const trax_config *cfg, const trax_grid_cfg *grid)
+{
+    if (!cfg) return TRAX_ERR_BAD_ARG;
+    if (cfg->n_layer_triplets == 0 || cfg->n_layer_triplets > TRAX_MAX_LAYER_TRIPLETS)
+        return TRAX_ERR_BAD_ARG;
+    if (cfg->n_geom_layers == 0 || cfg->n_geom_layers > TRAX_MAX_LAYERS) return TRAX_ERR_BAD_ARG;
+    if (!(cfg->min_pt > 0.0f)) return TRAX_ERR_BAD_ARG;
+    for (uint32_t i = 0; i < cfg->n_layer_triplets; ++i) {
+        const trax_layer_triplet &t = cfg->triplets[i];
+        /* the triplet index is derived from the innermost hit's layer
+         * (TripletThetaPhiPredictor.h:79, TripletThetaPhiFilter.h:73) */
+        if (t.layer1 != i + 1) return TRAX_ERR_BAD_ARG;
+        if (t.layer2 == 0 || t.layer3 == 0 || t.layer2 > cfg->n_geom_layers ||
+            t.layer3 > cfg->n_geom_layers || t.layer1 > cfg->n_geom_layers)
+            return TRAX_ERR_BAD_ARG;
+        if (grid && (t.layer1 > grid->n_layers || t.layer2 > grid->n_layers ||
+                     t.layer3 > grid->n_layers))
+            return TRAX_ERR_BAD_ARG;
+    }
+    if (grid) {
+        if (grid->n_sectors_z == 0 || grid->n_sectors_phi == 0 || grid->n_layers == 0 ||
+            grid->n_layers > TRAX_MAX_LAYERS)
+            return TRAX_ERR_BAD_ARG;
+        if ((uint64_t)(grid->n_sectors_z + 1) * (grid->n_sectors_phi + 1) > 65536)
+            return TRAX_ERR_BAD_ARG;
+    }
+    return TRAX_OK;
+}
+
+trax_status trax_layout_validate(const trax_layout *lay, uint32_t n_hits)
+{
+    if (!lay || !lay->layer_nhits) return TRAX_ERR_BAD_ARG;
+    const uint32_t E = lay->n_events, L = lay->n_layers;
+    uint64_t run = 0;
+    for (uint32_t e = 0; e < E; ++e) {
+        if (lay->event_offset && lay->event_offset[e] != run) return TRAX_ERR_BAD_INPUT;
+        uint64_t in_event = 0;
+        for (uint32_t l = 0; l < L; ++l) {
+            if (lay->layer_offset && lay->layer_offset[(size_t)e * L + l] != in_event)
+                return TRAX_ERR_BAD_INPUT;
+            in_event += lay->layer_nhits[(size_t)e * L + l];
+        }
+        if (lay->event_nhits && lay->event_nhits[e] != in_event) return TRAX_ERR_BAD_INPUT;
+        run += in_event;
+    }
+    return run == n_hits ? TRAX_OK : TRAX_ERR_BAD_INPUT;
+}
+
+size_t trax_abi_sizeof(const char *name)
+{
+    if (!name) return 0;
+    const struct { const char *n; size_t s; } t[] = {
+        {"trax_grid_cfg", sizeof(trax_grid_cfg)}, {"trax_layer_triplet", sizeof(trax_layer_triplet)},
+        {"trax_config", sizeof(trax_config)}, {"trax_hits", sizeof(trax_hits)},
+        {"trax_sorted_hits", sizeof(trax_sorted_hits)}, {"trax_layout", sizeof(trax_layout)},
+        {"trax_pairs", sizeof(trax_pairs)}, {"trax_tracklets", sizeof(trax_tracklets)},
+        {"trax_counts", sizeof(trax_counts)}, {"trax_event_batch", sizeof(trax_event_batch)},
+        {"trax_batch_result", sizeof(trax_batch_result)}};
+    for (const auto &e : t)
+        if (strcmp(e.n, name) == 0) return e.s;
+    return 0;
+}
+
+trax_status trax_eval_math(trax_ctx *ctx, int fn, const float *d_a, const float *d_b,
+                           float *d_out, uint32_t n)
+{
+    if (!ctx || fn < 0 || fn > 2 || !d_a || !d_out || (fn == 0 && !d_b)) return TRAX_ERR_BAD_ARG;
+    if (n == 0) return TRAX_OK;
+    k_eval_math<<<ctx->blk_small, 256, 0, ctx->stream>>>(fn, d_a, d_b, d_out, n);
+    CK(cudaGetLastError());
+    return TRAX_OK;
+}
+
+float trax_min_radius_curvature(float min_pt, float bz)
+{
+    /* TripletConfiguration.cpp:145-152 in double, returned as float. */
+    const double Q = 1.602177E-19;
+    const double GEV_C = 5.344286E-19;
+    if (bz == 0.0f) bz = (float)3.8112;
+    return (float)(min_pt * GEV_C / (bz * Q) * 1E2);
+}
+
+trax_status trax_ctx_create(trax_ctx **out, int device)
+{
+    if (!out) return TRAX_ERR_BAD_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return TRAX_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= n) return TRAX_ERR_BAD_ARG;
+    trax_ctx *ctx = new trax_ctx();
+    ctx->device = device;
+    auto bail = [&](cudaError_t e) {
+        (void)e;
+        delete ctx;
+        return TRAX_ERR_DEVICE;
+    };
+    cudaError_t e;
+    if ((e = cudaSetDevice(device)) != cudaSuccess) return bail(e);
+    if ((e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess) return bail(e);
+    int optin = 0;
+    if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device)) != cudaSuccess) return bail(e);
+    ctx->smem_optin = (size_t)optin;
+    if ((e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
+    ctx->stream = ctx->own_stream;
+    if ((e = cudaMalloc(&ctx->d_state, sizeof(DevState))) != cudaSuccess) return bail(e);
+    if ((e = cudaMemset(ctx->d_state, 0, sizeof(DevState))) != cudaSuccess) return bail(e);
+    if ((e = cudaMallocHost(&ctx->h_state, sizeof(DevState))) != cudaSuccess) return bail(e);
+    if ((e = cudaEventCreateWithFlags(&ctx->stage_free, cudaEventDisableTiming)) != cudaSuccess) return bail(e);
+    for (int i = 0; i < kTimerSlots; ++i)
+        if ((e = cudaEventCreate(&ctx->timers[i])) != cudaSuccess) return bail(e);
+    if ((e = cudaFuncSetAttribute(k_grid_build, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  optin)) != cudaSuccess) return bail(e);
+    int b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair<false>, 256, 0);
+    ctx->blk_pair = ctx->sm_count * std::max(b, 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_predict<false>, 256, 0);
+    ctx->blk_pred = ctx->sm_count * std::max(b, 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_filter, 256, 0);
+    ctx->blk_filter = ctx->sm_count * std::max(b, 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_scan<kScanItems>, kScanThreads, 0);
+    ctx->blk_scan = ctx->sm_count * std::max(b, 1);
+    ctx->blk_small = ctx->sm_count * 2;
+    if ((e = cudaGetLastError()) != cudaSuccess) return bail(e);
+    *out = ctx;
+    return TRAX_OK;
+}
+
+void trax_ctx_destroy(trax_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+    DevBuf *bufs[] = {&ctx->seg, &ctx->g_start, &ctx->g_base, &ctx->slots, &ctx->pcnt, &ctx->pexcl,
+                      &ctx->ccnt, &ctx->cexcl, &ctx->st0, &ctx->st1, &ctx->st2, &ctx->grid_buf,
+                      &ctx->pairs_buf, &ctx->pair_off, &ctx->cands_buf, &ctx->cand_off, &ctx->trk_off,
+                      &ctx->r_seg};
+    for (DevBuf *b : bufs) if (b->p) cudaFree(b->p);
+    for (auto &b : ctx->in_cols) if (b.p) cudaFree(b.p);
+    for (auto &b : ctx->srt_cols) if (b.p) cudaFree(b.p);
+    for (auto &b : ctx->trk_cols) if (b.p) cudaFree(b.p);
+    for (auto &b : ctx->trk_map) if (b.p) cudaFree(b.p);
+    if (ctx->d_state) cudaFree(ctx->d_state);
+    if (ctx->h_state) cudaFreeHost(ctx->h_state);
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    if (ctx->stage_free) cudaEventDestroy(ctx->stage_free);
+    for (auto &t : ctx->timers) if (t) cudaEventDestroy(t);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+}
+
+trax_status trax_ctx_set_stream(trax_ctx *ctx, void *stream)
+{
+    if (!ctx) return TRAX_ERR_BAD_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    if (ctx->graph) {
+        cudaGraphExecDestroy(ctx->graph);
+        ctx->graph = nullptr;
+    }
+    return TRAX_OK;
+}
+
+void *trax_ctx_get_stream(trax_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+const char *trax_ctx_last_error(const trax_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int trax_ctx_sm_count(const trax_ctx *ctx) { return ctx ? ctx->sm_count : 0; }
+
+trax_status trax_ctx_synchronize(trax_ctx *ctx)
+{
+    if (!ctx) return TRAX_ERR_BAD_ARG;
+    CK(cudaMemcpyAsync(&ctx->h_state->status, &ctx->d_state->status, 8, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return (trax_status)ctx->h_state->status;
+}
+
+trax_status trax_configure(trax_ctx *ctx, const trax_config *cfg)
+{
+    if (!ctx || !cfg) return TRAX_ERR_BAD_ARG;
+    if (trax_config_validate(cfg, nullptr) != TRAX_OK)
+        return fail(ctx, TRAX_ERR_BAD_ARG,
+                    "invalid configuration: 1..16 layer triplets, triplet i starting on layer "
+                    "i+1, geometry for every layer used, min_pt > 0");
+    ctx->cfg = *cfg;
+    KParams &kp = ctx->kp;
+    kp.n_lt = cfg->n_layer_triplets;
+    for (uint32_t i = 0; i < kMaxLT; ++i) {
+        const trax_layer_triplet &t = cfg->triplets[i < cfg->n_layer_triplets ? i : 0];
+        kp.l1[i] = t.layer1; kp.l2[i] = t.layer2; kp.l3[i] = t.layer3;
+        kp.dtheta[i] = t.dtheta_cut; kp.sigma_z[i] = t.sigma_z; kp.dphi[i] = t.dphi_cut;
+        kp.sigma_phi[i] = t.sigma_phi; kp.tip[i] = t.tip_cut; kp.z0[i] = t.z0;
+        kp.spread_phi[i] = t.pair_spread_phi;
+    }
+    for (uint32_t l = 0; l < kMaxLayers; ++l) {
+        kp.rmin[l] = l < cfg->n_geom_layers ? cfg->min_radius[l] : 0.0f;
+        kp.rmax[l] = l < cfg->n_geom_layers ? cfg->max_radius[l] : 0.0f;
+    }
+    kp.rmin_curv = trax_min_radius_curvature(cfg->min_pt, cfg->bz);
+    ctx->configured = true;
+    if (ctx->graph) {
+        cudaGraphExecDestroy(ctx->graph);
+        ctx->graph = nullptr;
+    }
+    return TRAX_OK;
+}
+
+trax_status trax_dev_alloc(trax_ctx *ctx, void **ptr, size_t bytes)
+{
+    if (!ctx || !ptr) return TRAX_ERR_BAD_ARG;
+    cudaError_t e = cudaMalloc(ptr, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, TRAX_ERR_OOM, cudaGetErrorString(e));
+    }
+    return TRAX_OK;
+}
+
+trax_status trax_dev_free(trax_ctx *ctx, void *ptr)
+{
+    if (!ctx) return TRAX_ERR_BAD_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaFree(ptr));
+    return TRAX_OK;
+}
+
+trax_status trax_host_alloc_pinned(trax_ctx *ctx, void **ptr, size_t bytes)
+{
+    if (!ctx || !ptr) return TRAX_ERR_BAD_ARG;
+    cudaError_t e = cudaMallocHost(ptr, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, TRAX_ERR_OOM, cudaGetErrorString(e));
+    }
+    return TRAX_OK;
+}
+
+trax_status trax_host_free_pinned(trax_ctx *ctx, void *ptr)
+{
+    if (!ctx) return TRAX_ERR_BAD_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaFreeHost(ptr));
+    return TRAX_OK;
+}
+
+trax_status trax_memcpy_h2d(trax_ctx *ctx, void *dst, const void *src, size_t bytes)
+{
+    if (!ctx) return TRAX_ERR_BAD_ARG;
+    if (bytes) CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    return TRAX_OK;
+}
+
+trax_status trax_memcpy_d2h(trax_ctx *ctx, void *dst, const void *src, size_t bytes)
+{
+    if (!ctx) return TRAX_ERR_BAD_ARG;
+    if (bytes) CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return TRAX_OK;
+}
+
+trax_status trax_memset_d(trax_ctx *ctx, void *dst, int value, size_t bytes)
+{
+    if (!ctx) return TRAX_ERR_BAD_ARG;
+    if (bytes) CK(cudaMemsetAsync(dst, value, bytes, ctx->stream));
+    return TRAX_OK;
+}
+
+trax_status trax_timer_record(trax_ctx *ctx, int slot)
+{
+    if (!ctx || slot < 0 || slot >= kTimerSlots) return TRAX_ERR_BAD_ARG;
+    CK(cudaEventRecord(ctx->timers[slot], ctx->stream));
+    return TRAX_OK;
+}
+
+trax_status trax_timer_elapsed_ms(trax_ctx *ctx, int a, int b, float *ms)
+{
+    if (!ctx || !ms || a < 0 || b < 0 || a >= kTimerSlots || b >= kTimerSlots) return TRAX_ERR_BAD_ARG;
+    CK(cudaEventSynchronize(ctx->timers[b]));
+    CK(cudaEventElapsedTime(ms, ctx->timers[a], ctx->timers[b]));
+    return TRAX_OK;
+}
+
+trax_status trax_reset_counts(trax_ctx *ctx)
+{
+    if (!ctx) return TRAX_ERR_BAD_ARG;
+    CK(cudaMemsetAsync(&ctx->d_state->n_outer, 0, sizeof(DevState) - 8, ctx->stream));
+    return TRAX_OK;
+}
+
+trax_status trax_read_counts(trax_ctx *ctx, trax_counts *out)
+{
+    if (!ctx || !out) return TRAX_ERR_BAD_ARG;
+    CK(cudaMemcpyAsync(ctx->h_state, ctx->d_state, sizeof(DevState), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const DevState &s = *ctx->h_state;
+    out->n_hits = s.n_hits;
+    out->n_pairs = s.n_pairs;
+    out->pair_slots = s.pair_slots;
+    out->n_candidates = s.n_cands;
+    out->cand_slots = s.cand_slots;
+    out->cand_truncated = s.cand_truncated;
+    out->n_tracklets = s.n_trk;
+    out->status = s.status;
+    out->error_detail = s.detail;
+    return TRAX_OK;
+}
+
+/* ---------------------------------------------------------------------- */
+
+trax_status trax_grid_build(trax_ctx *ctx, const trax_hits *in, const trax_layout *layout,
+                            const trax_grid_cfg *grid, trax_sorted_hits *out, uint32_t *d_grid)
+{
+    if (!ctx || !in || !layout || !grid || !out || !d_grid) return TRAX_ERR_BAD_ARG;
+    trax_status s = check_grid(ctx, grid);
+    if (s != TRAX_OK) return s;
+    if (layout->n_events != grid->n_events || layout->n_layers != grid->n_layers)
+        return fail(ctx, TRAX_ERR_BAD_ARG, "layout and grid disagree on events or layers");
+    if (out->n < in->n) return fail(ctx, TRAX_ERR_CAPACITY, "sorted output smaller than the input");
+    fill_grid_params(ctx->kp, grid);
+    uint32_t *d_start = nullptr, *d_n = nullptr;
+    if ((s = build_segments(ctx, layout, in->n, &d_start, &d_n)) != TRAX_OK) return s;
+    if ((s = set_sizes(ctx, grid->n_events, in->n)) != TRAX_OK) return s;
+    if (grid->n_events == 0) return TRAX_OK;
+    InCols ic{in->x, in->y, in->z, in->layer, in->detector_id, in->hit_id, in->event};
+    return enqueue_grid(ctx, ic, sorted_from(out), d_start, d_n, d_grid,
+                        grid->n_events * grid->n_layers);
+}
+
+trax_status trax_pair_gen(trax_ctx *ctx, const trax_sorted_hits *hits, const uint32_t *d_grid,
+                          const trax_grid_cfg *grid, trax_pairs *out)
+{
+    if (!ctx || !hits || !d_grid || !grid || !out) return TRAX_ERR_BAD_ARG;
+    trax_status s = check_grid(ctx, grid);
+    if (s != TRAX_OK) return s;
+    fill_grid_params(ctx->kp, grid);
+    if ((s = set_sizes(ctx, grid->n_events, hits->n)) != TRAX_OK) return s;
+    const uint32_t G = grid->n_events * ctx->kp.n_lt;
+    const uint64_t slot_cap = (uint64_t)hits->n * ctx->kp.n_lt + 1;
+    if (slot_cap > 0xF0000000ull) return fail(ctx, TRAX_ERR_BAD_ARG, "too many hits");
+    return enqueue_pairs(ctx, sorted_from(hits), d_grid, (uint2 *)out->pairs, out->offsets,
+                         out->capacity, (uint32_t)slot_cap, G);
+}
+
+trax_status trax_triplet_predict(trax_ctx *ctx, const trax_sorted_hits *hits,
+                                 const uint32_t *d_grid, const trax_grid_cfg *grid,
+                                 const trax_pairs *pairs, trax_pairs *cands)
+{
+    if (!ctx || !hits || !d_grid || !grid || !pairs || !cands) return TRAX_ERR_BAD_ARG;
+    trax_status s = check_grid(ctx, grid);
+    if (s != TRAX_OK) return s;
+    fill_grid_params(ctx->kp, grid);
+    const uint32_t G = grid->n_events * ctx->kp.n_lt;
+    /* the pair total is pairs->offsets[G]; copy it into the state word the
+     * kernels read (device to device, stream ordered) */
+    CK(cudaMemcpyAsync(&ctx->d_state->n_pairs, pairs->offsets + G, 4, cudaMemcpyDeviceToDevice,
+                       ctx->stream));
+    return enqueue_predict(ctx, sorted_from(hits), d_grid, (const uint2 *)pairs->pairs,
+                           pairs->offsets, pairs->capacity, (uint2 *)cands->pairs, cands->offsets,
+                           cands->capacity, G);
+}
+
+trax_status trax_triplet_filter(trax_ctx *ctx, const trax_sorted_hits *hits,
+                                const trax_grid_cfg *grid, const trax_pairs *pairs,
+                                const trax_pairs *cands, trax_tracklets *out)
+{
+    if (!ctx || !hits || !grid || !pairs || !cands || !out) return TRAX_ERR_BAD_ARG;
+    trax_status s = check_grid(ctx, grid);
+    if (s != TRAX_OK) return s;
+    fill_grid_params(ctx->kp, grid);
+    const uint32_t G = grid->n_events * ctx->kp.n_lt;
+    CK(cudaMemcpyAsync(&ctx->d_state->n_cands, cands->offsets + G, 4, cudaMemcpyDeviceToDevice,
+                       ctx->stream));
+    return enqueue_filter(ctx, sorted_from(hits), (const uint2 *)pairs->pairs,
+                          (const uint2 *)cands->pairs, cands->capacity, out->hit1, out->hit2,
+                          out->hit3, out->offsets, out->capacity, G);
+}
+
+/* ---------------------------------------------------------------------- */
+/* Batched pipeline                                                        */
+
+trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers,
+                         uint32_t max_hits, const trax_grid_cfg *grid, uint32_t max_pairs,
+                         uint32_t max_candidates, uint32_t max_tracklets)
+{
+    if (!ctx || !grid) return TRAX_ERR_BAD_ARG;
+    trax_grid_cfg g = *grid;
+    g.n_events = max_events;
+    g.n_layers = max_layers;
+    trax_status s = check_grid(ctx, &g);
+    if (s != TRAX_OK) return s;
+    if (ctx->graph) {
+        cudaGraphExecDestroy(ctx->graph);
+        ctx->graph = nullptr;
+    }
+    ctx->reserved = false;
+    const uint32_t T = ctx->kp.n_lt;
+    const uint64_t C = (uint64_t)(g.n_sectors_z + 1) * (g.n_sectors_phi + 1);
+    const uint64_t G = (uint64_t)max_events * T;
+    const uint64_t slot_cap = (uint64_t)max_hits * T + 1;
+    if (slot_cap > 0xF0000000ull || (uint64_t)max_events * max_layers * C > 0xF0000000ull)
+        return fail(ctx, TRAX_ERR_BAD_ARG, "reservation too large");
+    for (int i = 0; i < 7; ++i) if ((s = ensure(ctx, ctx->in_cols[i], (size_t)max_hits * 4)) != TRAX_OK) return s;
+    for (int i = 0; i < 9; ++i) if ((s = ensure(ctx, ctx->srt_cols[i], (size_t)max_hits * 4)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->grid_buf, (size_t)(max_events * max_layers * C) * 4)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->r_seg, (size_t)max_events * max_layers * 8 + 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->pairs_buf, (size_t)max_pairs * 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->pair_off, (size_t)(G + 1) * 4)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->cands_buf, (size_t)max_candidates * 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->cand_off, (size_t)(G + 1) * 4)) != TRAX_OK) return s;
+    for (int i = 0; i < 3; ++i) if ((s = ensure(ctx, ctx->trk_cols[i], (size_t)max_tracklets * 4)) != TRAX_OK) return s;
+    for (int i = 0; i < 3; ++i) if ((s = ensure(ctx, ctx->trk_map[i], (size_t)max_tracklets * 4)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->trk_off, (size_t)(G + 1) * 4)) != TRAX_OK) return s;
+    /* scratch at its maximum so the captured graph never reallocates */
+    if ((s = ensure(ctx, ctx->g_start, G * 4)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->g_base, (G + 1) * 4)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->slots, slot_cap * 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->pcnt, slot_cap * 4)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->pexcl, (slot_cap + 1) * 4)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->st0, (size_t)tiles_for((uint32_t)slot_cap, kScanThreads * kScanItems) * 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->ccnt, (size_t)max_pairs * 4)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->cexcl, (size_t)(max_pairs + 1) * 4)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->st1, (size_t)tiles_for(max_pairs, kScanThreads * kScanItems) * 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->st2, (size_t)tiles_for(max_candidates, 256 * kFilterItems) * 8)) != TRAX_OK) return s;
+    if ((s = ensure_stage(ctx, (size_t)max_events * max_layers * 2 + 4)) != TRAX_OK) return s;
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->r_events = max_events;
+    ctx->r_layers = max_layers;
+    ctx->r_hits = max_hits;
+    ctx->r_pairs = max_pairs;
+    ctx->r_cands = max_candidates;
+    ctx->r_trk = max_tracklets;
+    ctx->r_grid = g;
+    ctx->reserved = true;
+    return TRAX_OK;
+}
+
+namespace {
+
+SortedCols reserved_sorted(trax_ctx *ctx)
+{
+    SortedCols s;
+    s.x = (float *)ctx->srt_cols[0].p; s.y = (float *)ctx->srt_cols[1].p;
+    s.z = (float *)ctx->srt_cols[2].p; s.phi = (float *)ctx->srt_cols[3].p;
+    s.layer = (uint32_t *)ctx->srt_cols[4].p; s.det = (uint32_t *)ctx->srt_cols[5].p;
+    s.hitid = (uint32_t *)ctx->srt_cols[6].p; s.event = (uint32_t *)ctx->srt_cols[7].p;
+    s.orig = (uint32_t *)ctx->srt_cols[8].p;
+    return s;
+}
+
+/* The whole chain on reserved buffers; sizes come from DevState. */
+trax_status enqueue_pipeline(trax_ctx *ctx)
+{
+    const uint32_t T = ctx->kp.n_lt;
+    const uint32_t G = ctx->r_events * T;
+    const uint32_t nseg = ctx->r_events * ctx->r_layers;
+    InCols ic{(const float *)ctx->in_cols[0].p, (const float *)ctx->in_cols[1].p,
+              (const float *)ctx->in_cols[2].p, (const uint32_t *)ctx->in_cols[3].p,
+              (const uint32_t *)ctx->in_cols[4].p, (const uint32_t *)ctx->in_cols[5].p,
+              (const uint32_t *)ctx->in_cols[6].p};
+    const SortedCols sc = reserved_sorted(ctx);
+    uint32_t *grid = (uint32_t *)ctx->grid_buf.p;
+    const uint32_t *seg = (const uint32_t *)ctx->r_seg.p;
+    CK(cudaMemsetAsync(&ctx->d_state->n_outer, 0, sizeof(DevState) - 8, ctx->stream));
+    trax_status s = enqueue_grid(ctx, ic, sc, seg, seg + nseg, grid, nseg);
+    if (s != TRAX_OK) return s;
+    const uint32_t slot_cap = ctx->r_hits * T + 1;
+    s = enqueue_pairs(ctx, sc, grid, (uint2 *)ctx->pairs_buf.p, (uint32_t *)ctx->pair_off.p,
+                      ctx->r_pairs, slot_cap, G);
+    if (s != TRAX_OK) return s;
+    s = enqueue_predict(ctx, sc, grid, (const uint2 *)ctx->pairs_buf.p,
+                        (const uint32_t *)ctx->pair_off.p, ctx->r_pairs, (uint2 *)ctx->cands_buf.p,
+                        (uint32_t *)ctx->cand_off.p, ctx->r_cands, G);
+    if (s != TRAX_OK) return s;
+    return enqueue_filter(ctx, sc, (const uint2 *)ctx->pairs_buf.p,
+                          (const uint2 *)ctx->cands_buf.p, ctx->r_cands,
+                          (uint32_t *)ctx->trk_cols[0].p, (uint32_t *)ctx->trk_cols[1].p,
+                          (uint32_t *)ctx->trk_cols[2].p, (uint32_t *)ctx->trk_off.p, ctx->r_trk,
+                          G);
+}
+
+__global__ void k_map_orig(const uint32_t *orig, const uint32_t *t1, const uint32_t *t2,
+                           const uint32_t *t3, uint32_t *m1, uint32_t *m2, uint32_t *m3,
+                           uint32_t cap, const DevState *st)
+{
+    uint32_t n = st->n_trk;
+    if (n > cap) n = cap;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        m1[i] = orig[t1[i]];
+        m2[i] = orig[t2[i]];
+        m3[i] = orig[t3[i]];
+    }
+}
+
+}  // namespace
+
+trax_status trax_stage_batch(trax_ctx *ctx, const trax_event_batch *in)
+{
+    if (!ctx || !in) return TRAX_ERR_BAD_ARG;
+    if (!ctx->reserved) return fail(ctx, TRAX_ERR_BAD_ARG, "trax_reserve not called");
+    if (in->n_events > ctx->r_events || in->n_layers != ctx->r_layers || in->n_hits > ctx->r_hits)
+        return fail(ctx, TRAX_ERR_CAPACITY, "batch larger than the reservation");
+    /* the reserved segment buffer holds [start | count] at a fixed stride */
+    const uint32_t E = in->n_events, L = in->n_layers;
+    const size_t nseg_r = (size_t)ctx->r_events * L;
+    trax_status s = ensure_stage(ctx, 2 * nseg_r + 4);
+    if (s != TRAX_OK) return s;
+    uint32_t *hs = ctx->h_stage, *hn = ctx->h_stage + nseg_r;
+    uint64_t run = 0;
+    for (uint32_t e = 0; e < E; ++e)
+        for (uint32_t l = 0; l < L; ++l) {
+            hs[(size_t)e * L + l] = (uint32_t)run;
+            hn[(size_t)e * L + l] = in->layer_nhits[(size_t)e * L + l];
+            run += in->layer_nhits[(size_t)e * L + l];
+        }
+    if (run != in->n_hits) return fail(ctx, TRAX_ERR_BAD_INPUT, "layer_nhits do not sum to n_hits");
+    hs[2 * nseg_r] = E;
+    hs[2 * nseg_r + 1] = in->n_hits;
+    const size_t nseg = (size_t)E * L;
+    CK(cudaMemcpyAsync(ctx->r_seg.p, hs, nseg * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync((uint32_t *)ctx->r_seg.p + nseg_r, hn, nseg * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_state, hs + 2 * nseg_r, 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaEventRecord(ctx->stage_free, ctx->stream));
+    const void *src[7] = {in->x, in->y, in->z, in->layer, in->detector_id, in->hit_id, in->event};
+    for (int i = 0; i < 7; ++i)
+        if (in->n_hits) CK(cudaMemcpyAsync(ctx->in_cols[i].p, src[i], (size_t)in->n_hits * 4,
+                                           cudaMemcpyHostToDevice, ctx->stream));
+    ctx->staged_events = E;
+    ctx->staged_hits = in->n_hits;
+    return TRAX_OK;
+}
+
+trax_status trax_run_staged(trax_ctx *ctx)
+{
+    if (!ctx || !ctx->reserved) return TRAX_ERR_BAD_ARG;
+    fill_grid_params(ctx->kp, &ctx->r_grid);
+    if (!ctx->graph) {
+        trax_status s0 = grid_plan(ctx, ctx->kp.C);
+        if (s0 != TRAX_OK) return s0;
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        trax_status s = enqueue_pipeline(ctx);
+        cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+        if (s != TRAX_OK) {
+            if (g) cudaGraphDestroy(g);
+            return s;
+        }
+        if (e != cudaSuccess) return fail(ctx, TRAX_ERR_DEVICE, cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&ctx->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            ctx->graph = nullptr;
+            return fail(ctx, TRAX_ERR_DEVICE, cudaGetErrorString(e));
+        }
+    }
+    CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+    return TRAX_OK;
+}
+
+trax_status trax_seed_batch(trax_ctx *ctx, const trax_event_batch *in, trax_batch_result *out)
+{
+    if (!ctx || !in || !out) return TRAX_ERR_BAD_ARG;
+    trax_status s = trax_stage_batch(ctx, in);
+    if (s != TRAX_OK) return s;
+    if ((s = trax_run_staged(ctx)) != TRAX_OK) return s;
+    if (out->input_indices) {
+        k_map_orig<<<ctx->blk_small, 256, 0, ctx->stream>>>(
+            (const uint32_t *)ctx->srt_cols[8].p, (const uint32_t *)ctx->trk_cols[0].p,
+            (const uint32_t *)ctx->trk_cols[1].p, (const uint32_t *)ctx->trk_cols[2].p,
+            (uint32_t *)ctx->trk_map[0].p, (uint32_t *)ctx->trk_map[1].p,
+            (uint32_t *)ctx->trk_map[2].p, ctx->r_trk, ctx->d_state);
+        CK(cudaGetLastError());
+    }
+    if ((s = trax_read_counts(ctx, &out->counts)) != TRAX_OK) return s;
+    const uint32_t G = in->n_events * ctx->kp.n_lt;
+    uint32_t n = (uint32_t)out->counts.n_tracklets;
+    out->n_tracklets = n;
+    if (n > ctx->r_trk) n = ctx->r_trk;
+    const bool fits = n <= out->capacity;
+    if (fits && n) {
+        DevBuf *cols = out->input_indices ? ctx->trk_map : ctx->trk_cols;
+        uint32_t *dst[3] = {out->hit1, out->hit2, out->hit3};
+        for (int i = 0; i < 3; ++i)
+            if (dst[i]) CK(cudaMemcpyAsync(dst[i], cols[i].p, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    if (out->offsets)
+        CK(cudaMemcpyAsync(out->offsets, ctx->trk_off.p, (size_t)(G + 1) * 4, cudaMemcpyDeviceToHost,
+                           ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (out->counts.status != TRAX_OK) {
+        char buf[96];
+        snprintf(buf, sizeof buf, "device status %u detail %u", out->counts.status,
+                 out->counts.error_detail);
+        return fail(ctx, (trax_status)out->counts.status, buf);
+    }
+    if (!fits) return fail(ctx, TRAX_ERR_CAPACITY, "result larger than the output capacity");
+    return TRAX_OK;
+}
+
+}  // extern "C"

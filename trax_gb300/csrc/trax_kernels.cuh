@@ -1,0 +1,981 @@
+/*
+ * trax_kernels.cuh -- sm_103a kernels of the triplet-seeding path.
+ *
+ * Layout in HBM (all SoA, uint32 / float32):
+ *   hits (input)      x y z layer detector_id hit_id event      [N]
+ *   sorted hits       x y z phi layer detector_id hit_id event orig [N]
+ *   grid              [E][L][(Z+1)(P+1)] global start of each cell
+ *   outer slots       (outer hit, group) per (event, layer triplet) layer2 hit
+ *   pairs             uint2 (inner, outer)                         [M]
+ *   candidates        uint2 (pair index, hit3)                     [K]
+ *   tracklets         hit1 hit2 hit3                               [R]
+ *
+ * Every kernel is persistent (grid = a multiple of the SM count) and reads
+ * its problem size from device memory, so one launch sequence serves any
+ * batch up to the reserved capacity and can be captured in a CUDA graph.
+ *
+ * FP32 arithmetic mirrors the reference kernels operation by operation and
+ * is compiled with -fmad=false (see trax_math.h).
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "trax_math.h"
+#include "../../include/trax.h"
+
+namespace trax {
+
+constexpr int kMaxLT = TRAX_MAX_LAYER_TRIPLETS;
+constexpr int kMaxLayers = TRAX_MAX_LAYERS;
+constexpr uint32_t kFull = 0xffffffffu;
+
+/* Per-run constants, passed by value to every kernel. */
+struct KParams {
+    uint32_t n_layers, nz, nphi, C, n_lt;
+    float sz_z, sz_phi, rmin_curv;
+    uint32_t l1[kMaxLT], l2[kMaxLT], l3[kMaxLT];
+    float dtheta[kMaxLT], sigma_z[kMaxLT], dphi[kMaxLT], sigma_phi[kMaxLT];
+    float tip[kMaxLT], z0[kMaxLT];
+    uint32_t spread_phi[kMaxLT];
+    float rmin[kMaxLayers], rmax[kMaxLayers];
+};
+
+/* Device-side sizes, counters and status of one pipeline run. */
+struct DevState {
+    uint32_t n_events;
+    uint32_t n_hits;
+    uint32_t n_outer;        /* outer slots (sum of layer2 hits over groups) */
+    uint32_t n_pairs;
+    uint32_t n_cands;
+    uint32_t n_trk;
+    uint32_t status;
+    uint32_t detail;
+    unsigned long long pair_slots;
+    unsigned long long cand_slots;
+    unsigned long long cand_truncated;
+    uint32_t tile_ctr[4];    /* decoupled look-back tile tickets */
+    uint32_t pad[4];
+};
+
+struct SortedCols {
+    float *x, *y, *z, *phi;
+    uint32_t *layer, *det, *hitid, *event, *orig;
+};
+
+struct InCols {
+    const float *x, *y, *z;
+    const uint32_t *layer, *det, *hitid, *event;
+};
+
+__device__ __forceinline__ void set_fault(DevState *st, uint32_t status, uint32_t detail)
+{
+    if (atomicCAS(&st->status, 0u, status) == 0u) atomicExch(&st->detail, detail);
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt()
+{
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p)
+{
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long ld_relaxed64(const unsigned long long *p)
+{
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_relaxed64(unsigned long long *p, unsigned long long v)
+{
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" : : "l"(p), "l"(v) : "memory");
+}
+
+/* ------------------------------------------------------------------------
+ * Block-wide exclusive scan of one value per thread (blockDim <= 1024).
+ * ---------------------------------------------------------------------- */
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *s_warp,
+                                                         uint32_t *total)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t y = __shfl_up_sync(kFull, x, d);
+        if (lane >= d) x += y;
+    }
+    if (lane == 31) s_warp[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t w = lane < nw ? s_warp[lane] : 0u;
+        uint32_t t = w;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            uint32_t y = __shfl_up_sync(kFull, t, d);
+            if (lane >= d) t += y;
+        }
+        if (lane < nw) s_warp[lane] = t - w;
+        if (lane == 31) s_warp[32] = t;
+    }
+    __syncthreads();
+    const uint32_t r = s_warp[wid] + x - v;
+    if (total) *total = s_warp[32];
+    __syncthreads();
+    return r;
+}
+
+/* ------------------------------------------------------------------------
+ * Decoupled look-back (Merrill & Garland, "Single-pass Parallel Prefix Scan
+ * with Decoupled Look-back", 2016).  Tile status words pack a 2-bit flag
+ * (1 aggregate, 2 inclusive prefix) above a 32-bit value.  Waits are
+ * bounded: after kSpinLimit polls the tile records TRAX_ERR_TIMEOUT and
+ * treats the missing predecessor as 0, so the kernel always terminates.
+ * ---------------------------------------------------------------------- */
+constexpr unsigned long long kFlagAgg = 1ull << 32;
+constexpr unsigned long long kFlagInc = 2ull << 32;
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t lookback_prefix(unsigned long long *status, uint32_t tile,
+                                                    DevState *st)
+{
+    uint32_t prefix = 0;
+    int64_t k = (int64_t)tile - 1;
+    uint32_t spins = 0;
+    while (k >= 0) {
+        unsigned long long s = ld_relaxed64(status + k);
+        const unsigned long long flag = s & (3ull << 32);
+        if (flag == 0) {
+            if (++spins > kSpinLimit) {
+                set_fault(st, TRAX_ERR_TIMEOUT, TRAX_DETAIL_SCAN_TIMEOUT);
+                break;
+            }
+            __nanosleep(32);
+            continue;
+        }
+        prefix += (uint32_t)s;
+        if (flag == kFlagInc) break;
+        --k;
+    }
+    return prefix;
+}
+
+/*
+ * One persistent look-back scan over n items (n read from device memory by
+ * the caller).  Producer: uint32_t(uint32_t idx) gives the item value;
+ * Consumer: void(uint32_t idx, uint32_t exclusive, uint32_t value).
+ * Returns nothing; `on_total` receives the grand total from the last tile.
+ */
+template <int ITEMS, class Producer, class Consumer, class Total>
+__device__ __forceinline__ void lookback_scan(uint32_t n, uint32_t *tile_ctr,
+                                              unsigned long long *status, DevState *st,
+                                              Producer prod, Consumer cons, Total on_total)
+{
+    __shared__ uint32_t s_warp[33];
+    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_prefix;
+    const uint32_t tileItems = blockDim.x * ITEMS;
+    const uint32_t ntiles = (n + tileItems - 1) / tileItems;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(tile_ctr, 1u);
+        __syncthreads();
+        const uint32_t tile = s_tile;
+        if (tile >= ntiles) break;
+        const uint32_t base = tile * tileItems + threadIdx.x * ITEMS;
+        uint32_t v[ITEMS];
+        uint32_t sum = 0;
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            v[k] = (base + k < n) ? prod(base + k) : 0u;
+            sum += v[k];
+        }
+        uint32_t agg;
+        const uint32_t excl = block_exclusive_scan(sum, s_warp, &agg);
+        if (threadIdx.x == 0) {
+            uint32_t prefix = 0;
+            if (tile == 0) {
+                st_relaxed64(status, kFlagInc | agg);
+            } else {
+                st_relaxed64(status + tile, kFlagAgg | agg);
+                prefix = lookback_prefix(status, tile, st);
+                st_relaxed64(status + tile, kFlagInc | (uint32_t)(prefix + agg));
+            }
+            s_prefix = prefix;
+            if (tile == ntiles - 1) on_total(prefix + agg);
+        }
+        __syncthreads();
+        uint32_t run = s_prefix + excl;
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            if (base + k < n) cons(base + k, run, v[k]);
+            run += v[k];
+        }
+        __syncthreads();
+    }
+}
+
+/* Exclusive scan of in[0..n) into out[0..n], out[n] = total (in-place OK). */
+template <int ITEMS>
+__global__ void __launch_bounds__(256) k_scan(const uint32_t *in, uint32_t *out,
+                                              const uint32_t *n_ptr, uint32_t n_cap,
+                                              uint32_t *total_out, int ctr_slot,
+                                              unsigned long long *status, DevState *st)
+{
+    uint32_t n = *n_ptr;
+    if (n > n_cap) n = n_cap;
+    if (n == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            out[0] = 0;
+            if (total_out) *total_out = 0;
+        }
+        return;
+    }
+    lookback_scan<ITEMS>(
+        n, &st->tile_ctr[ctr_slot], status, st,
+        [&](uint32_t i) { return in[i]; },
+        [&](uint32_t i, uint32_t e, uint32_t) { out[i] = e; },
+        [&](uint32_t t) {
+            out[n] = t;
+            if (total_out) *total_out = t;
+        });
+}
+
+/* ------------------------------------------------------------------------
+ * Stage 1: grid build.  One CTA per (event, layer) segment (persistent
+ * loop).  Counting sort into (z, phi) cells, stable within a cell:
+ *   pass 1  each warp owns a contiguous sub-range of the segment and counts
+ *           its cells (warp match + one shared add per distinct cell);
+ *   pass 2  per cell, exclusive prefix over warps and an exclusive scan over
+ *           cells give every warp's write cursor; the grid row is written;
+ *   pass 3  each warp re-walks its sub-range in order and scatters the hit
+ *           columns at cursor + rank-in-warp.
+ * The segment's first sorted position equals its first input position
+ * (the input is event/layer bucketed), so no global scan is needed.
+ * Shared memory: (W + 1) * C uint32.
+ * ---------------------------------------------------------------------- */
+__device__ __forceinline__ uint32_t hit_cell(const KParams &kp, float x, float y, float z,
+                                             float *phi_out, bool *bad)
+{
+    uint32_t zs = trax_sector_z(z, kp.sz_z);
+    const float phi = trax_atan2f(y, x);
+    uint32_t ps = trax_sector_phi(phi, kp.sz_phi);
+    *bad = false;
+    if (zs > kp.nz) { zs = kp.nz; *bad = true; }
+    if (ps > kp.nphi) { ps = kp.nphi; *bad = true; }
+    *phi_out = phi;
+    return zs * (kp.nphi + 1) + ps;
+}
+
+__global__ void __launch_bounds__(1024) k_grid_build(KParams kp, InCols in, SortedCols out,
+                                                     const uint32_t *seg_start,
+                                                     const uint32_t *seg_n, uint32_t *grid,
+                                                     DevState *st)
+{
+    extern __shared__ uint32_t smem[];
+    __shared__ uint32_t s_warp[33];
+    const uint32_t C = kp.C;
+    const int W = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t *s_cnt = smem;           /* [W][C] */
+    uint32_t *s_tot = smem + W * C;   /* [C] */
+    const uint32_t nseg = st->n_events * kp.n_layers;
+    const uint32_t lt_mask = lanemask_lt();
+
+    for (uint32_t seg = blockIdx.x; seg < nseg; seg += gridDim.x) {
+        const uint32_t e = seg / kp.n_layers, l = seg % kp.n_layers;
+        const uint32_t start = seg_start[seg], n = seg_n[seg];
+        for (uint32_t k = threadIdx.x; k < (uint32_t)W * C; k += blockDim.x) s_cnt[k] = 0;
+        __syncthreads();
+        const uint32_t chunk = (n + W - 1) / W;
+        const uint32_t lo = min(n, w * chunk), hi = min(n, lo + chunk);
+
+        /* pass 1 */
+        for (uint32_t b = lo; b < hi; b += 32) {
+            const uint32_t i = b + lane;
+            const bool valid = i < hi;
+            const uint32_t act = __ballot_sync(kFull, valid);
+            if (valid) {
+                const uint32_t h = start + i;
+                float phi;
+                bool bad;
+                const uint32_t cell = hit_cell(kp, in.x[h], in.y[h], in.z[h], &phi, &bad);
+                if (bad) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_OUTSIDE_GRID);
+                const uint32_t peers = __match_any_sync(act, cell);
+                if (lane == __ffs(peers) - 1) s_cnt[w * C + cell] += __popc(peers);
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+
+        /* pass 2: prefix over warps per cell, then scan over cells */
+        for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
+            uint32_t run = 0;
+            for (int q = 0; q < W; ++q) {
+                const uint32_t t = s_cnt[q * C + c];
+                s_cnt[q * C + c] = run;
+                run += t;
+            }
+            s_tot[c] = run;
+        }
+        __syncthreads();
+        {
+            const uint32_t per = (C + blockDim.x - 1) / blockDim.x;
+            const uint32_t c0 = min(C, threadIdx.x * per), c1 = min(C, c0 + per);
+            uint32_t sum = 0;
+            for (uint32_t c = c0; c < c1; ++c) sum += s_tot[c];
+            uint32_t run = block_exclusive_scan(sum, s_warp, nullptr) + start;
+            for (uint32_t c = c0; c < c1; ++c) {
+                const uint32_t t = s_tot[c];
+                s_tot[c] = run;
+                run += t;
+            }
+        }
+        __syncthreads();
+        for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
+            const uint32_t b = s_tot[c];
+            grid[(size_t)seg * C + c] = b;
+            for (int q = 0; q < W; ++q) s_cnt[q * C + c] += b;
+        }
+        __syncthreads();
+
+        /* pass 3 */
+        for (uint32_t b = lo; b < hi; b += 32) {
+            const uint32_t i = b + lane;
+            const bool valid = i < hi;
+            const uint32_t act = __ballot_sync(kFull, valid);
+            uint32_t pos = 0, peers = 0, cell = 0;
+            float x = 0.f, y = 0.f, z = 0.f, phi = 0.f;
+            uint32_t h = 0;
+            if (valid) {
+                h = start + i;
+                x = in.x[h]; y = in.y[h]; z = in.z[h];
+                bool bad;
+                cell = hit_cell(kp, x, y, z, &phi, &bad);
+                peers = __match_any_sync(act, cell);
+                pos = s_cnt[w * C + cell] + __popc(peers & lt_mask);
+            }
+            __syncwarp();
+            if (valid && lane == __ffs(peers) - 1) s_cnt[w * C + cell] += __popc(peers);
+            __syncwarp();
+            if (valid) {
+                const uint32_t ly = in.layer[h], ev = in.event[h];
+                if (ly != l + 1 || ev != e) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_LAYER_MISMATCH);
+                out.x[pos] = x; out.y[pos] = y; out.z[pos] = z; out.phi[pos] = phi;
+                out.layer[pos] = ly; out.det[pos] = in.det[h]; out.hitid[pos] = in.hitid[h];
+                out.event[pos] = ev; out.orig[pos] = h;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * Stage 2: pair generation.
+ * ---------------------------------------------------------------------- */
+
+/* Group table: per (event, layer triplet) the first outer hit and the
+ * exclusive prefix of outer-hit counts.  One CTA. */
+__global__ void __launch_bounds__(1024) k_pair_groups(KParams kp, const uint32_t *grid,
+                                                      uint32_t *g_outer_start, uint32_t *g_base,
+                                                      DevState *st)
+{
+    __shared__ uint32_t s_warp[33];
+    __shared__ uint32_t s_carry;
+    const uint32_t G = st->n_events * kp.n_lt;
+    const uint32_t C = kp.C;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    for (uint32_t b = 0; b < G; b += blockDim.x) {
+        const uint32_t g = b + threadIdx.x;
+        uint32_t n2 = 0;
+        if (g < G) {
+            const uint32_t e = g / kp.n_lt, lt = g % kp.n_lt;
+            const uint32_t *row = grid + ((size_t)e * kp.n_layers + (kp.l2[lt] - 1)) * C;
+            g_outer_start[g] = row[0];
+            n2 = row[C - 1] - row[0];
+        }
+        uint32_t tot;
+        const uint32_t ex = block_exclusive_scan(n2, s_warp, &tot);
+        if (g < G) g_base[g] = s_carry + ex;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        g_base[G] = s_carry;
+        st->n_outer = s_carry;
+    }
+}
+
+/* Outer slot s -> (outer sorted hit, group).  One warp per group. */
+__global__ void __launch_bounds__(256) k_pair_slots(KParams kp, const uint32_t *g_outer_start,
+                                                    const uint32_t *g_base, uint2 *slots,
+                                                    uint32_t slot_cap, DevState *st)
+{
+    const uint32_t G = st->n_events * kp.n_lt;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t g = gw; g < G; g += nw) {
+        const uint32_t b0 = g_base[g], b1 = g_base[g + 1], o = g_outer_start[g];
+        for (uint32_t s = b0 + lane; s < b1 && s < slot_cap; s += 32) slots[s] = make_uint2(o + (s - b0), g);
+    }
+}
+
+struct PairWindow {
+    float zLow, zHigh, phiLow, phiHigh;
+    uint32_t zLowSector, zHighSector, phiLowSector, phiHighSector;
+    uint32_t wrap;
+    bool ok;
+};
+
+/* pairCount's window (PairGeneratorBeamspot.h:110-162), same FP32 order. */
+__device__ __forceinline__ PairWindow pair_window(const KParams &kp, uint32_t lt, float hx,
+                                                  float hy, float hz, float phi)
+{
+    PairWindow w;
+    const uint32_t layer = kp.l1[lt] - 1;
+    const float z0 = kp.z0[lt];
+    const float tip = kp.tip[lt];
+    const float sigmaZ = kp.sigma_z[lt];
+    const float sigmaPhi = __uint_as_float(kp.spread_phi[lt]);
+    const float minLayerRadius1 = kp.rmin[layer];
+    const float maxLayerRadius1 = kp.rmax[layer];
+    const float minRadiusCurvature = kp.rmin_curv;
+
+    const float signRadius = trax_signf(hy);
+    const float r = signRadius * sqrtf(hx * hx + hy * hy);
+    const float cotThetaHigh = (hz - z0) / r;
+    const float cotThetaLow = (hz + z0) / r;
+    float tmp = signRadius * maxLayerRadius1 * cotThetaHigh + z0;
+    float zHigh = signRadius * minLayerRadius1 * cotThetaHigh + z0;
+    zHigh = (float)(tmp < zHigh) * zHigh + (float)(tmp > zHigh) * tmp;
+    tmp = signRadius * maxLayerRadius1 * cotThetaLow - z0;
+    float zLow = signRadius * minLayerRadius1 * cotThetaLow - z0;
+    zLow = (float)(tmp < zLow) * tmp + (float)(tmp > zLow) * zLow;
+    zLow -= sigmaZ;
+    zHigh += sigmaZ;
+    const int32_t zl = trax_f2i(floorf((zLow - TRAX_MIN_Z) / kp.sz_z));
+    w.zLowSector = (uint32_t)(zl > 0 ? zl : 0);
+    const uint32_t zh = trax_f2u(floorf((zHigh - TRAX_MIN_Z) / kp.sz_z)) + 1u;
+    w.zHighSector = zh < kp.nz ? zh : kp.nz;
+
+    tmp = fabsf(trax_acosf(r / (2 * minRadiusCurvature)) - trax_acosf(maxLayerRadius1 / (2 * minRadiusCurvature)));
+    float dPhi = fabsf(trax_acosf(r / (2 * minRadiusCurvature)) - trax_acosf(minLayerRadius1 / (2 * minRadiusCurvature)));
+    dPhi = (float)(tmp < dPhi) * dPhi + (float)(tmp > dPhi) * tmp;
+    tmp = trax_atanf(tip * (r - minLayerRadius1)) / (r * minLayerRadius1);
+    float phiHigh = trax_atanf(tip * (r - maxLayerRadius1)) / (r * maxLayerRadius1);
+    dPhi += tmp > phiHigh ? tmp : phiHigh;
+    float phiLow = phi - dPhi - sigmaPhi;
+    phiHigh = phi + dPhi + sigmaPhi;
+    const bool wrap = phiLow < -TRAX_PI_F || phiHigh > TRAX_PI_F || phiLow > TRAX_PI_F || phiHigh < -TRAX_PI_F;
+    phiLow -= (float)((phiLow > TRAX_PI_F) * 2) * TRAX_PI_F;
+    phiLow += (float)((phiLow < -TRAX_PI_F) * 2) * TRAX_PI_F;
+    phiHigh -= (float)((phiHigh > TRAX_PI_F) * 2) * TRAX_PI_F;
+    phiHigh += (float)((phiHigh < -TRAX_PI_F) * 2) * TRAX_PI_F;
+    w.phiLowSector = trax_f2u(floorf((phiLow - TRAX_MIN_PHI) / kp.sz_phi));
+    w.phiHighSector = trax_f2u(floorf((phiHigh - TRAX_MIN_PHI) / kp.sz_phi)) + 1u;
+    w.zLow = zLow; w.zHigh = zHigh; w.phiLow = phiLow; w.phiHigh = phiHigh;
+    w.wrap = wrap ? 1u : 0u;
+    w.ok = w.phiLowSector <= kp.nphi + 1 && w.phiHighSector <= kp.nphi + 1;
+    return w;
+}
+
+__device__ __forceinline__ bool phi_in(float actPhi, float phiLow, float phiHigh, uint32_t wrap)
+{
+    return (!wrap && (phiLow <= actPhi && actPhi <= phiHigh))
+        || (wrap && ((phiLow <= actPhi && actPhi <= TRAX_PI_F) || (-TRAX_PI_F <= actPhi && actPhi <= phiHigh)));
+}
+
+/*
+ * Visits one outer hit's inner candidates row by row.  For each row the
+ * reference loop walks j in [jlo, end2) and maps j >= rowEnd back by the row
+ * length; that is the index range A = [jlo, min(end2, rowEnd)) followed by
+ * the wrapped range B = [max(jlo, rowEnd) - len, end2 - len).  The store
+ * emits the union in ascending index order (the reference's bitmap order):
+ * B first, then the part of A above B.  Counting mode returns the accepted
+ * visits (A and B, with repeats) and the distinct accepted indices.
+ */
+template <bool STORE>
+__device__ __forceinline__ void pair_visit(const KParams &kp, const uint32_t *lGrid1,
+                                           const float *Z, const float *PHI,
+                                           const PairWindow &w, uint32_t lane, uint32_t lt_mask,
+                                           uint32_t outer, uint32_t &visits, uint32_t &distinct,
+                                           uint2 *pairs, uint32_t pos, uint32_t cap)
+{
+    const uint32_t P1 = kp.nphi + 1;
+    for (uint32_t zs = w.zLowSector; zs < w.zHighSector; ++zs) {
+        const uint32_t rowStart = lGrid1[zs * P1];
+        const uint32_t rowEnd = lGrid1[(zs + 1) * P1 - 1];
+        const uint32_t len = rowEnd - rowStart;
+        const uint32_t jlo = lGrid1[zs * P1 + w.phiLowSector];
+        const uint32_t end2 = w.wrap * rowEnd + lGrid1[zs * P1 + w.phiHighSector] - w.wrap * rowStart;
+        const uint32_t aLo = jlo, aHi = min(end2, rowEnd);
+        const uint32_t jb = max(jlo, rowEnd);
+        const uint32_t bLo = jb - len;
+        const uint32_t bHi = end2 > jb ? end2 - len : bLo;
+        if (!STORE) {
+            for (uint32_t c = aLo; c < aHi; c += 32) {
+                const uint32_t idx = c + lane;
+                bool acc = false;
+                if (idx < aHi) {
+                    const float zz = Z[idx];
+                    acc = w.zLow <= zz && zz <= w.zHigh && phi_in(PHI[idx], w.phiLow, w.phiHigh, w.wrap);
+                }
+                const uint32_t b = __popc(__ballot_sync(kFull, acc));
+                visits += b;
+                distinct += b;
+            }
+            for (uint32_t c = bLo; c < bHi; c += 32) {
+                const uint32_t idx = c + lane;
+                bool acc = false, dup = false;
+                if (idx < bHi) {
+                    const float zz = Z[idx];
+                    acc = w.zLow <= zz && zz <= w.zHigh && phi_in(PHI[idx], w.phiLow, w.phiHigh, w.wrap);
+                    dup = idx >= aLo && idx < aHi;
+                }
+                visits += __popc(__ballot_sync(kFull, acc));
+                distinct += __popc(__ballot_sync(kFull, acc && !dup));
+            }
+        } else {
+            /* ascending union: B, then A above B */
+            const uint32_t a2 = max(aLo, bHi);
+            for (int part = 0; part < 2; ++part) {
+                const uint32_t lo = part == 0 ? bLo : a2;
+                const uint32_t hi = part == 0 ? bHi : aHi;
+                for (uint32_t c = lo; c < hi; c += 32) {
+                    const uint32_t idx = c + lane;
+                    bool acc = false;
+                    if (idx < hi) {
+                        const float zz = Z[idx];
+                        acc = w.zLow <= zz && zz <= w.zHigh && phi_in(PHI[idx], w.phiLow, w.phiHigh, w.wrap);
+                    }
+                    const uint32_t b = __ballot_sync(kFull, acc);
+                    if (acc) {
+                        const uint32_t p = pos + distinct + __popc(b & lt_mask);
+                        if (p < cap) pairs[p] = make_uint2(idx, outer);
+                    }
+                    distinct += __popc(b);
+                }
+            }
+        }
+    }
+}
+
+template <bool STORE>
+__global__ void __launch_bounds__(256) k_pair(KParams kp, const uint32_t *grid, const float *X,
+                                              const float *Y, const float *Z, const float *PHI,
+                                              const uint2 *slots, uint32_t slot_cap,
+                                              uint32_t *cnt, const uint32_t *excl, uint2 *pairs,
+                                              uint32_t pair_cap, DevState *st)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lt_mask = lanemask_lt();
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    uint32_t n = st->n_outer;
+    if (n > slot_cap) n = slot_cap;
+    unsigned long long my_visits = 0;
+    for (uint32_t s = gw; s < n; s += nw) {
+        const uint2 sl = slots[s];
+        const uint32_t outer = sl.x, g = sl.y;
+        const uint32_t e = g / kp.n_lt, lt = g % kp.n_lt;
+        const uint32_t *lGrid1 = grid + ((size_t)e * kp.n_layers + (kp.l1[lt] - 1)) * kp.C;
+        const PairWindow w = pair_window(kp, lt, X[outer], Y[outer], Z[outer], PHI[outer]);
+        uint32_t visits = 0, distinct = 0;
+        if (!w.ok) {
+            if (lane == 0) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_WINDOW_OUTSIDE_GRID);
+        } else if (!STORE) {
+            pair_visit<false>(kp, lGrid1, Z, PHI, w, lane, lt_mask, outer, visits, distinct,
+                              nullptr, 0, 0);
+        } else {
+            pair_visit<true>(kp, lGrid1, Z, PHI, w, lane, lt_mask, outer, visits, distinct,
+                             pairs, excl[s], pair_cap);
+        }
+        if (!STORE && lane == 0) {
+            cnt[s] = distinct;
+            my_visits += visits;
+        }
+    }
+    if (!STORE && lane == 0 && my_visits) atomicAdd(&st->pair_slots, my_visits);
+}
+
+/* pair_offsets[g+1] = pairs before the first slot of group g+1. */
+__global__ void k_group_offsets(const uint32_t *g_base, const uint32_t *excl, uint32_t *offsets,
+                                uint32_t n_lt, uint32_t slot_cap, const uint32_t *total,
+                                uint32_t cap, uint32_t detail, DevState *st)
+{
+    const uint32_t G = st->n_events * n_lt;
+    uint32_t n = st->n_outer;
+    if (n > slot_cap) n = slot_cap;
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g <= G; g += gridDim.x * blockDim.x) {
+        uint32_t q = g_base[g];
+        if (q > n) q = n;
+        offsets[g] = g == 0 ? 0u : excl[q];
+        if (g == G && *total > cap) set_fault(st, TRAX_ERR_CAPACITY, detail);
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * Stage 3: triplet prediction.  One warp per pair.
+ * ---------------------------------------------------------------------- */
+struct PredWindow {
+    float zLow[2], zHigh[2];
+    uint32_t zLowSector[2], zHighSector[2];
+    float phiLow, phiHigh;
+    uint32_t phiLowSector, phiHighSector, wrap;
+    bool ok;
+};
+
+/* predictCount (variant 0, TripletThetaPhiPredictor.h:111-166) and
+ * predictStore (variant 1, :320-375): identical except rOrigin
+ * (sqrt(r^2 - tip2) vs sqrt(sqrt(r^2)^2 - tip2)) and zHigh padding
+ * (sigmaPhi vs sigmaZ). */
+__device__ __forceinline__ PredWindow pred_window(const KParams &kp, uint32_t lt, float p1x,
+                                                  float p1y, float p1z, float p2x, float p2y,
+                                                  float p2z, float phi1, float phi2)
+{
+    PredWindow w;
+    const uint32_t layer = kp.l3[lt] - 1;
+    const float sigmaZ = kp.sigma_z[lt];
+    const float sigmaPhi = kp.sigma_phi[lt];
+    const float minLayerRadius = kp.rmin[layer];
+    const float maxLayerRadius = kp.rmax[layer];
+    const float minRadiusCurvature = kp.rmin_curv;
+
+    float tip2 = p1y * (p2x - p1x) - p1x * (p2y - p1y);
+    tip2 *= tip2;
+    tip2 /= ((p2x - p1x) * (p2x - p1x) + (p2y - p1y) * (p2y - p1y));
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+        float rOrigin;
+        if (v == 0) {
+            rOrigin = p1x * p1x + p1y * p1y;
+            rOrigin = sqrtf(rOrigin - tip2);
+        } else {
+            rOrigin = sqrtf(p1x * p1x + p1y * p1y);
+            rOrigin = sqrtf(rOrigin * rOrigin - tip2);
+        }
+        const float cotTheta = (p2z - p1z) / (sqrtf(p2x * p2x + p2y * p2y - tip2) - rOrigin);
+        const float tmp = p1z + (sqrtf(maxLayerRadius * maxLayerRadius - tip2) - rOrigin) * cotTheta;
+        float zLow = p1z + (sqrtf(minLayerRadius * minLayerRadius - tip2) - rOrigin) * cotTheta;
+        float zHigh = (float)(tmp > zLow) * tmp + (float)(tmp < zLow) * zLow;
+        zLow = (float)(tmp > zLow) * zLow + (float)(tmp < zLow) * tmp;
+        zLow -= sigmaZ;
+        zHigh += v == 0 ? sigmaPhi : sigmaZ;
+        const int32_t zl = trax_f2i(floorf((zLow - TRAX_MIN_Z) / kp.sz_z));
+        w.zLowSector[v] = (uint32_t)(zl > 0 ? zl : 0);
+        const uint32_t zh = trax_f2u(floorf((zHigh - TRAX_MIN_Z) / kp.sz_z)) + 1u;
+        w.zHighSector[v] = zh < kp.nz ? zh : kp.nz;
+        w.zLow[v] = zLow;
+        w.zHigh[v] = zHigh;
+    }
+    const float phi = phi2;
+    float tmp = phi1;
+    float dPhi = phi - tmp;
+    dPhi += (dPhi > TRAX_PI_F) ? -2 * TRAX_PI_F : (dPhi < -TRAX_PI_F) ? 2 * TRAX_PI_F : 0;
+    dPhi = fabsf(dPhi);
+    const float dHits = sqrtf((p2x - p1x) * (p2x - p1x) + (p2y - p1y) * (p2y - p1y));
+    tmp = fabsf(trax_acosf(dHits / (2 * minRadiusCurvature)) - trax_acosf(maxLayerRadius / (2 * minRadiusCurvature)));
+    float phiLow = fabsf(trax_acosf(dHits / (2 * minRadiusCurvature)) - trax_acosf(minLayerRadius / (2 * minRadiusCurvature)));
+    dPhi = trax_maxf(dPhi, trax_maxf(tmp, phiLow));
+    float phiHigh = phi + dPhi + sigmaPhi;
+    phiLow = phi - dPhi - sigmaPhi;
+    const bool wrap = phiLow < -TRAX_PI_F || phiHigh > TRAX_PI_F || phiLow > TRAX_PI_F || phiHigh < -TRAX_PI_F;
+    phiLow -= (float)((phiLow > TRAX_PI_F) * 2) * TRAX_PI_F;
+    phiLow += (float)((phiLow < -TRAX_PI_F) * 2) * TRAX_PI_F;
+    phiHigh -= (float)((phiHigh > TRAX_PI_F) * 2) * TRAX_PI_F;
+    phiHigh += (float)((phiHigh < -TRAX_PI_F) * 2) * TRAX_PI_F;
+    w.phiLowSector = trax_f2u(floorf((phiLow - TRAX_MIN_PHI) / kp.sz_phi));
+    const uint32_t ph = trax_f2u(floorf((phiHigh - TRAX_MIN_PHI) / kp.sz_phi)) + 1u;
+    w.phiHighSector = ph < kp.nphi ? ph : kp.nphi;
+    w.phiLow = phiLow;
+    w.phiHigh = phiHigh;
+    w.wrap = wrap ? 1u : 0u;
+    w.ok = w.phiLowSector <= kp.nphi + 1;
+    return w;
+}
+
+template <bool STORE>
+__global__ void __launch_bounds__(256) k_predict(KParams kp, const uint32_t *grid,
+                                                 const float *X, const float *Y, const float *Z,
+                                                 const float *PHI, const uint32_t *EVENT,
+                                                 const uint32_t *LAYER, const uint2 *pairs,
+                                                 const uint32_t *n_pairs_ptr, uint32_t pair_cap,
+                                                 uint32_t *cnt, const uint32_t *excl,
+                                                 uint2 *cands, uint32_t cand_cap, DevState *st)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lt_mask = lanemask_lt();
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    uint32_t n = *n_pairs_ptr;
+    if (n > pair_cap) n = pair_cap;
+    const uint32_t P1 = kp.nphi + 1;
+    const uint32_t E = st->n_events;
+    unsigned long long my_slots = 0, my_trunc = 0;
+    for (uint32_t p = gw; p < n; p += nw) {
+        const uint2 pr = pairs[p];
+        const uint32_t h1 = pr.x, h2 = pr.y;
+        const uint32_t event = EVENT[h1];
+        const uint32_t lt = LAYER[h1] - 1;
+        if (lt >= kp.n_lt || event >= E) {
+            if (lane == 0) {
+                set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_BAD_TRIPLET_INDEX);
+                if (!STORE) cnt[p] = 0;
+            }
+            continue;
+        }
+        const uint32_t *lGrid3 = grid + ((size_t)event * kp.n_layers + (kp.l3[lt] - 1)) * kp.C;
+        const PredWindow w = pred_window(kp, lt, X[h1], Y[h1], Z[h1], X[h2], Y[h2], Z[h2],
+                                         PHI[h1], PHI[h2]);
+        if (!w.ok) {
+            if (lane == 0) {
+                set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_WINDOW_OUTSIDE_GRID);
+                if (!STORE) cnt[p] = 0;
+            }
+            continue;
+        }
+        if (!STORE) {
+            /* count window (A) and store window (B) in one sweep */
+            const uint32_t zlo = min(w.zLowSector[0], w.zLowSector[1]);
+            const uint32_t zhi = max(w.zHighSector[0], w.zHighSector[1]);
+            uint32_t cA = 0, cB = 0;
+            for (uint32_t zs = zlo; zs < zhi; ++zs) {
+                const bool inA = zs >= w.zLowSector[0] && zs < w.zHighSector[0];
+                const bool inB = zs >= w.zLowSector[1] && zs < w.zHighSector[1];
+                const uint32_t rowStart = lGrid3[zs * P1];
+                const uint32_t rowEnd = lGrid3[(zs + 1) * P1];
+                const uint32_t len = rowEnd - rowStart;
+                const uint32_t jlo = lGrid3[zs * P1 + w.phiLowSector];
+                const uint32_t end2 = w.wrap * rowEnd + lGrid3[zs * P1 + w.phiHighSector] - w.wrap * rowStart;
+                for (uint32_t jb = jlo; jb < end2; jb += 32) {
+                    const uint32_t j = jb + lane;
+                    bool a = false, b = false;
+                    if (j < end2) {
+                        const uint32_t idx = j - (uint32_t)(j >= rowEnd) * len;
+                        const float zz = Z[idx];
+                        const bool ph = phi_in(PHI[idx], w.phiLow, w.phiHigh, w.wrap);
+                        a = inA && ph && w.zLow[0] <= zz && zz <= w.zHigh[0];
+                        b = inB && ph && w.zLow[1] <= zz && zz <= w.zHigh[1];
+                    }
+                    cA += __popc(__ballot_sync(kFull, a));
+                    cB += __popc(__ballot_sync(kFull, b));
+                }
+            }
+            const uint32_t emitted = cA < cB ? cA : cB;
+            if (lane == 0) {
+                cnt[p] = emitted;
+                my_slots += cA;
+                my_trunc += cB - emitted;
+            }
+        } else {
+            const uint32_t pos = excl[p];
+            const uint32_t limit = excl[p + 1] - pos;
+            uint32_t written = 0;
+            for (uint32_t zs = w.zLowSector[1]; zs < w.zHighSector[1] && written < limit; ++zs) {
+                const uint32_t rowStart = lGrid3[zs * P1];
+                const uint32_t rowEnd = lGrid3[(zs + 1) * P1];
+                const uint32_t len = rowEnd - rowStart;
+                const uint32_t jlo = lGrid3[zs * P1 + w.phiLowSector];
+                const uint32_t end2 = w.wrap * rowEnd + lGrid3[zs * P1 + w.phiHighSector] - w.wrap * rowStart;
+                for (uint32_t jb = jlo; jb < end2 && written < limit; jb += 32) {
+                    const uint32_t j = jb + lane;
+                    bool b = false;
+                    uint32_t idx = 0;
+                    if (j < end2) {
+                        idx = j - (uint32_t)(j >= rowEnd) * len;
+                        const float zz = Z[idx];
+                        b = w.zLow[1] <= zz && zz <= w.zHigh[1] && phi_in(PHI[idx], w.phiLow, w.phiHigh, w.wrap);
+                    }
+                    const uint32_t m = __ballot_sync(kFull, b);
+                    if (b) {
+                        const uint32_t r = written + __popc(m & lt_mask);
+                        if (r < limit && pos + r < cand_cap) cands[pos + r] = make_uint2(p, idx);
+                    }
+                    written += __popc(m);
+                }
+            }
+        }
+    }
+    if (!STORE && lane == 0 && (my_slots | my_trunc)) {
+        atomicAdd(&st->cand_slots, my_slots);
+        atomicAdd(&st->cand_truncated, my_trunc);
+    }
+}
+
+/* cand_offsets[g+1] = candidates before the first pair of group g+1. */
+__global__ void k_cand_offsets(const uint32_t *pair_offsets, const uint32_t *cexcl,
+                               uint32_t *cand_offsets, uint32_t n_lt, uint32_t pair_cap,
+                               const uint32_t *total, uint32_t cap, DevState *st)
+{
+    const uint32_t G = st->n_events * n_lt;
+    uint32_t n = st->n_pairs;
+    if (n > pair_cap) n = pair_cap;
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g <= G; g += gridDim.x * blockDim.x) {
+        uint32_t q = pair_offsets[g];
+        if (q > n) q = n;
+        cand_offsets[g] = g == 0 ? 0u : cexcl[q];
+        if (g == G && *total > cap) set_fault(st, TRAX_ERR_CAPACITY, TRAX_DETAIL_CAND_CAPACITY);
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * Stage 4: triplet filter + stable compaction in one pass.
+ * ---------------------------------------------------------------------- */
+__device__ __forceinline__ bool filter_cut(const KParams &kp, uint32_t lt, const float *X,
+                                           const float *Y, const float *Z, uint32_t firstHit,
+                                           uint32_t secondHit, uint32_t thirdHit)
+{
+    const float dThetaCut = kp.dtheta[lt];
+    const float dPhiCut = kp.dphi[lt];
+    const float tipCut = kp.tip[lt];
+    const float minRadius = kp.rmin_curv;
+    const float x1 = X[firstHit], y1 = Y[firstHit], z1 = Z[firstHit];
+    const float x2 = X[secondHit], y2 = Y[secondHit], z2 = Z[secondHit];
+    const float x3 = X[thirdHit], y3 = Y[thirdHit], z3 = Z[thirdHit];
+    bool valid = true;
+    float angle1 = trax_atan2f(sqrtf((x2 - x1) * (x2 - x1) + (y2 - y1) * (y2 - y1)), (z2 - z1));
+    float angle2 = trax_atan2f(sqrtf((x3 - x2) * (x3 - x2) + (y3 - y2) * (y3 - y2)), (z3 - z2));
+    float delta = fabsf(angle2 / angle1);
+    valid = valid && (1 - dThetaCut <= delta && delta <= 1 + dThetaCut);
+    angle1 = trax_atan2f((y2 - y1), (x2 - x1));
+    angle2 = trax_atan2f((y3 - y2), (x3 - x2));
+    delta = angle2 - angle1;
+    delta += (delta > TRAX_PI_F) ? -2 * TRAX_PI_F : (delta < -TRAX_PI_F) ? 2 * TRAX_PI_F : 0;
+    valid = valid && (fabsf(delta) <= dPhiCut);
+    const float p1z = x1 * x1 + y1 * y1;
+    const float p2z = x2 * x2 + y2 * y2;
+    const float p3z = x3 * x3 + y3 * y3;
+    const float ax = x2 - x1, ay = y2 - y1, az = p2z - p1z;
+    const float bx = x3 - x1, by = y3 - y1, bz = p3z - p1z;
+    float nx = ay * bz - az * by;
+    float ny = az * bx - ax * bz;
+    float nz = ax * by - ay * bx;
+    const float nlen = sqrtf(nx * nx + ny * ny + nz * nz);
+    nx = nx / nlen; ny = ny / nlen; nz = nz / nlen;
+    const float cOx = (-nx) / (2 * nz);
+    const float cOy = (-ny) / (2 * nz);
+    const float c = -(nx * x1 + ny * y1 + nz * p1z);
+    const float cR = sqrtf((1 - nz * nz - 4 * c * nz) / (4 * nz * nz));
+    float vx = -cOx, vy = -cOy;
+    const float vlen = sqrtf(vx * vx + vy * vy);
+    vx = vx / vlen; vy = vy / vlen;
+    const float pCAx = cOx + cR * vx;
+    const float pCAy = cOy + cR * vy;
+    const float tip = pCAx * pCAx + pCAy * pCAy;
+    valid = valid && (tip <= (tipCut * tipCut));
+    valid = valid && (cR >= minRadius);
+    return valid;
+}
+
+__global__ void __launch_bounds__(256) k_filter(KParams kp, const float *X, const float *Y,
+                                                const float *Z, const uint32_t *LAYER,
+                                                const uint2 *pairs, const uint2 *cands,
+                                                const uint32_t *n_cands_ptr, uint32_t cand_cap,
+                                                uint32_t *t1, uint32_t *t2, uint32_t *t3,
+                                                uint32_t trk_cap, unsigned long long *status,
+                                                DevState *st)
+{
+    uint32_t n = *n_cands_ptr;
+    if (n > cand_cap) n = cand_cap;
+    if (n == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) st->n_trk = 0;
+        return;
+    }
+    lookback_scan<4>(
+        n, &st->tile_ctr[2], status, st,
+        [&](uint32_t i) -> uint32_t {
+            const uint2 c = cands[i];
+            const uint2 pr = pairs[c.x];
+            const uint32_t lt = LAYER[pr.x] - 1;
+            if (lt >= kp.n_lt) {
+                set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_BAD_TRIPLET_INDEX);
+                return 0u;
+            }
+            return filter_cut(kp, lt, X, Y, Z, pr.x, pr.y, c.y) ? 1u : 0u;
+        },
+        [&](uint32_t i, uint32_t pos, uint32_t v) {
+            if (v && pos < trk_cap) {
+                const uint2 c = cands[i];
+                const uint2 pr = pairs[c.x];
+                t1[pos] = pr.x;
+                t2[pos] = pr.y;
+                t3[pos] = c.y;
+            }
+        },
+        [&](uint32_t total) {
+            st->n_trk = total;
+            if (total > trk_cap) set_fault(st, TRAX_ERR_CAPACITY, TRAX_DETAIL_TRACKLET_CAPACITY);
+        });
+}
+
+/* filterOffsetStore (TripletThetaPhiFilter.h:270-292): the last tracklet of
+ * each (event, layer triplet) writes its end; offsets must start zeroed. */
+__global__ void k_trk_offsets(const uint32_t *t1, const uint32_t *EVENT, const uint32_t *LAYER,
+                              uint32_t *offsets, uint32_t n_lt, uint32_t trk_cap, DevState *st)
+{
+    uint32_t n = st->n_trk;
+    if (n > trk_cap) n = trk_cap;
+    const uint32_t G = st->n_events * n_lt;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t h = t1[i];
+        const uint32_t g = EVENT[h] * n_lt + LAYER[h] - 1;
+        bool last = i + 1 == n;
+        if (!last) {
+            const uint32_t hn = t1[i + 1];
+            last = (EVENT[hn] * n_lt + LAYER[hn] - 1) != g;
+        }
+        if (last && g < G) offsets[g + 1] = i + 1;
+    }
+}
+
+/* filterOffsetMonotonizeStore with sequential semantics: a zero entry takes
+ * the previous value, i.e. a running maximum.  One CTA. */
+__global__ void __launch_bounds__(1024) k_monotonize(uint32_t *offsets, uint32_t n_lt, DevState *st)
+{
+    __shared__ uint32_t s_carry;
+    __shared__ uint32_t s_w[32];
+    const uint32_t n = st->n_events * n_lt + 1;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    for (uint32_t b = 0; b < n; b += blockDim.x) {
+        const uint32_t i = b + threadIdx.x;
+        uint32_t v = i < n ? offsets[i] : 0u;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFull, v, d);
+            if (lane >= d) v = max(v, y);
+        }
+        if (lane == 31) s_w[wid] = v;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t t = lane < (int)(blockDim.x >> 5) ? s_w[lane] : 0u;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t y = __shfl_up_sync(kFull, t, d);
+                if (lane >= d) t = max(t, y);
+            }
+            s_w[lane] = t;
+        }
+        __syncthreads();
+        uint32_t r = max(v, s_carry);
+        if (wid > 0) r = max(r, s_w[wid - 1]);
+        if (i < n) offsets[i] = r;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) s_carry = r;
+        __syncthreads();
+    }
+}
+
+}  // namespace trax

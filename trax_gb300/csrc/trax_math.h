@@ -1,0 +1,175 @@
+/*
+ * trax_math.h -- project-owned FP32 math for the triplet-seeding path.
+ *
+ * Every transcendental the reference kernels call (OpenCL atan2, acos, atan;
+ * GridBuilder.h:81, PairGeneratorBeamspot.h:138-145,212,
+ * TripletThetaPhiPredictor.h:138-150,208, TripletThetaPhiFilter.h:86-99) is
+ * defined here once, as __host__ __device__ code, so that the CUDA kernels and
+ * the CPU oracle execute the same IEEE-754 single-precision operations in the
+ * same order.  The OpenCL built-ins were vendor defined (OpenCL 1.1 allows up
+ * to 6 ulp for atan2), so bit-level agreement is defined against these
+ * functions, not against any particular OpenCL runtime.
+ *
+ * Build contract (checked by the build scripts):
+ *   device: nvcc -fmad=false -prec-div=true -prec-sqrt=true -ftz=false
+ *   host:   gcc/g++ -ffp-contract=off, no -ffast-math
+ * With these flags every +,-,*,/ and sqrtf below is one correctly rounded
+ * IEEE operation on both sides, and nothing is contracted into an FMA.
+ *
+ * Methods (all written for this project):
+ *   trax_atan01  atan(t) for t in [0,1] as t + t^3*P(t^2), P of degree 8,
+ *                coefficients fitted by fit_atan.py (Lawson-weighted least
+ *                squares for minimax relative error), float32 Horner.
+ *                Max error 1.1 ulp on [0,1].
+ *   trax_atanf   reduction atan(x) = pi/2 - atan(1/x) for |x| > 1, odd symmetry.
+ *   trax_atan2f  quadrant reduction on t = min(|x|,|y|)/max(|x|,|y|).
+ *   trax_acosf   half-angle identity acos(x) = 2*atan(sqrt((1-x)/(1+x))).
+ */
+#ifndef TRAX_MATH_H
+#define TRAX_MATH_H
+
+#include <stdint.h>
+#include <math.h>
+
+#if defined(__CUDACC__)
+#define TRAX_HD __host__ __device__ __forceinline__
+#else
+#define TRAX_HD static inline
+#endif
+
+/* OpenCL M_PI_F: the float nearest to pi (3.14159274f). */
+#define TRAX_PI_F 0x1.921fb6p+1f
+#define TRAX_TWO_PI_F 0x1.921fb6p+2f
+#define TRAX_PIO2_F 0x1.921fb6p+0f
+#define TRAX_3PIO4_F 0x1.2d97c8p+1f
+#define TRAX_PIO4_F 0x1.921fb6p-1f
+
+/* Grid extent (Grid.h:33-37): MIN_Z/MAX_Z = -/+300 cm, MIN/MAX_PHI = -/+ (float)M_PI. */
+#define TRAX_MIN_Z (-300.0f)
+#define TRAX_MAX_Z (300.0f)
+#define TRAX_MIN_PHI (-TRAX_PI_F)
+#define TRAX_MAX_PHI (TRAX_PI_F)
+
+TRAX_HD float trax_atan01(float t)
+{
+    const float s = t * t;
+    float p = -0x1.d63692p-10f;
+    p = p * s; p = p + 0x1.65aaa0p-7f;
+    p = p * s; p = p + -0x1.fed606p-6f;
+    p = p * s; p = p + 0x1.daccb0p-5f;
+    p = p * s; p = p + -0x1.583592p-4f;
+    p = p * s; p = p + 0x1.c09a6ep-4f;
+    p = p * s; p = p + -0x1.2421c4p-3f;
+    p = p * s; p = p + 0x1.9991fep-3f;
+    p = p * s; p = p + -0x1.55553ep-2f;
+    float r = t * s;
+    r = r * p;
+    return t + r;
+}
+
+TRAX_HD float trax_atanf(float x)
+{
+    const float a = fabsf(x);
+    if (!(a == a)) return x; /* NaN */
+    float r;
+    if (a > 1.0f) {
+        const float inv = 1.0f / a; /* 1/inf = 0 -> pi/2 */
+        r = TRAX_PIO2_F - trax_atan01(inv);
+    } else {
+        r = trax_atan01(a);
+    }
+    return copysignf(r, x);
+}
+
+/* Result lies in [-TRAX_PI_F, TRAX_PI_F]; signed zeros follow IEEE atan2. */
+TRAX_HD float trax_atan2f(float y, float x)
+{
+    if (!(x == x) || !(y == y)) return x + y;
+    const float ax = fabsf(x);
+    const float ay = fabsf(y);
+    float r;
+    if (ay == 0.0f) {
+        r = signbit(x) ? TRAX_PI_F : 0.0f;
+    } else if (ax == 0.0f) {
+        r = TRAX_PIO2_F;
+    } else if (isinf(ax) && isinf(ay)) {
+        r = signbit(x) ? TRAX_3PIO4_F : TRAX_PIO4_F;
+    } else {
+        const int yb = ay > ax;
+        const float mx = yb ? ay : ax;
+        const float mn = yb ? ax : ay;
+        const float t = mn / mx;
+        r = trax_atan01(t);
+        if (yb) r = TRAX_PIO2_F - r;
+        if (x < 0.0f) r = TRAX_PI_F - r;
+    }
+    return copysignf(r, y);
+}
+
+TRAX_HD float trax_acosf(float x)
+{
+    const float num = 1.0f - x;
+    const float den = 1.0f + x;
+    const float q = num / den;
+    const float s = sqrtf(q);
+    return 2.0f * trax_atanf(s);
+}
+
+/* OpenCL sign(): 1, -1, +/-0 for +/-0, 0 for NaN. */
+TRAX_HD float trax_signf(float v)
+{
+    if (v > 0.0f) return 1.0f;
+    if (v < 0.0f) return -1.0f;
+    if (v == 0.0f) return v;
+    return 0.0f;
+}
+
+/* OpenCL max()/min() on floats: "y if x < y, otherwise x" (and mirror). */
+TRAX_HD float trax_maxf(float x, float y) { return (x < y) ? y : x; }
+TRAX_HD float trax_minf(float x, float y) { return (y < x) ? y : x; }
+
+/*
+ * Float to integer conversions as the reference's implicit casts compile on a
+ * two's-complement target: `uint u = floor(v)` truncates toward zero into a
+ * 64-bit integer and keeps the low 32 bits (so -1.0f -> 0xFFFFFFFF);
+ * `(int) floor(v)` saturates to INT_MIN when out of range.  NaN maps to 0 and
+ * INT_MIN respectively.  Written with explicit range checks so that host and
+ * device agree for every input.
+ */
+TRAX_HD uint32_t trax_f2u(float v)
+{
+    if (!(v == v)) return 0u;
+    if (v >= 9.2233715e18f || v <= -9.2233715e18f) return 0u;
+    return (uint32_t)(uint64_t)(int64_t)v;
+}
+
+TRAX_HD int32_t trax_f2i(float v)
+{
+    if (!(v == v)) return INT32_MIN;
+    if (v >= 2147483648.0f || v < -2147483648.0f) return INT32_MIN;
+    return (int32_t)v;
+}
+
+/* Cell of a hit in its layer grid (GridBuilder.h:80-84). */
+TRAX_HD uint32_t trax_sector_z(float z, float sector_size_z)
+{
+    return trax_f2u(floorf((z - TRAX_MIN_Z) / sector_size_z));
+}
+
+TRAX_HD uint32_t trax_sector_phi(float phi, float sector_size_phi)
+{
+    return trax_f2u(floorf((phi - TRAX_MIN_PHI) / sector_size_phi));
+}
+
+/* GridConfig::sectorSizeZ/Phi (Grid.h:9-15), evaluated in float. */
+TRAX_HD float trax_sector_size_z(uint32_t n_sectors_z)
+{
+    return (TRAX_MAX_Z - TRAX_MIN_Z) / (float)n_sectors_z;
+}
+
+TRAX_HD float trax_sector_size_phi(uint32_t n_sectors_phi)
+{
+    return (TRAX_MAX_PHI - TRAX_MIN_PHI) / (float)n_sectors_phi;
+}
+
+#endif /* TRAX_MATH_H */
