@@ -1,0 +1,438 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 triplet-seeding path; prints one JSON line.
+
+A step is one pass of the whole path (grid build -> pairs -> prediction ->
+filter) over one batch of synthetic events of the named workload.
+  value  events/s with the batch already resident in HBM (CUDA-graph replay)
+  e2e    events/s through trax_seed_batch with pinned host buffers: H2D of
+         the hit columns, the graph, D2H of the tracklets, every step
+Also reported: pairs/s and triplets/s, the plain per-event GPU form (one
+event per launch sequence, no graph), per-kernel times, the dominant
+kernel's HBM roofline, the CPU oracle on all host cores, and SM clocks
+sampled during the timed region.
+
+--impl reference times the CPU restatement of the reference's algorithm
+(the reference itself cannot be built here: no OpenCL, clever, Boost or
+protobuf-2.4), on all host threads, on a bounded sample of the same workload.
+
+Multi-GPU: replicas only (events are independent); every rank runs its own
+batch, the time is the max over ranks, value = all ranks' events / time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="multimuon-1000trk")
+    ap.add_argument("--events", type=int, default=2048, help="events per step (batch)")
+    ap.add_argument("--per-event-sample", type=int, default=64)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------------------
+# distributed plumbing (host side only: barrier and max over ranks)
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, v: float) -> float:
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+# --------------------------------------------------------------------------
+# clocks sampled during the timed region
+
+CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+class ClockSampler:
+    def __init__(self, device: int):
+        self.proc = None
+        self.device = device
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={CLOCK_FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        if self.proc is None:
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# --------------------------------------------------------------------------
+# algorithmic bytes per kernel (traffic a perfect kernel must move)
+
+def algorithmic_bytes(kernel, b, w, counts):
+    N = b.n_hits
+    E, L = b.n_events, b.n_layers
+    C = (w.n_sectors_z + 1) * (w.n_sectors_phi + 1)
+    M, K, R = counts["n_pairs"], counts["n_candidates"], counts["n_tracklets"]
+    ln = b.layer_nhits.astype(np.int64)
+    cfg = w.config()
+    n1 = sum(int(ln[:, cfg.triplets[t].layer1 - 1].sum()) for t in range(cfg.n_layer_triplets))
+    n2 = sum(int(ln[:, cfg.triplets[t].layer2 - 1].sum()) for t in range(cfg.n_layer_triplets))
+    n3 = sum(int(ln[:, cfg.triplets[t].layer3 - 1].sum()) for t in range(cfg.n_layer_triplets))
+    table = {
+        "grid_build": N * (12 + 28 + 28) + E * L * C * 4 * 3,
+        "pair_count": 12 * (n1 + n2) + 4 * n2,
+        "pair_store": 12 * (n1 + n2) + 4 * n2 + 8 * M,
+        "predict_count": M * (8 + 24) + 12 * n3 + 4 * M,
+        "predict_store": M * (8 + 24) + 12 * n3 + 4 * M + 8 * K,
+        "filter": K * (8 + 8 + 36) + 12 * R,
+    }
+    return table.get(kernel)
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def traffic_from_profiles(kernel, workload):
+    """Per-launch DRAM bytes for `kernel` from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(p) as f:
+            t = json.load(f)
+        e = t[workload][kernel]
+        return e
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+# --------------------------------------------------------------------------
+# CPU restatement (oracle) timing
+
+def cpu_events_per_s(b, w, seconds, threads):
+    import oracle
+    cfg = w.config()
+    t0 = time.perf_counter()
+    probe = b.slice_events(0, min(4, b.n_events))
+    oracle.run(probe, cfg, w.grid(probe.n_events), 4, 256, threads)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    n = int(max(1, min(b.n_events, probe.n_events * seconds / dt)))
+    sample = b.slice_events(0, n)
+    t0 = time.perf_counter()
+    r = oracle.run(sample, cfg, w.grid(n), 4, 256, threads)
+    dt = time.perf_counter() - t0
+    return n / dt, n, dt, r["stats"]
+
+
+def run_reference(args, dist):
+    from trax_gb300 import gen
+    w = gen.WORKLOADS[args.workload]
+    if dist.rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    b = gen.generate_batch(w, args.events)
+    per_step_s = max(2.0, 150.0 / max(1, args.steps + args.warmup))
+    import oracle
+    cfg = w.config()
+    t0 = time.perf_counter()
+    probe = b.slice_events(0, min(4, b.n_events))
+    oracle.run(probe, cfg, w.grid(probe.n_events), 4, 256, threads)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    n = int(max(1, min(b.n_events, probe.n_events * per_step_s / dt)))
+    sample = b.slice_events(0, n)
+    for _ in range(args.warmup):
+        oracle.run(sample, cfg, w.grid(n), 4, 256, threads)
+    times = []
+    stats = None
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        r = oracle.run(sample, cfg, w.grid(n), 4, 256, threads)
+        times.append(time.perf_counter() - t0)
+        stats = r["stats"]
+    total = sum(times)
+    value = n * args.steps / total
+    line = {
+        "impl": "reference", "metric": "events/s", "value": round(value, 3), "unit": "events/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000 * total / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "events_per_step": n,
+                   "grid": f"{w.n_sectors_z}x{w.n_sectors_phi}", "layer_triplets": w.n_triplets,
+                   "sample": f"first {n} of the {args.events}-event batch per step"},
+        "cpu_baseline": {"value": round(value, 3), "unit": "events/s", "cores": threads,
+                         "kind": "port",
+                         "sample": f"{n} events per step, OpenMP over {threads} threads"},
+        "e2e": {"value": round(value, 3), "unit": "events/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "triplets_per_s": round(stats["tracklets"] * args.steps / total, 1),
+        "pairs_per_s": round(stats["pairs"] * args.steps / total, 1),
+        "note": "reference OpenCL path unbuildable here; CPU restatement of its algorithm",
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------
+
+def run_ours(args, dist):
+    from trax_gb300 import Context, gen
+    from trax_gb300.ops import Pipeline
+    from trax_gb300.runtime import PinnedBuffer
+    import ctypes as C
+
+    w = gen.WORKLOADS[args.workload]
+    ctx = Context(dist.local)
+    B = args.events
+    b = gen.generate_batch(w, B, first_event=dist.rank * B)
+    cfg, grid = w.config(), w.grid(B)
+    N = b.n_hits
+    caps = [12 * N + 4096, 12 * N + 4096, 2 * N + 4096]
+    for _ in range(3):
+        p = Pipeline(ctx, cfg, grid, B, N, *caps)
+        _, _, counts = p.seed(b)
+        if counts["status"] != 5:
+            break
+        caps = [max(c, 2 * int(v)) for c, v in zip(
+            caps, (counts["n_pairs"], counts["n_candidates"], counts["n_tracklets"]))]
+    if counts["status"] != 0:
+        raise SystemExit(f"device status {counts}")
+
+    # ---- device-resident value: graph replay on staged inputs -------------
+    p.stage(b)
+    for _ in range(args.warmup):
+        p.run_staged()
+    ctx.synchronize()
+    dist.barrier()
+    with ClockSampler(dist.local) as clk:
+        ctx.synchronize()
+        ctx.timer_record(62)
+        for _ in range(args.steps):
+            p.run_staged()
+        ctx.timer_record(63)
+        ctx.synchronize()
+    dist.barrier()
+    ms_total = ctx.timer_elapsed_ms(62, 63)
+    ms_total = dist.max(ms_total)
+    launches = int(ctx.lib.trax_kernel_launches(ctx.h))
+    counts = ctx.counts()
+    if counts["status"] != 0:
+        raise SystemExit(f"device status after timed run {counts}")
+    events_all = dist.sum(B)
+    value = events_all * args.steps / (ms_total / 1000.0)
+
+    # ---- per-kernel times (separate profiled run) ------------------------
+    ctx._check(ctx.lib.trax_set_profiling(ctx.h, 1))
+    p.run_staged()  # captures the profiled graph
+    kt = {}
+    reps = 5
+    for _ in range(reps):
+        p.run_staged()
+        ms = (C.c_float * 64)()
+        names = (C.c_char_p * 64)()
+        n = C.c_int()
+        ctx._check(ctx.lib.trax_kernel_times(ctx.h, ms, names, 64, C.byref(n)))
+        for i in range(n.value):
+            kt.setdefault(names[i].decode(), []).append(ms[i])
+    ctx._check(ctx.lib.trax_set_profiling(ctx.h, 0))
+    kernel_ms = {k: statistics.median(v) for k, v in kt.items()}
+    top = max(kernel_ms, key=kernel_ms.get)
+    peak, peak_src = hbm_peak()
+    alg = algorithmic_bytes(top, b, w, counts)
+    roofline = None
+    if alg is not None:
+        achieved = alg / (kernel_ms[top] / 1000.0) / 1e9
+        traffic = traffic_from_profiles(top, args.workload)
+        roofline = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 2),
+                    "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5),
+                    "traffic": traffic, "algorithmic_bytes": int(alg),
+                    "launch_ms": round(kernel_ms[top], 4), "peak_source": peak_src}
+    stage_bytes = {k: algorithmic_bytes(k, b, w, counts) for k in kernel_ms}
+    kernels = {k: {"ms": round(v, 4),
+                   "gbs": (round(stage_bytes[k] / (v / 1000) / 1e9, 1) if stage_bytes[k] and v > 0
+                           else None)} for k, v in kernel_ms.items()}
+
+    # ---- e2e through trax_seed_batch with pinned host buffers ------------
+    cols = b.columns()
+    pinned = []
+    pb = []
+    for c in cols:
+        buf = PinnedBuffer(ctx, c.nbytes, c.dtype)
+        buf.array[:] = c
+        pinned.append(buf)
+        pb.append(buf.array)
+    from trax_gb300.gen import EventBatch
+    pinned_batch = EventBatch(*pb, b.layer_nhits)
+    for _ in range(args.warmup):
+        p.seed(pinned_batch)
+    dist.barrier()
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    trk = None
+    for _ in range(args.steps):
+        trk, off, c2 = p.seed(pinned_batch)
+    e2e_s = time.perf_counter() - t0
+    e2e_s = dist.max(e2e_s)
+    h2d = sum(c.nbytes for c in cols) + b.layer_nhits.nbytes
+    d2h = int(trk.nbytes + off.nbytes + 72)
+    e2e = {"value": round(events_all * args.steps / e2e_s, 2), "unit": "events/s",
+           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h,
+           "ms_per_step": round(1000 * e2e_s / args.steps, 3)}
+    for x in pinned:
+        x.free()
+
+    # ---- plain per-event GPU form (no graph, one event per sequence) -----
+    S = min(args.per_event_sample, B)
+    singles = [b.slice_events(e, 1) for e in range(S)]
+    pe = Pipeline(ctx, cfg, w.grid(1), 1, max(s.n_hits for s in singles) + 1, *caps)
+    for s in singles[:2]:
+        pe.stage(s)
+        ctx._check(ctx.lib.trax_run_staged_eager(ctx.h))
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for s in singles:
+        pe.stage(s)
+        ctx._check(ctx.lib.trax_run_staged_eager(ctx.h))
+        ctx.synchronize()
+    per_event = S / (time.perf_counter() - t0)
+
+    # ---- CPU baseline (rank 0, N=1 only) ----------------------------------
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, n, dt, _ = cpu_events_per_s(b, w, args.cpu_seconds, threads)
+        cpu = {"value": round(v, 3), "unit": "events/s", "cores": threads, "kind": "port",
+               "sample": f"first {n} events of the batch, {dt:.1f} s, OpenMP oracle"}
+
+    clocks = clk.summary()
+    if dist.rank == 0:
+        mb_resident = (N * (28 + 36) + counts["n_pairs"] * 8 + counts["n_candidates"] * 8) / 1e6
+        line = {
+            "metric": "events/s", "value": round(value, 2), "unit": "events/s",
+            "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms_total / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "events_per_step": B, "hits_per_step": N,
+                       "layers": w.n_layers, "layer_triplets": w.n_triplets,
+                       "grid": f"{w.n_sectors_z}x{w.n_sectors_phi}",
+                       "form": "batched: one CUDA graph per step",
+                       "l2": f"inputs larger than L2 ({mb_resident:.0f} MB touched per step)",
+                       "parallelism": f"replicas x{dist.world}"},
+            "e2e": e2e,
+            "pairs_per_s": round(counts["n_pairs"] * dist.world * args.steps / (ms_total / 1000), 1),
+            "triplets_per_s": round(counts["n_tracklets"] * dist.world * args.steps / (ms_total / 1000), 1),
+            "per_event_form": {"value": round(per_event, 2), "unit": "events/s",
+                               "sample": f"{S} events, one launch sequence each, no graph"},
+            "batched_over_per_event": round(value / dist.world / per_event, 2),
+            "roofline": roofline,
+            "kernels": kernels,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": launches * args.steps,
+            "counts_per_step": {k: counts[k] for k in ("n_hits", "n_pairs", "pair_slots",
+                                                        "n_candidates", "cand_slots",
+                                                        "cand_truncated", "n_tracklets")},
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

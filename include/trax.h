@@ -170,6 +170,8 @@ void trax_ctx_destroy(trax_ctx *ctx);
 /* cudaStream_t passed as void*; NULL selects the context's own stream. */
 trax_status trax_ctx_set_stream(trax_ctx *ctx, void *stream);
 void *trax_ctx_get_stream(trax_ctx *ctx);
+/* Message of the last failed call on ctx; with ctx == NULL, of the last
+ * failed trax_ctx_create. */
 const char *trax_ctx_last_error(const trax_ctx *ctx);
 /* Waits for the stream; returns the device status word (or a CUDA error). */
 trax_status trax_ctx_synchronize(trax_ctx *ctx);
@@ -284,6 +286,16 @@ trax_status trax_seed_batch(trax_ctx *ctx, const trax_event_batch *in, trax_batc
  * by trax_stage_batch; runs the graph only (asynchronous). */
 trax_status trax_stage_batch(trax_ctx *ctx, const trax_event_batch *in);
 trax_status trax_run_staged(trax_ctx *ctx);
+/* The same chain launched kernel by kernel, without a graph (the plain form). */
+trax_status trax_run_staged_eager(trax_ctx *ctx);
+
+/* Per-kernel timing of the batched chain: when on, CUDA events are recorded
+ * between kernels (also inside the graph).  trax_kernel_times returns the
+ * durations (ms) and names of the last run's kernels in launch order. */
+trax_status trax_set_profiling(trax_ctx *ctx, int on);
+trax_status trax_kernel_times(trax_ctx *ctx, float *ms, const char **names, int max_n, int *n);
+/* Kernels launched by the last pipeline enqueue (graph capture or eager). */
+int trax_kernel_launches(const trax_ctx *ctx);
 
 #ifdef __cplusplus
 }

@@ -109,7 +109,11 @@ def test_device_math_bit_exact(gpu_ctx):
         gpu_ctx._check(gpu_ctx.lib.trax_eval_math(gpu_ctx.h, fn, x.ptr, y.ptr, out.ptr, n))
         got = out.download(n)
         host = oracle.math_batch(fn, a if fn != 1 else u, bb if fn == 0 else None)
-        assert np.array_equal(bits(got), bits(host)), fn
+        # NaN results may differ in payload bits (the GPU returns the
+        # canonical NaN); every other result must match bit for bit
+        same = (bits(got) == bits(host)) | (np.isnan(got) & np.isnan(host))
+        bad = np.nonzero(~same)[0]
+        assert bad.size == 0, (fn, bad[:8], got[bad[:8]], host[bad[:8]])
 
 
 def test_batched_pipeline_equals_stages(gpu_ctx):

@@ -66,6 +66,11 @@ struct trax_ctx {
     int gb_warps = 0, gb_per_sm = 0;
     cudaGraphExec_t graph = nullptr;
     uint32_t staged_events = 0, staged_hits = 0;
+    /* per-kernel timing marks (events recorded between launches) */
+    bool profiling = false;
+    int n_marks = 0;
+    const char *mark_names[kTimerSlots] = {};
+    int launches = 0;                     /* kernels enqueued by the last pipeline */
 };
 
 namespace {
@@ -173,6 +178,29 @@ trax_status grid_plan(trax_ctx *ctx, uint32_t C)
     return TRAX_OK;
 }
 
+/* Called after every kernel launch: counts it and, when profiling, records
+ * a timing event named after it (timer slot 0 is the pipeline start). */
+trax_status mark(trax_ctx *ctx, const char *name)
+{
+    ++ctx->launches;
+    if (!ctx->profiling || ctx->n_marks + 1 >= kTimerSlots) return TRAX_OK;
+    ++ctx->n_marks;
+    ctx->mark_names[ctx->n_marks] = name;
+    /* External: inside a stream capture the record becomes a graph node that
+     * fires on every replay */
+    CK(cudaEventRecordWithFlags(ctx->timers[ctx->n_marks], ctx->stream, cudaEventRecordExternal));
+    return TRAX_OK;
+}
+
+trax_status begin_marks(trax_ctx *ctx)
+{
+    ctx->n_marks = 0;
+    ctx->launches = 0;
+    if (ctx->profiling)
+        CK(cudaEventRecordWithFlags(ctx->timers[0], ctx->stream, cudaEventRecordExternal));
+    return TRAX_OK;
+}
+
 trax_status set_sizes(trax_ctx *ctx, uint32_t n_events, uint32_t n_hits)
 {
     trax_status s = ensure_stage(ctx, 2);
@@ -201,7 +229,7 @@ trax_status enqueue_grid(trax_ctx *ctx, const InCols &in, const SortedCols &out,
     k_grid_build<<<blocks, W * 32, smem, ctx->stream>>>(kp, in, out, seg_start, seg_n, grid,
                                                         ctx->d_state);
     CK(cudaGetLastError());
-    return TRAX_OK;
+    return mark(ctx, "grid_build");
 }
 
 trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *grid, uint2 *pairs,
@@ -223,22 +251,27 @@ trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *gr
     DevState *st = ctx->d_state;
 
     k_pair_groups<<<1, 1024, 0, ctx->stream>>>(kp, grid, g_start, g_base, st);
+    if ((s = mark(ctx, "pair_groups")) != TRAX_OK) return s;
     k_pair_slots<<<ctx->blk_small, 256, 0, ctx->stream>>>(kp, g_start, g_base, slots, slot_cap, st);
+    if ((s = mark(ctx, "pair_slots")) != TRAX_OK) return s;
     k_pair<false><<<ctx->blk_pair, 256, 0, ctx->stream>>>(kp, grid, h.x, h.y, h.z, h.phi, slots,
                                                           slot_cap, pcnt, nullptr, nullptr, 0, st);
+    if ((s = mark(ctx, "pair_count")) != TRAX_OK) return s;
     CK(cudaMemsetAsync(&st->tile_ctr[0], 0, 4, ctx->stream));
     CK(cudaMemsetAsync(ctx->st0.p, 0, (size_t)ntile * 8, ctx->stream));
     k_scan<kScanItems><<<ctx->blk_scan, kScanThreads, 0, ctx->stream>>>(
         pcnt, pexcl, &st->n_outer, slot_cap, &st->n_pairs, 0,
         (unsigned long long *)ctx->st0.p, st);
+    if ((s = mark(ctx, "pair_scan")) != TRAX_OK) return s;
     k_group_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(g_base, pexcl, pair_offsets, kp.n_lt,
                                                              slot_cap, &st->n_pairs, pair_cap,
                                                              TRAX_DETAIL_PAIR_CAPACITY, st);
+    if ((s = mark(ctx, "pair_offsets")) != TRAX_OK) return s;
     k_pair<true><<<ctx->blk_pair, 256, 0, ctx->stream>>>(kp, grid, h.x, h.y, h.z, h.phi, slots,
                                                          slot_cap, nullptr, pexcl, pairs, pair_cap,
                                                          st);
     CK(cudaGetLastError());
-    return TRAX_OK;
+    return mark(ctx, "pair_store");
 }
 
 trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *grid,
@@ -259,19 +292,22 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
     k_predict<false><<<ctx->blk_pred, 256, 0, ctx->stream>>>(
         kp, grid, h.x, h.y, h.z, h.phi, h.event, h.layer, pairs, &st->n_pairs, pair_cap, ccnt,
         nullptr, nullptr, 0, st);
+    if ((s = mark(ctx, "predict_count")) != TRAX_OK) return s;
     CK(cudaMemsetAsync(&st->tile_ctr[1], 0, 4, ctx->stream));
     CK(cudaMemsetAsync(ctx->st1.p, 0, (size_t)ntile * 8, ctx->stream));
     k_scan<kScanItems><<<ctx->blk_scan, kScanThreads, 0, ctx->stream>>>(
         ccnt, cexcl, &st->n_pairs, pair_cap, &st->n_cands, 1,
         (unsigned long long *)ctx->st1.p, st);
+    if ((s = mark(ctx, "predict_scan")) != TRAX_OK) return s;
     k_cand_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(pair_offsets, cexcl, cand_offsets,
                                                             kp.n_lt, pair_cap, &st->n_cands,
                                                             cand_cap, st);
+    if ((s = mark(ctx, "predict_offsets")) != TRAX_OK) return s;
     k_predict<true><<<ctx->blk_pred, 256, 0, ctx->stream>>>(
         kp, grid, h.x, h.y, h.z, h.phi, h.event, h.layer, pairs, &st->n_pairs, pair_cap, nullptr,
         cexcl, cands, cand_cap, st);
     CK(cudaGetLastError());
-    return TRAX_OK;
+    return mark(ctx, "predict_store");
 }
 
 trax_status enqueue_filter(trax_ctx *ctx, const SortedCols &h, const uint2 *pairs,
@@ -290,11 +326,13 @@ trax_status enqueue_filter(trax_ctx *ctx, const SortedCols &h, const uint2 *pair
     k_filter<<<ctx->blk_filter, 256, 0, ctx->stream>>>(kp, h.x, h.y, h.z, h.layer, pairs, cands,
                                                        &st->n_cands, cand_cap, t1, t2, t3, trk_cap,
                                                        (unsigned long long *)ctx->st2.p, st);
+    if ((s = mark(ctx, "filter")) != TRAX_OK) return s;
     k_trk_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(t1, h.event, h.layer, trk_offsets,
                                                            kp.n_lt, trk_cap, st);
+    if ((s = mark(ctx, "filter_offsets")) != TRAX_OK) return s;
     k_monotonize<<<1, 1024, 0, ctx->stream>>>(trk_offsets, kp.n_lt, st);
     CK(cudaGetLastError());
-    return TRAX_OK;
+    return mark(ctx, "filter_monotonize");
 }
 
 SortedCols sorted_from(const trax_sorted_hits *o)
@@ -352,7 +390,7 @@ __global__ void k_eval_math(int fn, const float *a, const float *b, float *out, 
         out[i] = fn == 0 ? trax_atan2f(a[i], b[i]) : fn == 1 ? trax_acosf(a[i]) : trax_atanf(a[i]);
 }
 
-std::string g_validate_msg;
+std::string g_create_error;
 
 }  // namespace
 
@@ -455,7 +493,8 @@ trax_status trax_ctx_create(trax_ctx **out, int device)
     trax_ctx *ctx = new trax_ctx();
     ctx->device = device;
     auto bail = [&](cudaError_t e) {
-        (void)e;
+        g_create_error = std::string("trax_ctx_create: ") + cudaGetErrorString(e);
+        cudaGetLastError();
         delete ctx;
         return TRAX_ERR_DEVICE;
     };
@@ -473,8 +512,11 @@ trax_status trax_ctx_create(trax_ctx **out, int device)
     if ((e = cudaEventCreateWithFlags(&ctx->stage_free, cudaEventDisableTiming)) != cudaSuccess) return bail(e);
     for (int i = 0; i < kTimerSlots; ++i)
         if ((e = cudaEventCreate(&ctx->timers[i])) != cudaSuccess) return bail(e);
+    cudaFuncAttributes fa{};
+    if ((e = cudaFuncGetAttributes(&fa, k_grid_build)) != cudaSuccess) return bail(e);
+    ctx->smem_optin = (size_t)optin - fa.sharedSizeBytes;
     if ((e = cudaFuncSetAttribute(k_grid_build, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  optin)) != cudaSuccess) return bail(e);
+                                  (int)ctx->smem_optin)) != cudaSuccess) return bail(e);
     int b = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair<false>, 256, 0);
     ctx->blk_pair = ctx->sm_count * std::max(b, 1);
@@ -528,7 +570,10 @@ trax_status trax_ctx_set_stream(trax_ctx *ctx, void *stream)
 
 void *trax_ctx_get_stream(trax_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 
-const char *trax_ctx_last_error(const trax_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+const char *trax_ctx_last_error(const trax_ctx *ctx)
+{
+    return ctx ? ctx->err.c_str() : g_create_error.c_str();
+}
 
 int trax_ctx_sm_count(const trax_ctx *ctx) { return ctx ? ctx->sm_count : 0; }
 
@@ -827,8 +872,10 @@ trax_status enqueue_pipeline(trax_ctx *ctx)
     const SortedCols sc = reserved_sorted(ctx);
     uint32_t *grid = (uint32_t *)ctx->grid_buf.p;
     const uint32_t *seg = (const uint32_t *)ctx->r_seg.p;
+    trax_status s = begin_marks(ctx);
+    if (s != TRAX_OK) return s;
     CK(cudaMemsetAsync(&ctx->d_state->n_outer, 0, sizeof(DevState) - 8, ctx->stream));
-    trax_status s = enqueue_grid(ctx, ic, sc, seg, seg + nseg, grid, nseg);
+    s = enqueue_grid(ctx, ic, sc, seg, seg + nseg, grid, nseg);
     if (s != TRAX_OK) return s;
     const uint32_t slot_cap = ctx->r_hits * T + 1;
     s = enqueue_pairs(ctx, sc, grid, (uint2 *)ctx->pairs_buf.p, (uint32_t *)ctx->pair_off.p,
@@ -920,6 +967,43 @@ trax_status trax_run_staged(trax_ctx *ctx)
         }
     }
     CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+    return TRAX_OK;
+}
+
+trax_status trax_run_staged_eager(trax_ctx *ctx)
+{
+    if (!ctx || !ctx->reserved) return TRAX_ERR_BAD_ARG;
+    fill_grid_params(ctx->kp, &ctx->r_grid);
+    return enqueue_pipeline(ctx);
+}
+
+trax_status trax_set_profiling(trax_ctx *ctx, int on)
+{
+    if (!ctx) return TRAX_ERR_BAD_ARG;
+    if ((bool)on != ctx->profiling && ctx->graph) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        cudaGraphExecDestroy(ctx->graph);
+        ctx->graph = nullptr;
+    }
+    ctx->profiling = on != 0;
+    return TRAX_OK;
+}
+
+int trax_kernel_launches(const trax_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+trax_status trax_kernel_times(trax_ctx *ctx, float *ms, const char **names, int max_n, int *n)
+{
+    if (!ctx || !n) return TRAX_ERR_BAD_ARG;
+    *n = 0;
+    if (!ctx->profiling) return TRAX_OK;
+    CK(cudaEventSynchronize(ctx->timers[ctx->n_marks]));
+    for (int i = 1; i <= ctx->n_marks && *n < max_n; ++i) {
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, ctx->timers[i - 1], ctx->timers[i]));
+        if (ms) ms[*n] = t;
+        if (names) names[*n] = ctx->mark_names[i];
+        ++*n;
+    }
     return TRAX_OK;
 }
 

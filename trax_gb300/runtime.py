@@ -70,6 +70,11 @@ _SIGS = {
                                   C.POINTER(A.TraxBatchResult)]),
     "trax_stage_batch": (C.c_int, [C.c_void_p, C.POINTER(A.TraxEventBatch)]),
     "trax_run_staged": (C.c_int, [C.c_void_p]),
+    "trax_run_staged_eager": (C.c_int, [C.c_void_p]),
+    "trax_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "trax_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_char_p),
+                                    C.c_int, C.POINTER(C.c_int)]),
+    "trax_kernel_launches": (C.c_int, [C.c_void_p]),
 }
 
 EXPORTED_SYMBOLS = tuple(_SIGS)
@@ -175,7 +180,8 @@ class Context:
         h = C.c_void_p()
         st = self.lib.trax_ctx_create(C.byref(h), device)
         if st != 0:
-            raise TraxError(st, "trax_ctx_create failed")
+            msg = self.lib.trax_ctx_last_error(None)
+            raise TraxError(st, "trax_ctx_create failed: " + (msg.decode() if msg else ""))
         self.h = h.value
         self.config = None
 
