@@ -164,11 +164,9 @@ def algorithmic_bytes(kernel, b, w, counts):
     n3 = sum(int(ln[:, cfg.triplets[t].layer3 - 1].sum()) for t in range(cfg.n_layer_triplets))
     table = {
         "grid_build": N * (12 + 28 + 28) + E * L * C * 4 * 3,
-        "pair_count": 12 * (n1 + n2) + 4 * n2,
-        "pair_store": 12 * (n1 + n2) + 4 * n2 + 8 * M,
-        "predict_count": M * (8 + 24) + 12 * n3 + 4 * M,
-        "predict_store": M * (8 + 24) + 12 * n3 + 4 * M + 8 * K,
-        "filter": K * (8 + 8 + 36) + 12 * R,
+        "pair_gen": 12 * (n1 + n2) + 4 * n2 * 2 + 8 * M,
+        "predict": M * (8 + 24) + 12 * n3 + 4 * M * 2 + 8 * K,
+        "filter": K * (8 + 8 + 36) + 4 * ((K + 31) // 32) * 3 + 12 * R,
     }
     return table.get(kernel)
 

@@ -29,6 +29,7 @@ constexpr int kTimerSlots = 64;
 constexpr int kScanItems = 8;       /* items per thread in k_scan */
 constexpr int kScanThreads = 256;
 constexpr int kFilterItems = 4;
+constexpr int kTileItems = 256;     /* threads (= items) per fused pair / predict tile */
 
 struct DevBuf {
     void *p = nullptr;
@@ -241,37 +242,29 @@ trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *gr
     if ((s = ensure(ctx, ctx->g_start, (size_t)max_groups * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->g_base, (size_t)(max_groups + 1) * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->slots, (size_t)slot_cap * 8)) != TRAX_OK) return s;
-    if ((s = ensure(ctx, ctx->pcnt, (size_t)slot_cap * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->pexcl, (size_t)(slot_cap + 1) * 4)) != TRAX_OK) return s;
-    const uint32_t ntile = tiles_for(slot_cap, kScanThreads * kScanItems);
+    const uint32_t ntile = tiles_for(slot_cap, kTileItems);
     if ((s = ensure(ctx, ctx->st0, (size_t)ntile * 8)) != TRAX_OK) return s;
     uint32_t *g_start = (uint32_t *)ctx->g_start.p, *g_base = (uint32_t *)ctx->g_base.p;
     uint2 *slots = (uint2 *)ctx->slots.p;
-    uint32_t *pcnt = (uint32_t *)ctx->pcnt.p, *pexcl = (uint32_t *)ctx->pexcl.p;
+    uint32_t *pexcl = (uint32_t *)ctx->pexcl.p;
     DevState *st = ctx->d_state;
 
     k_pair_groups<<<1, 1024, 0, ctx->stream>>>(kp, grid, g_start, g_base, st);
     if ((s = mark(ctx, "pair_groups")) != TRAX_OK) return s;
     k_pair_slots<<<ctx->blk_small, 256, 0, ctx->stream>>>(kp, g_start, g_base, slots, slot_cap, st);
     if ((s = mark(ctx, "pair_slots")) != TRAX_OK) return s;
-    k_pair<false><<<ctx->blk_pair, 256, 0, ctx->stream>>>(kp, grid, h.x, h.y, h.z, h.phi, slots,
-                                                          slot_cap, pcnt, nullptr, nullptr, 0, st);
-    if ((s = mark(ctx, "pair_count")) != TRAX_OK) return s;
     CK(cudaMemsetAsync(&st->tile_ctr[0], 0, 4, ctx->stream));
     CK(cudaMemsetAsync(ctx->st0.p, 0, (size_t)ntile * 8, ctx->stream));
-    k_scan<kScanItems><<<ctx->blk_scan, kScanThreads, 0, ctx->stream>>>(
-        pcnt, pexcl, &st->n_outer, slot_cap, &st->n_pairs, 0,
+    k_pair_fused<<<ctx->blk_pair, kTileItems, 0, ctx->stream>>>(
+        kp, grid, h.x, h.y, h.z, h.phi, slots, slot_cap, pexcl, pairs, pair_cap,
         (unsigned long long *)ctx->st0.p, st);
-    if ((s = mark(ctx, "pair_scan")) != TRAX_OK) return s;
+    if ((s = mark(ctx, "pair_gen")) != TRAX_OK) return s;
     k_group_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(g_base, pexcl, pair_offsets, kp.n_lt,
                                                              slot_cap, &st->n_pairs, pair_cap,
                                                              TRAX_DETAIL_PAIR_CAPACITY, st);
-    if ((s = mark(ctx, "pair_offsets")) != TRAX_OK) return s;
-    k_pair<true><<<ctx->blk_pair, 256, 0, ctx->stream>>>(kp, grid, h.x, h.y, h.z, h.phi, slots,
-                                                         slot_cap, nullptr, pexcl, pairs, pair_cap,
-                                                         st);
     CK(cudaGetLastError());
-    return mark(ctx, "pair_store");
+    return mark(ctx, "pair_offsets");
 }
 
 trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *grid,
@@ -281,33 +274,24 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
 {
     const KParams &kp = ctx->kp;
     trax_status s;
-    if ((s = ensure(ctx, ctx->ccnt, (size_t)pair_cap * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->cexcl, (size_t)(pair_cap + 1) * 4)) != TRAX_OK) return s;
-    const uint32_t ntile = tiles_for(pair_cap, kScanThreads * kScanItems);
+    const uint32_t ntile = tiles_for(pair_cap, kTileItems);
     if ((s = ensure(ctx, ctx->st1, (size_t)ntile * 8)) != TRAX_OK) return s;
-    uint32_t *ccnt = (uint32_t *)ctx->ccnt.p, *cexcl = (uint32_t *)ctx->cexcl.p;
+    uint32_t *cexcl = (uint32_t *)ctx->cexcl.p;
     DevState *st = ctx->d_state;
-    /* the pair total is st->n_pairs: written by the pair scan, or copied
+    /* the pair total is st->n_pairs: written by the pair stage, or copied
      * from pair_offsets[G] by trax_triplet_predict */
-    k_predict<false><<<ctx->blk_pred, 256, 0, ctx->stream>>>(
-        kp, grid, h.x, h.y, h.z, h.phi, h.event, h.layer, pairs, &st->n_pairs, pair_cap, ccnt,
-        nullptr, nullptr, 0, st);
-    if ((s = mark(ctx, "predict_count")) != TRAX_OK) return s;
     CK(cudaMemsetAsync(&st->tile_ctr[1], 0, 4, ctx->stream));
     CK(cudaMemsetAsync(ctx->st1.p, 0, (size_t)ntile * 8, ctx->stream));
-    k_scan<kScanItems><<<ctx->blk_scan, kScanThreads, 0, ctx->stream>>>(
-        ccnt, cexcl, &st->n_pairs, pair_cap, &st->n_cands, 1,
-        (unsigned long long *)ctx->st1.p, st);
-    if ((s = mark(ctx, "predict_scan")) != TRAX_OK) return s;
+    k_predict_fused<<<ctx->blk_pred, kTileItems, 0, ctx->stream>>>(
+        kp, grid, h.x, h.y, h.z, h.phi, h.event, h.layer, pairs, &st->n_pairs, pair_cap, cexcl,
+        cands, cand_cap, (unsigned long long *)ctx->st1.p, st);
+    if ((s = mark(ctx, "predict")) != TRAX_OK) return s;
     k_cand_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(pair_offsets, cexcl, cand_offsets,
                                                             kp.n_lt, pair_cap, &st->n_cands,
                                                             cand_cap, st);
-    if ((s = mark(ctx, "predict_offsets")) != TRAX_OK) return s;
-    k_predict<true><<<ctx->blk_pred, 256, 0, ctx->stream>>>(
-        kp, grid, h.x, h.y, h.z, h.phi, h.event, h.layer, pairs, &st->n_pairs, pair_cap, nullptr,
-        cexcl, cands, cand_cap, st);
     CK(cudaGetLastError());
-    return mark(ctx, "predict_store");
+    return mark(ctx, "predict_offsets");
 }
 
 trax_status enqueue_filter(trax_ctx *ctx, const SortedCols &h, const uint2 *pairs,
@@ -518,9 +502,9 @@ trax_status trax_ctx_create(trax_ctx **out, int device)
     if ((e = cudaFuncSetAttribute(k_grid_build, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)ctx->smem_optin)) != cudaSuccess) return bail(e);
     int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair<false>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_fused, kTileItems, 0);
     ctx->blk_pair = ctx->sm_count * std::max(b, 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_predict<false>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_predict_fused, kTileItems, 0);
     ctx->blk_pred = ctx->sm_count * std::max(b, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_filter, 256, 0);
     ctx->blk_filter = ctx->sm_count * std::max(b, 1);
@@ -826,12 +810,10 @@ trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers
     if ((s = ensure(ctx, ctx->g_start, G * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->g_base, (G + 1) * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->slots, slot_cap * 8)) != TRAX_OK) return s;
-    if ((s = ensure(ctx, ctx->pcnt, slot_cap * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->pexcl, (slot_cap + 1) * 4)) != TRAX_OK) return s;
-    if ((s = ensure(ctx, ctx->st0, (size_t)tiles_for((uint32_t)slot_cap, kScanThreads * kScanItems) * 8)) != TRAX_OK) return s;
-    if ((s = ensure(ctx, ctx->ccnt, (size_t)max_pairs * 4)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->st0, (size_t)tiles_for((uint32_t)slot_cap, kTileItems) * 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->cexcl, (size_t)(max_pairs + 1) * 4)) != TRAX_OK) return s;
-    if ((s = ensure(ctx, ctx->st1, (size_t)tiles_for(max_pairs, kScanThreads * kScanItems) * 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->st1, (size_t)tiles_for(max_pairs, kTileItems) * 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->st2, (size_t)tiles_for(max_candidates, 256 * kFilterItems) * 8)) != TRAX_OK) return s;
     if ((s = ensure_stage(ctx, (size_t)max_events * max_layers * 2 + 4)) != TRAX_OK) return s;
     CK(cudaStreamSynchronize(ctx->stream));

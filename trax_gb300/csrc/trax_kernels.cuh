@@ -223,6 +223,35 @@ __device__ __forceinline__ void lookback_scan(uint32_t n, uint32_t *tile_ctr,
     }
 }
 
+/* Tile ticket for persistent look-back loops (thread 0 draws, all read). */
+__device__ __forceinline__ uint32_t next_tile(uint32_t *ctr, uint32_t *s_tile)
+{
+    if (threadIdx.x == 0) *s_tile = atomicAdd(ctr, 1u);
+    __syncthreads();
+    return *s_tile;
+}
+
+/* Publishes this tile's aggregate, looks back for its exclusive prefix and
+ * publishes the inclusive prefix; every thread receives the prefix. */
+__device__ __forceinline__ uint32_t tile_prefix(uint32_t tile, uint32_t agg,
+                                                unsigned long long *status, DevState *st,
+                                                uint32_t *s_bcast)
+{
+    if (threadIdx.x == 0) {
+        uint32_t prefix = 0;
+        if (tile == 0) {
+            st_relaxed64(status, kFlagInc | agg);
+        } else {
+            st_relaxed64(status + tile, kFlagAgg | agg);
+            prefix = lookback_prefix(status, tile, st);
+            st_relaxed64(status + tile, kFlagInc | (uint32_t)(prefix + agg));
+        }
+        *s_bcast = prefix;
+    }
+    __syncthreads();
+    return *s_bcast;
+}
+
 /* Exclusive scan of in[0..n) into out[0..n], out[n] = total (in-place OK). */
 template <int ITEMS>
 __global__ void __launch_bounds__(256) k_scan(const uint32_t *in, uint32_t *out,
@@ -571,42 +600,107 @@ __device__ __forceinline__ void pair_visit(const KParams &kp, const uint32_t *lG
     }
 }
 
-template <bool STORE>
-__global__ void __launch_bounds__(256) k_pair(KParams kp, const uint32_t *grid, const float *X,
-                                              const float *Y, const float *Z, const float *PHI,
-                                              const uint2 *slots, uint32_t slot_cap,
-                                              uint32_t *cnt, const uint32_t *excl, uint2 *pairs,
-                                              uint32_t pair_cap, DevState *st)
+/*
+ * Pair stage in one pass.  Tiles of 256 outer slots, one slot per thread:
+ * each lane computes its own outer hit's window (no redundant math), then
+ * the warp sweeps the candidates of its 32 items one item at a time with all
+ * lanes (coalesced loads; ballots keep the inner-hit order).  A block scan
+ * plus decoupled look-back turns the distinct counts into output positions
+ * and a second sweep, on L1-resident hits, stores the pairs.
+ */
+__device__ __forceinline__ PairWindow shfl_window(const PairWindow &w, int k)
 {
+    PairWindow r;
+    r.zLow = __shfl_sync(kFull, w.zLow, k);
+    r.zHigh = __shfl_sync(kFull, w.zHigh, k);
+    r.phiLow = __shfl_sync(kFull, w.phiLow, k);
+    r.phiHigh = __shfl_sync(kFull, w.phiHigh, k);
+    r.zLowSector = __shfl_sync(kFull, w.zLowSector, k);
+    r.zHighSector = __shfl_sync(kFull, w.zHighSector, k);
+    r.phiLowSector = __shfl_sync(kFull, w.phiLowSector, k);
+    r.phiHighSector = __shfl_sync(kFull, w.phiHighSector, k);
+    r.wrap = __shfl_sync(kFull, w.wrap, k);
+    r.ok = true;
+    return r;
+}
+
+__global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *grid,
+                                                    const float *X, const float *Y,
+                                                    const float *Z, const float *PHI,
+                                                    const uint2 *slots, uint32_t slot_cap,
+                                                    uint32_t *pexcl, uint2 *pairs,
+                                                    uint32_t pair_cap, unsigned long long *status,
+                                                    DevState *st)
+{
+    __shared__ uint32_t s_warp[33];
+    __shared__ uint32_t s_tile, s_prefix;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt_mask = lanemask_lt();
-    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     uint32_t n = st->n_outer;
     if (n > slot_cap) n = slot_cap;
-    unsigned long long my_visits = 0;
-    for (uint32_t s = gw; s < n; s += nw) {
-        const uint2 sl = slots[s];
-        const uint32_t outer = sl.x, g = sl.y;
-        const uint32_t e = g / kp.n_lt, lt = g % kp.n_lt;
-        const uint32_t *lGrid1 = grid + ((size_t)e * kp.n_layers + (kp.l1[lt] - 1)) * kp.C;
-        const PairWindow w = pair_window(kp, lt, X[outer], Y[outer], Z[outer], PHI[outer]);
-        uint32_t visits = 0, distinct = 0;
-        if (!w.ok) {
-            if (lane == 0) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_WINDOW_OUTSIDE_GRID);
-        } else if (!STORE) {
-            pair_visit<false>(kp, lGrid1, Z, PHI, w, lane, lt_mask, outer, visits, distinct,
-                              nullptr, 0, 0);
-        } else {
-            pair_visit<true>(kp, lGrid1, Z, PHI, w, lane, lt_mask, outer, visits, distinct,
-                             pairs, excl[s], pair_cap);
+    if (n == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            pexcl[0] = 0;
+            st->n_pairs = 0;
         }
-        if (!STORE && lane == 0) {
-            cnt[s] = distinct;
-            my_visits += visits;
-        }
+        return;
     }
-    if (!STORE && lane == 0 && my_visits) atomicAdd(&st->pair_slots, my_visits);
+    const uint32_t ntiles = (n + blockDim.x - 1) / blockDim.x;
+    unsigned long long my_visits = 0;
+    for (;;) {
+        const uint32_t tile = next_tile(&st->tile_ctr[0], &s_tile);
+        if (tile >= ntiles) break;
+        const uint32_t s = tile * blockDim.x + threadIdx.x;
+        bool live = s < n;
+        PairWindow w{};
+        uint32_t outer = 0, lgoff = 0;
+        if (live) {
+            const uint2 sl = slots[s];
+            outer = sl.x;
+            const uint32_t e = sl.y / kp.n_lt, lt = sl.y % kp.n_lt;
+            lgoff = (e * kp.n_layers + (kp.l1[lt] - 1)) * kp.C;
+            w = pair_window(kp, lt, X[outer], Y[outer], Z[outer], PHI[outer]);
+            if (!w.ok) {
+                set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_WINDOW_OUTSIDE_GRID);
+                live = false;
+            }
+        }
+        /* count sweep */
+        uint32_t mine = 0;
+        const uint32_t live_mask = __ballot_sync(kFull, live);
+        for (uint32_t m = live_mask; m; m &= m - 1) {
+            const int k = __ffs(m) - 1;
+            const PairWindow wk = shfl_window(w, k);
+            const uint32_t lgk = __shfl_sync(kFull, lgoff, k);
+            uint32_t visits = 0, distinct = 0;
+            pair_visit<false>(kp, grid + lgk, Z, PHI, wk, lane, lt_mask, 0, visits, distinct,
+                              nullptr, 0, 0);
+            if (lane == (uint32_t)k) mine = distinct;
+            if (lane == 0) my_visits += visits;
+        }
+        uint32_t agg;
+        const uint32_t excl = block_exclusive_scan(mine, s_warp, &agg);
+        const uint32_t prefix = tile_prefix(tile, agg, status, st, &s_prefix);
+        const uint32_t pos = prefix + excl;
+        if (s < n) pexcl[s] = pos;
+        if (tile == ntiles - 1 && threadIdx.x == 0) {
+            pexcl[n] = prefix + agg;
+            st->n_pairs = prefix + agg;
+        }
+        /* store sweep */
+        for (uint32_t m = live_mask; m; m &= m - 1) {
+            const int k = __ffs(m) - 1;
+            const PairWindow wk = shfl_window(w, k);
+            const uint32_t lgk = __shfl_sync(kFull, lgoff, k);
+            const uint32_t pk = __shfl_sync(kFull, pos, k);
+            const uint32_t ok = __shfl_sync(kFull, outer, k);
+            uint32_t visits = 0, distinct = 0;
+            pair_visit<true>(kp, grid + lgk, Z, PHI, wk, lane, lt_mask, ok, visits, distinct,
+                             pairs, pk, pair_cap);
+        }
+        __syncthreads();
+    }
+    if (lane == 0 && my_visits) atomicAdd(&st->pair_slots, my_visits);
 }
 
 /* pair_offsets[g+1] = pairs before the first slot of group g+1. */
@@ -705,109 +799,130 @@ __device__ __forceinline__ PredWindow pred_window(const KParams &kp, uint32_t lt
     return w;
 }
 
-template <bool STORE>
-__global__ void __launch_bounds__(256) k_predict(KParams kp, const uint32_t *grid,
-                                                 const float *X, const float *Y, const float *Z,
-                                                 const float *PHI, const uint32_t *EVENT,
-                                                 const uint32_t *LAYER, const uint2 *pairs,
-                                                 const uint32_t *n_pairs_ptr, uint32_t pair_cap,
-                                                 uint32_t *cnt, const uint32_t *excl,
-                                                 uint2 *cands, uint32_t cand_cap, DevState *st)
+/*
+ * Prediction in one pass.  Tiles of 256 pairs, one pair per thread (the
+ * window math is the expensive part and ~20 candidates follow per pair).
+ * Consecutive pairs share their outer hit, so a warp's windows overlap and
+ * its candidate loads hit the same L1 lines.  The count sweep evaluates the
+ * count window (A) and the store window (B) together; a block scan plus
+ * decoupled look-back gives each pair its position; the store sweep writes
+ * the first min(A, B) accepts of window B, the reference's truncation.
+ */
+__device__ __forceinline__ void pred_row(const uint32_t *lGrid3, uint32_t P1, uint32_t zs,
+                                         uint32_t pLow, uint32_t pHigh, uint32_t wrap,
+                                         uint32_t &jlo, uint32_t &end2, uint32_t &rowEnd,
+                                         uint32_t &len)
 {
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t lt_mask = lanemask_lt();
-    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t rowStart = lGrid3[zs * P1];
+    rowEnd = lGrid3[(zs + 1) * P1];
+    len = rowEnd - rowStart;
+    jlo = lGrid3[zs * P1 + pLow];
+    end2 = wrap * rowEnd + lGrid3[zs * P1 + pHigh] - wrap * rowStart;
+}
+
+__global__ void __launch_bounds__(256) k_predict_fused(
+    KParams kp, const uint32_t *grid, const float *X, const float *Y, const float *Z,
+    const float *PHI, const uint32_t *EVENT, const uint32_t *LAYER, const uint2 *pairs,
+    const uint32_t *n_pairs_ptr, uint32_t pair_cap, uint32_t *cexcl, uint2 *cands,
+    uint32_t cand_cap, unsigned long long *status, DevState *st)
+{
+    __shared__ uint32_t s_warp[33];
+    __shared__ uint32_t s_tile, s_prefix;
     uint32_t n = *n_pairs_ptr;
     if (n > pair_cap) n = pair_cap;
+    if (n == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            cexcl[0] = 0;
+            st->n_cands = 0;
+        }
+        return;
+    }
     const uint32_t P1 = kp.nphi + 1;
     const uint32_t E = st->n_events;
+    const uint32_t ntiles = (n + blockDim.x - 1) / blockDim.x;
     unsigned long long my_slots = 0, my_trunc = 0;
-    for (uint32_t p = gw; p < n; p += nw) {
-        const uint2 pr = pairs[p];
-        const uint32_t h1 = pr.x, h2 = pr.y;
-        const uint32_t event = EVENT[h1];
-        const uint32_t lt = LAYER[h1] - 1;
-        if (lt >= kp.n_lt || event >= E) {
-            if (lane == 0) {
+    for (;;) {
+        const uint32_t tile = next_tile(&st->tile_ctr[1], &s_tile);
+        if (tile >= ntiles) break;
+        const uint32_t p = tile * blockDim.x + threadIdx.x;
+        bool live = p < n;
+        PredWindow w{};
+        const uint32_t *lGrid3 = grid;
+        if (live) {
+            const uint2 pr = pairs[p];
+            const uint32_t h1 = pr.x, h2 = pr.y;
+            const uint32_t event = EVENT[h1];
+            const uint32_t lt = LAYER[h1] - 1;
+            if (lt >= kp.n_lt || event >= E) {
                 set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_BAD_TRIPLET_INDEX);
-                if (!STORE) cnt[p] = 0;
+                live = false;
+            } else {
+                lGrid3 = grid + ((size_t)event * kp.n_layers + (kp.l3[lt] - 1)) * kp.C;
+                w = pred_window(kp, lt, X[h1], Y[h1], Z[h1], X[h2], Y[h2], Z[h2], PHI[h1],
+                                PHI[h2]);
+                if (!w.ok) {
+                    set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_WINDOW_OUTSIDE_GRID);
+                    live = false;
+                }
             }
-            continue;
         }
-        const uint32_t *lGrid3 = grid + ((size_t)event * kp.n_layers + (kp.l3[lt] - 1)) * kp.C;
-        const PredWindow w = pred_window(kp, lt, X[h1], Y[h1], Z[h1], X[h2], Y[h2], Z[h2],
-                                         PHI[h1], PHI[h2]);
-        if (!w.ok) {
-            if (lane == 0) {
-                set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_WINDOW_OUTSIDE_GRID);
-                if (!STORE) cnt[p] = 0;
-            }
-            continue;
-        }
-        if (!STORE) {
-            /* count window (A) and store window (B) in one sweep */
+        uint32_t emitted = 0;
+        if (live) {
+            uint32_t cA = 0, cB = 0;
             const uint32_t zlo = min(w.zLowSector[0], w.zLowSector[1]);
             const uint32_t zhi = max(w.zHighSector[0], w.zHighSector[1]);
-            uint32_t cA = 0, cB = 0;
             for (uint32_t zs = zlo; zs < zhi; ++zs) {
                 const bool inA = zs >= w.zLowSector[0] && zs < w.zHighSector[0];
                 const bool inB = zs >= w.zLowSector[1] && zs < w.zHighSector[1];
-                const uint32_t rowStart = lGrid3[zs * P1];
-                const uint32_t rowEnd = lGrid3[(zs + 1) * P1];
-                const uint32_t len = rowEnd - rowStart;
-                const uint32_t jlo = lGrid3[zs * P1 + w.phiLowSector];
-                const uint32_t end2 = w.wrap * rowEnd + lGrid3[zs * P1 + w.phiHighSector] - w.wrap * rowStart;
-                for (uint32_t jb = jlo; jb < end2; jb += 32) {
-                    const uint32_t j = jb + lane;
-                    bool a = false, b = false;
-                    if (j < end2) {
-                        const uint32_t idx = j - (uint32_t)(j >= rowEnd) * len;
-                        const float zz = Z[idx];
-                        const bool ph = phi_in(PHI[idx], w.phiLow, w.phiHigh, w.wrap);
-                        a = inA && ph && w.zLow[0] <= zz && zz <= w.zHigh[0];
-                        b = inB && ph && w.zLow[1] <= zz && zz <= w.zHigh[1];
-                    }
-                    cA += __popc(__ballot_sync(kFull, a));
-                    cB += __popc(__ballot_sync(kFull, b));
+                uint32_t j, end2, rowEnd, len;
+                pred_row(lGrid3, P1, zs, w.phiLowSector, w.phiHighSector, w.wrap, j, end2,
+                         rowEnd, len);
+                for (; j < end2; ++j) {
+                    const uint32_t idx = j - (j >= rowEnd ? len : 0u);
+                    const float zz = Z[idx];
+                    const bool ph = phi_in(PHI[idx], w.phiLow, w.phiHigh, w.wrap);
+                    cA += (inA && ph && w.zLow[0] <= zz && zz <= w.zHigh[0]) ? 1u : 0u;
+                    cB += (inB && ph && w.zLow[1] <= zz && zz <= w.zHigh[1]) ? 1u : 0u;
                 }
             }
-            const uint32_t emitted = cA < cB ? cA : cB;
-            if (lane == 0) {
-                cnt[p] = emitted;
-                my_slots += cA;
-                my_trunc += cB - emitted;
-            }
-        } else {
-            const uint32_t pos = excl[p];
-            const uint32_t limit = excl[p + 1] - pos;
+            emitted = cA < cB ? cA : cB;
+            my_slots += cA;
+            my_trunc += cB - emitted;
+        }
+        uint32_t agg;
+        const uint32_t excl = block_exclusive_scan(emitted, s_warp, &agg);
+        const uint32_t prefix = tile_prefix(tile, agg, status, st, &s_prefix);
+        const uint32_t pos = prefix + excl;
+        if (p < n) cexcl[p] = pos;
+        if (tile == ntiles - 1 && threadIdx.x == 0) {
+            cexcl[n] = prefix + agg;
+            st->n_cands = prefix + agg;
+        }
+        if (emitted) {
             uint32_t written = 0;
-            for (uint32_t zs = w.zLowSector[1]; zs < w.zHighSector[1] && written < limit; ++zs) {
-                const uint32_t rowStart = lGrid3[zs * P1];
-                const uint32_t rowEnd = lGrid3[(zs + 1) * P1];
-                const uint32_t len = rowEnd - rowStart;
-                const uint32_t jlo = lGrid3[zs * P1 + w.phiLowSector];
-                const uint32_t end2 = w.wrap * rowEnd + lGrid3[zs * P1 + w.phiHighSector] - w.wrap * rowStart;
-                for (uint32_t jb = jlo; jb < end2 && written < limit; jb += 32) {
-                    const uint32_t j = jb + lane;
-                    bool b = false;
-                    uint32_t idx = 0;
-                    if (j < end2) {
-                        idx = j - (uint32_t)(j >= rowEnd) * len;
-                        const float zz = Z[idx];
-                        b = w.zLow[1] <= zz && zz <= w.zHigh[1] && phi_in(PHI[idx], w.phiLow, w.phiHigh, w.wrap);
+            for (uint32_t zs = w.zLowSector[1]; zs < w.zHighSector[1] && written < emitted; ++zs) {
+                uint32_t j, end2, rowEnd, len;
+                pred_row(lGrid3, P1, zs, w.phiLowSector, w.phiHighSector, w.wrap, j, end2,
+                         rowEnd, len);
+                for (; j < end2 && written < emitted; ++j) {
+                    const uint32_t idx = j - (j >= rowEnd ? len : 0u);
+                    const float zz = Z[idx];
+                    if (w.zLow[1] <= zz && zz <= w.zHigh[1] &&
+                        phi_in(PHI[idx], w.phiLow, w.phiHigh, w.wrap)) {
+                        if (pos + written < cand_cap) cands[pos + written] = make_uint2(p, idx);
+                        ++written;
                     }
-                    const uint32_t m = __ballot_sync(kFull, b);
-                    if (b) {
-                        const uint32_t r = written + __popc(m & lt_mask);
-                        if (r < limit && pos + r < cand_cap) cands[pos + r] = make_uint2(p, idx);
-                    }
-                    written += __popc(m);
                 }
             }
         }
+        __syncthreads();
     }
-    if (!STORE && lane == 0 && (my_slots | my_trunc)) {
+    /* warp-reduce the statistics, one atomic per warp */
+    for (int d = 16; d; d >>= 1) {
+        my_slots += __shfl_down_sync(kFull, my_slots, d);
+        my_trunc += __shfl_down_sync(kFull, my_trunc, d);
+    }
+    if ((threadIdx.x & 31) == 0 && (my_slots | my_trunc)) {
         atomicAdd(&st->cand_slots, my_slots);
         atomicAdd(&st->cand_truncated, my_trunc);
     }
