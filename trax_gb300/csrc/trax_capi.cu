@@ -29,7 +29,8 @@ constexpr int kTimerSlots = 64;
 constexpr int kScanItems = 8;       /* items per thread in k_scan */
 constexpr int kScanThreads = 256;
 constexpr int kFilterItems = 4;
-constexpr int kTileItems = 256;     /* threads (= items) per fused pair / predict tile */
+constexpr int kTileItems = 32;      /* items per fused pair / predict tile (one warp) */
+constexpr int kFusedThreads = 256;  /* threads per block of the fused kernels */
 
 struct DevBuf {
     void *p = nullptr;
@@ -63,7 +64,7 @@ struct trax_ctx {
     trax_grid_cfg r_grid{};
     DevBuf in_cols[7], srt_cols[9], grid_buf, pairs_buf, pair_off, cands_buf, cand_off;
     DevBuf trk_cols[3], trk_off, trk_map[3], r_seg;
-    uint32_t gb_C = 0;                    /* cached k_grid_build launch plan */
+    uint32_t gb_C = 0, gb_avg = 0;        /* cached k_grid_build launch plan */
     int gb_warps = 0, gb_per_sm = 0;
     cudaGraphExec_t graph = nullptr;
     uint32_t staged_events = 0, staged_hits = 0;
@@ -153,27 +154,31 @@ trax_status check_grid(trax_ctx *ctx, const trax_grid_cfg *g)
     return TRAX_OK;
 }
 
-/* Dynamic shared memory plan of k_grid_build: W warps with (W+1)*C words. */
-int grid_build_warps(const trax_ctx *ctx, uint32_t C)
+/* Dynamic shared memory plan of k_grid_build: W warps with (W+1)*C words.
+ * A warp should own about 128 hits of its segment: fewer warps waste the
+ * per-warp cell tables, more leave warps idle. */
+int grid_build_warps(const trax_ctx *ctx, uint32_t C, uint32_t avg_seg)
 {
     const size_t budget = std::min<size_t>(ctx->smem_optin, 200 * 1024);
     long w = (long)(budget / (4ull * C)) - 1;
-    if (w > 32) w = 32;
-    if (w > 16 && C > 2048) w = 16;
+    long want = 1;
+    while (want < 32 && want * 128 < (long)avg_seg) want <<= 1;
+    if (w > want) w = want;
     return (int)w;
 }
 
 /* Warps and resident CTAs of k_grid_build for C cells; computed outside
  * any stream capture and cached. */
-trax_status grid_plan(trax_ctx *ctx, uint32_t C)
+trax_status grid_plan(trax_ctx *ctx, uint32_t C, uint32_t avg_seg)
 {
-    if (ctx->gb_C == C && ctx->gb_warps > 0) return TRAX_OK;
-    const int W = grid_build_warps(ctx, C);
+    if (ctx->gb_C == C && ctx->gb_avg == avg_seg && ctx->gb_warps > 0) return TRAX_OK;
+    const int W = grid_build_warps(ctx, C, avg_seg);
     if (W < 1) return fail(ctx, TRAX_ERR_BAD_ARG, "grid too large for shared memory");
     int per_sm = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_grid_build, W * 32,
                                                      (size_t)(W + 1) * C * 4));
     ctx->gb_C = C;
+    ctx->gb_avg = avg_seg;
     ctx->gb_warps = W;
     ctx->gb_per_sm = per_sm < 1 ? 1 : per_sm;
     return TRAX_OK;
@@ -218,10 +223,10 @@ trax_status set_sizes(trax_ctx *ctx, uint32_t n_events, uint32_t n_hits)
 
 trax_status enqueue_grid(trax_ctx *ctx, const InCols &in, const SortedCols &out,
                          const uint32_t *seg_start, const uint32_t *seg_n, uint32_t *grid,
-                         uint32_t max_segs)
+                         uint32_t max_segs, uint32_t n_hits)
 {
     const KParams &kp = ctx->kp;
-    trax_status s = grid_plan(ctx, kp.C);
+    trax_status s = grid_plan(ctx, kp.C, max_segs ? n_hits / max_segs : 0);
     if (s != TRAX_OK) return s;
     const int W = ctx->gb_warps, per_sm = ctx->gb_per_sm;
     const size_t smem = (size_t)(W + 1) * kp.C * 4;
@@ -256,7 +261,7 @@ trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *gr
     if ((s = mark(ctx, "pair_slots")) != TRAX_OK) return s;
     CK(cudaMemsetAsync(&st->tile_ctr[0], 0, 4, ctx->stream));
     CK(cudaMemsetAsync(ctx->st0.p, 0, (size_t)ntile * 8, ctx->stream));
-    k_pair_fused<<<ctx->blk_pair, kTileItems, 0, ctx->stream>>>(
+    k_pair_fused<<<ctx->blk_pair, kFusedThreads, 0, ctx->stream>>>(
         kp, grid, h.x, h.y, h.z, h.phi, slots, slot_cap, pexcl, pairs, pair_cap,
         (unsigned long long *)ctx->st0.p, st);
     if ((s = mark(ctx, "pair_gen")) != TRAX_OK) return s;
@@ -283,7 +288,7 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
      * from pair_offsets[G] by trax_triplet_predict */
     CK(cudaMemsetAsync(&st->tile_ctr[1], 0, 4, ctx->stream));
     CK(cudaMemsetAsync(ctx->st1.p, 0, (size_t)ntile * 8, ctx->stream));
-    k_predict_fused<<<ctx->blk_pred, kTileItems, 0, ctx->stream>>>(
+    k_predict_fused<<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
         kp, grid, h.x, h.y, h.z, h.phi, h.event, h.layer, pairs, &st->n_pairs, pair_cap, cexcl,
         cands, cand_cap, (unsigned long long *)ctx->st1.p, st);
     if ((s = mark(ctx, "predict")) != TRAX_OK) return s;
@@ -502,9 +507,9 @@ trax_status trax_ctx_create(trax_ctx **out, int device)
     if ((e = cudaFuncSetAttribute(k_grid_build, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)ctx->smem_optin)) != cudaSuccess) return bail(e);
     int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_fused, kTileItems, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_fused, kFusedThreads, 0);
     ctx->blk_pair = ctx->sm_count * std::max(b, 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_predict_fused, kTileItems, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_predict_fused, kFusedThreads, 0);
     ctx->blk_pred = ctx->sm_count * std::max(b, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_filter, 256, 0);
     ctx->blk_filter = ctx->sm_count * std::max(b, 1);
@@ -592,6 +597,10 @@ trax_status trax_configure(trax_ctx *ctx, const trax_config *cfg)
         kp.rmax[l] = l < cfg->n_geom_layers ? cfg->max_radius[l] : 0.0f;
     }
     kp.rmin_curv = trax_min_radius_curvature(cfg->min_pt, cfg->bz);
+    for (uint32_t l = 0; l < kMaxLayers; ++l) {
+        kp.acos_rmin[l] = trax_acosf(kp.rmin[l] / (2 * kp.rmin_curv));
+        kp.acos_rmax[l] = trax_acosf(kp.rmax[l] / (2 * kp.rmin_curv));
+    }
     ctx->configured = true;
     if (ctx->graph) {
         cudaGraphExecDestroy(ctx->graph);
@@ -719,7 +728,7 @@ trax_status trax_grid_build(trax_ctx *ctx, const trax_hits *in, const trax_layou
     if (grid->n_events == 0) return TRAX_OK;
     InCols ic{in->x, in->y, in->z, in->layer, in->detector_id, in->hit_id, in->event};
     return enqueue_grid(ctx, ic, sorted_from(out), d_start, d_n, d_grid,
-                        grid->n_events * grid->n_layers);
+                        grid->n_events * grid->n_layers, in->n);
 }
 
 trax_status trax_pair_gen(trax_ctx *ctx, const trax_sorted_hits *hits, const uint32_t *d_grid,
@@ -857,7 +866,7 @@ trax_status enqueue_pipeline(trax_ctx *ctx)
     trax_status s = begin_marks(ctx);
     if (s != TRAX_OK) return s;
     CK(cudaMemsetAsync(&ctx->d_state->n_outer, 0, sizeof(DevState) - 8, ctx->stream));
-    s = enqueue_grid(ctx, ic, sc, seg, seg + nseg, grid, nseg);
+    s = enqueue_grid(ctx, ic, sc, seg, seg + nseg, grid, nseg, ctx->r_hits);
     if (s != TRAX_OK) return s;
     const uint32_t slot_cap = ctx->r_hits * T + 1;
     s = enqueue_pairs(ctx, sc, grid, (uint2 *)ctx->pairs_buf.p, (uint32_t *)ctx->pair_off.p,
@@ -930,7 +939,8 @@ trax_status trax_run_staged(trax_ctx *ctx)
     if (!ctx || !ctx->reserved) return TRAX_ERR_BAD_ARG;
     fill_grid_params(ctx->kp, &ctx->r_grid);
     if (!ctx->graph) {
-        trax_status s0 = grid_plan(ctx, ctx->kp.C);
+        const uint32_t nseg = ctx->r_events * ctx->r_layers;
+        trax_status s0 = grid_plan(ctx, ctx->kp.C, nseg ? ctx->r_hits / nseg : 0);
         if (s0 != TRAX_OK) return s0;
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));

@@ -40,6 +40,10 @@ struct KParams {
     float tip[kMaxLT], z0[kMaxLT];
     uint32_t spread_phi[kMaxLT];
     float rmin[kMaxLayers], rmax[kMaxLayers];
+    /* acos(r / (2 * minRadiusCurvature)) of each layer's min / max radius:
+     * loop invariants of the phi windows, evaluated once on the host with the
+     * same trax_acosf (host and device agree bit for bit) */
+    float acos_rmin[kMaxLayers], acos_rmax[kMaxLayers];
 };
 
 /* Device-side sizes, counters and status of one pipeline run. */
@@ -250,6 +254,70 @@ __device__ __forceinline__ uint32_t tile_prefix(uint32_t tile, uint32_t agg,
     }
     __syncthreads();
     return *s_bcast;
+}
+
+/* Warp-wide decoupled look-back for a warp-sized tile: lane i inspects
+ * predecessor tile - 1 - i, so 32 predecessors are examined per poll.  The
+ * prefix is the sum of the aggregates up to and including the nearest
+ * inclusive prefix.  Bounded like lookback_prefix. */
+__device__ __forceinline__ uint32_t warp_lookback(unsigned long long *status, uint32_t tile,
+                                                  DevState *st)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t prefix = 0;
+    int64_t base = (int64_t)tile - 1;
+    uint32_t spins = 0;
+    while (base >= 0) {
+        const int64_t k = base - lane;
+        unsigned long long s = k >= 0 ? ld_relaxed64(status + k) : (kFlagInc | 0ull);
+        const unsigned long long flag = s & (3ull << 32);
+        const uint32_t inc = __ballot_sync(kFull, flag == kFlagInc);
+        const uint32_t zero = __ballot_sync(kFull, flag == 0);
+        const uint32_t first_inc = inc ? (uint32_t)(__ffs(inc) - 1) : 32u;
+        const uint32_t upto = first_inc < 32 ? ((first_inc == 31) ? kFull : ((2u << first_inc) - 1u)) : kFull;
+        if (zero & upto) {
+            if (++spins > kSpinLimit) {
+                if (lane == 0) set_fault(st, TRAX_ERR_TIMEOUT, TRAX_DETAIL_SCAN_TIMEOUT);
+                break;
+            }
+            __nanosleep(32);
+            continue;
+        }
+        uint32_t v = ((upto >> lane) & 1u) ? (uint32_t)s : 0u;
+#pragma unroll
+        for (int d = 16; d; d >>= 1) v += __shfl_xor_sync(kFull, v, d);
+        prefix += v;
+        if (first_inc < 32) break;
+        base -= 32;
+    }
+    return prefix;
+}
+
+/* Warp-sized tile scan: exclusive prefix of v within the warp, the tile's
+ * aggregate published and looked back; returns the global exclusive position
+ * and (lane-uniform) the inclusive end of the tile. */
+__device__ __forceinline__ uint32_t warp_tile_position(uint32_t v, uint32_t tile,
+                                                       unsigned long long *status,
+                                                       DevState *st, uint32_t *tile_end)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, x, d);
+        if (lane >= (uint32_t)d) x += y;
+    }
+    const uint32_t agg = __shfl_sync(kFull, x, 31);
+    uint32_t prefix = 0;
+    if (tile == 0) {
+        if (lane == 0) st_relaxed64(status, kFlagInc | agg);
+    } else {
+        if (lane == 0) st_relaxed64(status + tile, kFlagAgg | agg);
+        prefix = warp_lookback(status, tile, st);
+        if (lane == 0) st_relaxed64(status + tile, kFlagInc | (uint32_t)(prefix + agg));
+    }
+    *tile_end = prefix + agg;
+    return prefix + x - v;
 }
 
 /* Exclusive scan of in[0..n) into out[0..n], out[n] = total (in-place OK). */
@@ -498,8 +566,9 @@ __device__ __forceinline__ PairWindow pair_window(const KParams &kp, uint32_t lt
     const uint32_t zh = trax_f2u(floorf((zHigh - TRAX_MIN_Z) / kp.sz_z)) + 1u;
     w.zHighSector = zh < kp.nz ? zh : kp.nz;
 
-    tmp = fabsf(trax_acosf(r / (2 * minRadiusCurvature)) - trax_acosf(maxLayerRadius1 / (2 * minRadiusCurvature)));
-    float dPhi = fabsf(trax_acosf(r / (2 * minRadiusCurvature)) - trax_acosf(minLayerRadius1 / (2 * minRadiusCurvature)));
+    const float acos_r = trax_acosf(r / (2 * minRadiusCurvature));
+    tmp = fabsf(acos_r - kp.acos_rmax[layer]);
+    float dPhi = fabsf(acos_r - kp.acos_rmin[layer]);
     dPhi = (float)(tmp < dPhi) * dPhi + (float)(tmp > dPhi) * tmp;
     tmp = trax_atanf(tip * (r - minLayerRadius1)) / (r * minLayerRadius1);
     float phiHigh = trax_atanf(tip * (r - maxLayerRadius1)) / (r * maxLayerRadius1);
@@ -601,11 +670,11 @@ __device__ __forceinline__ void pair_visit(const KParams &kp, const uint32_t *lG
 }
 
 /*
- * Pair stage in one pass.  Tiles of 256 outer slots, one slot per thread:
+ * Pair stage in one pass.  Warp-sized tiles of 32 outer slots, one per lane:
  * each lane computes its own outer hit's window (no redundant math), then
  * the warp sweeps the candidates of its 32 items one item at a time with all
- * lanes (coalesced loads; ballots keep the inner-hit order).  A block scan
- * plus decoupled look-back turns the distinct counts into output positions
+ * lanes (coalesced loads; ballots keep the inner-hit order).  A warp scan
+ * plus warp-wide decoupled look-back turns the distinct counts into positions
  * and a second sweep, on L1-resident hits, stores the pairs.
  */
 __device__ __forceinline__ PairWindow shfl_window(const PairWindow &w, int k)
@@ -632,8 +701,6 @@ __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *
                                                     uint32_t pair_cap, unsigned long long *status,
                                                     DevState *st)
 {
-    __shared__ uint32_t s_warp[33];
-    __shared__ uint32_t s_tile, s_prefix;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt_mask = lanemask_lt();
     uint32_t n = st->n_outer;
@@ -645,12 +712,14 @@ __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *
         }
         return;
     }
-    const uint32_t ntiles = (n + blockDim.x - 1) / blockDim.x;
+    const uint32_t ntiles = (n + 31) / 32;
     unsigned long long my_visits = 0;
     for (;;) {
-        const uint32_t tile = next_tile(&st->tile_ctr[0], &s_tile);
+        uint32_t tile = 0;
+        if (lane == 0) tile = atomicAdd(&st->tile_ctr[0], 1u);
+        tile = __shfl_sync(kFull, tile, 0);
         if (tile >= ntiles) break;
-        const uint32_t s = tile * blockDim.x + threadIdx.x;
+        const uint32_t s = tile * 32 + lane;
         bool live = s < n;
         PairWindow w{};
         uint32_t outer = 0, lgoff = 0;
@@ -665,7 +734,7 @@ __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *
                 live = false;
             }
         }
-        /* count sweep */
+        /* count sweep: the warp walks each live item's candidates */
         uint32_t mine = 0;
         const uint32_t live_mask = __ballot_sync(kFull, live);
         for (uint32_t m = live_mask; m; m &= m - 1) {
@@ -678,14 +747,12 @@ __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *
             if (lane == (uint32_t)k) mine = distinct;
             if (lane == 0) my_visits += visits;
         }
-        uint32_t agg;
-        const uint32_t excl = block_exclusive_scan(mine, s_warp, &agg);
-        const uint32_t prefix = tile_prefix(tile, agg, status, st, &s_prefix);
-        const uint32_t pos = prefix + excl;
+        uint32_t tile_end;
+        const uint32_t pos = warp_tile_position(mine, tile, status, st, &tile_end);
         if (s < n) pexcl[s] = pos;
-        if (tile == ntiles - 1 && threadIdx.x == 0) {
-            pexcl[n] = prefix + agg;
-            st->n_pairs = prefix + agg;
+        if (tile == ntiles - 1 && lane == 0) {
+            pexcl[n] = tile_end;
+            st->n_pairs = tile_end;
         }
         /* store sweep */
         for (uint32_t m = live_mask; m; m &= m - 1) {
@@ -698,7 +765,6 @@ __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *
             pair_visit<true>(kp, grid + lgk, Z, PHI, wk, lane, lt_mask, ok, visits, distinct,
                              pairs, pk, pair_cap);
         }
-        __syncthreads();
     }
     if (lane == 0 && my_visits) atomicAdd(&st->pair_slots, my_visits);
 }
@@ -779,8 +845,9 @@ __device__ __forceinline__ PredWindow pred_window(const KParams &kp, uint32_t lt
     dPhi += (dPhi > TRAX_PI_F) ? -2 * TRAX_PI_F : (dPhi < -TRAX_PI_F) ? 2 * TRAX_PI_F : 0;
     dPhi = fabsf(dPhi);
     const float dHits = sqrtf((p2x - p1x) * (p2x - p1x) + (p2y - p1y) * (p2y - p1y));
-    tmp = fabsf(trax_acosf(dHits / (2 * minRadiusCurvature)) - trax_acosf(maxLayerRadius / (2 * minRadiusCurvature)));
-    float phiLow = fabsf(trax_acosf(dHits / (2 * minRadiusCurvature)) - trax_acosf(minLayerRadius / (2 * minRadiusCurvature)));
+    const float acos_d = trax_acosf(dHits / (2 * minRadiusCurvature));
+    tmp = fabsf(acos_d - kp.acos_rmax[layer]);
+    float phiLow = fabsf(acos_d - kp.acos_rmin[layer]);
     dPhi = trax_maxf(dPhi, trax_maxf(tmp, phiLow));
     float phiHigh = phi + dPhi + sigmaPhi;
     phiLow = phi - dPhi - sigmaPhi;
@@ -800,12 +867,13 @@ __device__ __forceinline__ PredWindow pred_window(const KParams &kp, uint32_t lt
 }
 
 /*
- * Prediction in one pass.  Tiles of 256 pairs, one pair per thread (the
+ * Prediction in one pass.  Warp-sized tiles of 32 pairs, one pair per thread (the
  * window math is the expensive part and ~20 candidates follow per pair).
  * Consecutive pairs share their outer hit, so a warp's windows overlap and
  * its candidate loads hit the same L1 lines.  The count sweep evaluates the
- * count window (A) and the store window (B) together; a block scan plus
- * decoupled look-back gives each pair its position; the store sweep writes
+ * count window (A) and the store window (B) together; a warp scan plus
+ * warp-wide decoupled look-back gives each pair its position without any
+ * block barrier (so no warp waits for a slower warp); the store sweep writes
  * the first min(A, B) accepts of window B, the reference's truncation.
  */
 __device__ __forceinline__ void pred_row(const uint32_t *lGrid3, uint32_t P1, uint32_t zs,
@@ -826,8 +894,7 @@ __global__ void __launch_bounds__(256) k_predict_fused(
     const uint32_t *n_pairs_ptr, uint32_t pair_cap, uint32_t *cexcl, uint2 *cands,
     uint32_t cand_cap, unsigned long long *status, DevState *st)
 {
-    __shared__ uint32_t s_warp[33];
-    __shared__ uint32_t s_tile, s_prefix;
+    const uint32_t lane = threadIdx.x & 31;
     uint32_t n = *n_pairs_ptr;
     if (n > pair_cap) n = pair_cap;
     if (n == 0) {
@@ -839,12 +906,14 @@ __global__ void __launch_bounds__(256) k_predict_fused(
     }
     const uint32_t P1 = kp.nphi + 1;
     const uint32_t E = st->n_events;
-    const uint32_t ntiles = (n + blockDim.x - 1) / blockDim.x;
+    const uint32_t ntiles = (n + 31) / 32;
     unsigned long long my_slots = 0, my_trunc = 0;
     for (;;) {
-        const uint32_t tile = next_tile(&st->tile_ctr[1], &s_tile);
+        uint32_t tile = 0;
+        if (lane == 0) tile = atomicAdd(&st->tile_ctr[1], 1u);
+        tile = __shfl_sync(kFull, tile, 0);
         if (tile >= ntiles) break;
-        const uint32_t p = tile * blockDim.x + threadIdx.x;
+        const uint32_t p = tile * 32 + lane;
         bool live = p < n;
         PredWindow w{};
         const uint32_t *lGrid3 = grid;
@@ -889,14 +958,12 @@ __global__ void __launch_bounds__(256) k_predict_fused(
             my_slots += cA;
             my_trunc += cB - emitted;
         }
-        uint32_t agg;
-        const uint32_t excl = block_exclusive_scan(emitted, s_warp, &agg);
-        const uint32_t prefix = tile_prefix(tile, agg, status, st, &s_prefix);
-        const uint32_t pos = prefix + excl;
+        uint32_t tile_end;
+        const uint32_t pos = warp_tile_position(emitted, tile, status, st, &tile_end);
         if (p < n) cexcl[p] = pos;
-        if (tile == ntiles - 1 && threadIdx.x == 0) {
-            cexcl[n] = prefix + agg;
-            st->n_cands = prefix + agg;
+        if (tile == ntiles - 1 && lane == 0) {
+            cexcl[n] = tile_end;
+            st->n_cands = tile_end;
         }
         if (emitted) {
             uint32_t written = 0;
@@ -915,7 +982,6 @@ __global__ void __launch_bounds__(256) k_predict_fused(
                 }
             }
         }
-        __syncthreads();
     }
     /* warp-reduce the statistics, one atomic per warp */
     for (int d = 16; d; d >>= 1) {

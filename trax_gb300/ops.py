@@ -296,6 +296,10 @@ class Pipeline:
                                         C.byref(grid), int(max_pairs), int(max_candidates),
                                         int(max_tracklets)))
         self._keep = []
+        # pinned result buffers, reused by every seed() call
+        cap = self.max_tracklets
+        self._out = [PinnedBuffer(ctx, 4 * cap, U32) for _ in range(3)]
+        self._off = PinnedBuffer(ctx, 4 * (int(max_events) * self.n_triplets + 1), U32)
 
     def _batch_struct(self, b: EventBatch):
         cols = [np.ascontiguousarray(c) for c in b.columns()]
@@ -304,17 +308,21 @@ class Pipeline:
         return A.TraxEventBatch(b.n_events, b.n_layers, b.n_hits,
                                 *[c.ctypes.data for c in cols], ln.ctypes.data)
 
-    def seed(self, b: EventBatch, input_indices=False):
-        """Host arrays in, tracklets out (synchronous)."""
+    def seed(self, b: EventBatch, input_indices=False, copy=True):
+        """Host arrays in, tracklets out (synchronous).  With copy=False the
+        returned arrays are views of pinned buffers that the next call
+        overwrites."""
         bs = self._batch_struct(b)
         cap = self.max_tracklets
-        h = [np.empty(cap, U32) for _ in range(3)]
-        off = np.empty(b.n_events * self.n_triplets + 1, U32)
-        r = A.TraxBatchResult(h[0].ctypes.data, h[1].ctypes.data, h[2].ctypes.data,
-                              off.ctypes.data, cap, 1 if input_indices else 0, 0, A.TraxCounts())
+        h = [o.array for o in self._out]
+        r = A.TraxBatchResult(self._out[0].ptr, self._out[1].ptr, self._out[2].ptr,
+                              self._off.ptr, cap, 1 if input_indices else 0, 0, A.TraxCounts())
         self.ctx._check(self.ctx.lib.trax_seed_batch(self.ctx.h, C.byref(bs), C.byref(r)))
         n = r.n_tracklets
-        return np.stack([x[:n] for x in h], axis=1), off, r.counts.as_dict()
+        off = self._off.array[: b.n_events * self.n_triplets + 1]
+        if not copy:
+            return [x[:n] for x in h], off, r.counts.as_dict()
+        return np.stack([x[:n] for x in h], axis=1), off.copy(), r.counts.as_dict()
 
     def stage(self, b: EventBatch):
         bs = self._batch_struct(b)
