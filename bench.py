@@ -379,6 +379,23 @@ def run_ours(args, dist):
         ctx.synchronize()
     per_event = S / (time.perf_counter() - t0)
 
+    # ---- PrefixSum micro-benchmark: 1 Mi uint32, the reference's own
+    # prefix-sum benchmark shape (src/trax_test/trax_test.cpp:436-479)
+    n_scan = 1024 * 1024
+    d_scan = ctx.upload(np.ones(n_scan, np.uint32))
+    for _ in range(5):
+        ctx.prefix_sum(d_scan, d_scan, n_scan)
+    ctx.synchronize()
+    reps = 100
+    ctx.timer_record(60)
+    for _ in range(reps):
+        ctx.prefix_sum(d_scan, d_scan, n_scan)
+    ctx.timer_record(61)
+    scan_ms = ctx.timer_elapsed_ms(60, 61) / reps
+    prefix_sum = {"n": n_scan, "ms": round(scan_ms, 5),
+                  "gbs": round(8 * n_scan / (scan_ms / 1000) / 1e9, 1),
+                  "note": "in place, 4 B read + 4 B written per element"}
+
     # ---- CPU baseline (rank 0, N=1 only) ----------------------------------
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
@@ -410,6 +427,7 @@ def run_ours(args, dist):
             "roofline": roofline,
             "kernels": kernels,
             "cpu_baseline": cpu,
+            "prefix_sum_1mi": prefix_sum,
             "clocks": clocks,
             "gpu_launches": launches * args.steps,
             "counts_per_step": {k: counts[k] for k in ("n_hits", "n_pairs", "pair_slots",

@@ -239,6 +239,13 @@ trax_status trax_triplet_filter(trax_ctx *ctx, const trax_sorted_hits *hits,
                                 const trax_grid_cfg *grid, const trax_pairs *pairs,
                                 const trax_pairs *candidates, trax_tracklets *out);
 
+/* PrefixSum::run (src/algorithms/PrefixSum.h:42-43, PrefixSum.cpp:8-30):
+ * exclusive scan of n uint32 (device pointers; in place allowed).  One
+ * single-pass decoupled-look-back kernel instead of the reference's
+ * recursive work-group scans.  The total goes to *d_total when non-NULL. */
+trax_status trax_prefix_sum(trax_ctx *ctx, const uint32_t *d_in, uint32_t *d_out, uint32_t n,
+                            uint32_t *d_total);
+
 trax_status trax_read_counts(trax_ctx *ctx, trax_counts *out);  /* synchronises */
 
 /* Diagnostic: evaluates the path's FP32 math on the device for n inputs

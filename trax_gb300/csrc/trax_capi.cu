@@ -54,7 +54,7 @@ struct trax_ctx {
     uint32_t *h_stage = nullptr;          /* pinned staging for small uploads */
     size_t h_stage_words = 0;
     cudaEvent_t stage_free = nullptr;     /* last upload from h_stage done */
-    DevBuf seg, g_start, g_base, slots, pcnt, pexcl, ccnt, cexcl, st0, st1, st2;
+    DevBuf seg, g_start, g_base, slots, pexcl, cexcl, st0, st1, st2, st3;
     cudaEvent_t timers[kTimerSlots] = {};
     int blk_pair = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
 
@@ -527,8 +527,8 @@ void trax_ctx_destroy(trax_ctx *ctx)
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
-    DevBuf *bufs[] = {&ctx->seg, &ctx->g_start, &ctx->g_base, &ctx->slots, &ctx->pcnt, &ctx->pexcl,
-                      &ctx->ccnt, &ctx->cexcl, &ctx->st0, &ctx->st1, &ctx->st2, &ctx->grid_buf,
+    DevBuf *bufs[] = {&ctx->seg, &ctx->g_start, &ctx->g_base, &ctx->slots, &ctx->pexcl,
+                      &ctx->cexcl, &ctx->st0, &ctx->st1, &ctx->st2, &ctx->st3, &ctx->grid_buf,
                       &ctx->pairs_buf, &ctx->pair_off, &ctx->cands_buf, &ctx->cand_off, &ctx->trk_off,
                       &ctx->r_seg};
     for (DevBuf *b : bufs) if (b->p) cudaFree(b->p);
@@ -688,6 +688,28 @@ trax_status trax_reset_counts(trax_ctx *ctx)
 {
     if (!ctx) return TRAX_ERR_BAD_ARG;
     CK(cudaMemsetAsync(&ctx->d_state->n_outer, 0, sizeof(DevState) - 8, ctx->stream));
+    return TRAX_OK;
+}
+
+trax_status trax_prefix_sum(trax_ctx *ctx, const uint32_t *d_in, uint32_t *d_out, uint32_t n,
+                            uint32_t *d_total)
+{
+    if (!ctx || (n && (!d_in || !d_out))) return TRAX_ERR_BAD_ARG;
+    const uint32_t items = kScanThreads * kScanItems;
+    trax_status s = ensure(ctx, ctx->st3, (size_t)tiles_for(n, items) * 8);
+    if (s != TRAX_OK) return s;
+    if ((s = ensure_stage(ctx, 1)) != TRAX_OK) return s;
+    ctx->h_stage[0] = n;
+    DevState *st = ctx->d_state;
+    CK(cudaMemcpyAsync(&st->aux_n, ctx->h_stage, 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaEventRecord(ctx->stage_free, ctx->stream));
+    CK(cudaMemsetAsync(&st->tile_ctr[3], 0, 4, ctx->stream));
+    CK(cudaMemsetAsync(ctx->st3.p, 0, (size_t)tiles_for(n, items) * 8, ctx->stream));
+    const uint32_t blocks = std::max(1u, std::min<uint32_t>((n + items - 1) / items,
+                                                            (uint32_t)ctx->blk_scan));
+    k_scan<kScanItems><<<blocks, kScanThreads, 0, ctx->stream>>>(
+        d_in, d_out, &st->aux_n, n, d_total, 3, (unsigned long long *)ctx->st3.p, st);
+    CK(cudaGetLastError());
     return TRAX_OK;
 }
 

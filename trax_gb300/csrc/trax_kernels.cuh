@@ -60,7 +60,8 @@ struct DevState {
     unsigned long long cand_slots;
     unsigned long long cand_truncated;
     uint32_t tile_ctr[4];    /* decoupled look-back tile tickets */
-    uint32_t pad[4];
+    uint32_t aux_n;          /* element count of a standalone prefix sum */
+    uint32_t pad[3];
 };
 
 struct SortedCols {
@@ -320,7 +321,8 @@ __device__ __forceinline__ uint32_t warp_tile_position(uint32_t v, uint32_t tile
     return prefix + x - v;
 }
 
-/* Exclusive scan of in[0..n) into out[0..n], out[n] = total (in-place OK). */
+/* Exclusive scan of in[0..n) into out[0..n) (in place allowed); the total
+ * goes to *total_out when given. */
 template <int ITEMS>
 __global__ void __launch_bounds__(256) k_scan(const uint32_t *in, uint32_t *out,
                                               const uint32_t *n_ptr, uint32_t n_cap,
@@ -330,10 +332,7 @@ __global__ void __launch_bounds__(256) k_scan(const uint32_t *in, uint32_t *out,
     uint32_t n = *n_ptr;
     if (n > n_cap) n = n_cap;
     if (n == 0) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            out[0] = 0;
-            if (total_out) *total_out = 0;
-        }
+        if (blockIdx.x == 0 && threadIdx.x == 0 && total_out) *total_out = 0;
         return;
     }
     lookback_scan<ITEMS>(
@@ -341,7 +340,6 @@ __global__ void __launch_bounds__(256) k_scan(const uint32_t *in, uint32_t *out,
         [&](uint32_t i) { return in[i]; },
         [&](uint32_t i, uint32_t e, uint32_t) { out[i] = e; },
         [&](uint32_t t) {
-            out[n] = t;
             if (total_out) *total_out = t;
         });
 }

@@ -58,6 +58,7 @@ _SIGS = {
                                       C.POINTER(A.TraxGridCfg), C.POINTER(A.TraxPairs),
                                       C.POINTER(A.TraxPairs), C.POINTER(A.TraxTracklets)]),
     "trax_read_counts": (C.c_int, [C.c_void_p, C.POINTER(A.TraxCounts)]),
+    "trax_prefix_sum": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     "trax_reset_counts": (C.c_int, [C.c_void_p]),
     "trax_config_validate": (C.c_int, [C.POINTER(A.TraxConfig), C.POINTER(A.TraxGridCfg)]),
     "trax_layout_validate": (C.c_int, [C.POINTER(A.TraxLayout), C.c_uint32]),
@@ -241,6 +242,11 @@ class Context:
 
     def reset_counts(self):
         self._check(self.lib.trax_reset_counts(self.h))
+
+    def prefix_sum(self, d_in: DeviceBuffer, d_out: DeviceBuffer, n: int, d_total=None):
+        """Exclusive scan of n uint32 on the device (PrefixSum::run)."""
+        self._check(self.lib.trax_prefix_sum(self.h, d_in.ptr, d_out.ptr, int(n),
+                                             d_total.ptr if d_total is not None else None))
 
     def timer_record(self, slot):
         self._check(self.lib.trax_timer_record(self.h, slot))
