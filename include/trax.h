@@ -246,6 +246,25 @@ trax_status trax_triplet_filter(trax_ctx *ctx, const trax_sorted_hits *hits,
 trax_status trax_prefix_sum(trax_ctx *ctx, const uint32_t *d_in, uint32_t *d_out, uint32_t n,
                             uint32_t *d_total);
 
+/* Allocation-free exclusive scan.  No counterpart in the reference: it is
+ * for callers that cannot call cudaMalloc -- code running inside another
+ * framework's memory pool or allocator lock, or inside a stream capture
+ * where allocation is not allowed.  Same result as trax_prefix_sum, but no
+ * context and no allocation: the kernel's look-back scratch is a file-scope
+ * device array of about 33 KB that every GPU loading this library holds
+ * until the process exits.  n is limited to TRAX_PREFIX_SUM_NOALLOC_MAX
+ * (larger n returns TRAX_ERR_BAD_ARG; the message is in
+ * trax_prefix_sum_noalloc_error()).  Runs on the current device and on
+ * `stream` (a cudaStream_t, NULL = the legacy default stream).  The first
+ * call on each device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Every call clears and reuses the same array, so calls that overlap on the
+ * GPU (different streams, or threads without ordering) race: serialise them. */
+#define TRAX_PREFIX_SUM_NOALLOC_MAX 8388608u
+trax_status trax_prefix_sum_noalloc(const uint32_t *d_in, uint32_t *d_out, uint32_t n,
+                                    uint32_t *d_total, void *stream);
+const char *trax_prefix_sum_noalloc_error(void);
+
 trax_status trax_read_counts(trax_ctx *ctx, trax_counts *out);  /* synchronises */
 
 /* Diagnostic: evaluates the path's FP32 math on the device for n inputs

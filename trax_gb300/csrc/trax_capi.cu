@@ -381,6 +381,44 @@ __global__ void k_eval_math(int fn, const float *a, const float *b, float *out, 
 
 std::string g_create_error;
 
+/* ---- allocation-free prefix sum ------------------------------------------
+ * Scratch of trax_prefix_sum_noalloc: a DevState (tile ticket, element count,
+ * status word) followed by one look-back status word per tile.  It lives in
+ * this file-scope device array, so the entry point never allocates; every
+ * GPU that loads the library holds it until the process exits. */
+constexpr uint32_t kNoAllocTiles =
+    (TRAX_PREFIX_SUM_NOALLOC_MAX + kScanThreads * kScanItems - 1) / (kScanThreads * kScanItems);
+constexpr size_t kNoAllocStateWords = (sizeof(DevState) + 7) / 8;
+constexpr size_t kNoAllocWords = kNoAllocStateWords + kNoAllocTiles + 1;
+static __device__ __align__(256) unsigned long long g_noalloc_scratch[kNoAllocWords];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void *g_noalloc_addr[kMaxDevices] = {};
+std::string g_noalloc_error;
+
+__global__ void k_set_u32(uint32_t *dst, uint32_t v) { *dst = v; }
+
+/* Device address of the scratch array on the current device; looked up
+ * once per device (the host-side symbol is only a stand-in). */
+trax_status noalloc_scratch(int dev, unsigned long long **out)
+{
+    if (dev < 0 || dev >= kMaxDevices) return TRAX_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        void *ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess || !ptr) {
+            g_noalloc_error = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+            cudaGetLastError();
+            return TRAX_ERR_DEVICE;
+        }
+        g_noalloc_addr[dev] = ptr;
+    }
+    *out = (unsigned long long *)g_noalloc_addr[dev];
+    return TRAX_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -712,6 +750,51 @@ trax_status trax_prefix_sum(trax_ctx *ctx, const uint32_t *d_in, uint32_t *d_out
     CK(cudaGetLastError());
     return TRAX_OK;
 }
+
+trax_status trax_prefix_sum_noalloc(const uint32_t *d_in, uint32_t *d_out, uint32_t n,
+                                    uint32_t *d_total, void *stream)
+{
+    if (n && (!d_in || !d_out)) {
+        g_noalloc_error = "trax_prefix_sum_noalloc: null input or output";
+        return TRAX_ERR_BAD_ARG;
+    }
+    if (n > TRAX_PREFIX_SUM_NOALLOC_MAX) {
+        g_noalloc_error = "trax_prefix_sum_noalloc: n exceeds TRAX_PREFIX_SUM_NOALLOC_MAX (" +
+                          std::to_string(TRAX_PREFIX_SUM_NOALLOC_MAX) + " elements)";
+        return TRAX_ERR_BAD_ARG;
+    }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        g_noalloc_error = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
+        cudaGetLastError();
+        return TRAX_ERR_NO_DEVICE;
+    }
+    unsigned long long *scratch = nullptr;
+    trax_status s = noalloc_scratch(dev, &scratch);
+    if (s != TRAX_OK) return s;
+    cudaStream_t st = (cudaStream_t)stream;
+    DevState *ds = (DevState *)scratch;
+    unsigned long long *status = scratch + kNoAllocStateWords;
+    const uint32_t items = kScanThreads * kScanItems;
+    const uint32_t tiles = (n + items - 1) / items;
+    /* the previous call's tickets, count and tile flags must start at zero */
+    e = cudaMemsetAsync(scratch, 0, (kNoAllocStateWords + tiles + 1) * 8, st);
+    if (e == cudaSuccess) {
+        k_set_u32<<<1, 1, 0, st>>>(&ds->aux_n, n);
+        const uint32_t blocks = std::max(1u, std::min(tiles, 4u * kNoAllocTiles));
+        k_scan<kScanItems><<<blocks, kScanThreads, 0, st>>>(d_in, d_out, &ds->aux_n, n, d_total,
+                                                            0, status, ds);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+        g_noalloc_error = std::string("trax_prefix_sum_noalloc: ") + cudaGetErrorString(e);
+        return TRAX_ERR_DEVICE;
+    }
+    return TRAX_OK;
+}
+
+const char *trax_prefix_sum_noalloc_error(void) { return g_noalloc_error.c_str(); }
 
 trax_status trax_read_counts(trax_ctx *ctx, trax_counts *out)
 {

@@ -59,6 +59,9 @@ _SIGS = {
                                       C.POINTER(A.TraxPairs), C.POINTER(A.TraxTracklets)]),
     "trax_read_counts": (C.c_int, [C.c_void_p, C.POINTER(A.TraxCounts)]),
     "trax_prefix_sum": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "trax_prefix_sum_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
+                                          C.c_void_p]),
+    "trax_prefix_sum_noalloc_error": (C.c_char_p, []),
     "trax_reset_counts": (C.c_int, [C.c_void_p]),
     "trax_config_validate": (C.c_int, [C.POINTER(A.TraxConfig), C.POINTER(A.TraxGridCfg)]),
     "trax_layout_validate": (C.c_int, [C.POINTER(A.TraxLayout), C.c_uint32]),
