@@ -49,6 +49,10 @@ def parse():
     ap.add_argument("--per-event-sample", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-rates", default="5000,20000",
+                    help="Poisson arrival rates (events/s) for the streaming measurement")
+    ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--serve-pool", type=int, default=128)
     return ap.parse_args()
 
 
@@ -258,6 +262,43 @@ def run_reference(args, dist):
 
 # --------------------------------------------------------------------------
 
+def run_serving(args):
+    """Poisson streams of pile-up ~ U{0..200} events through the
+    continuous-batching server; p50/p99 arrival-to-result latency."""
+    from trax_gb300 import gen
+    from trax_gb300.serve import Server, poisson_arrivals
+    w = gen.WORKLOADS["stream-pileup-u200"]
+    pool = [gen.generate_batch(w, 1, first_event=i) for i in range(args.serve_pool)]
+    hits = np.array([e.n_hits for e in pool])
+    out = {"workload": w.name, "grid": f"{w.n_sectors_z}x{w.n_sectors_phi}",
+           "pool_events": len(pool), "hits_per_event_mean": round(float(hits.mean()), 1),
+           "hits_per_event_max": int(hits.max()), "slots": 3, "max_batch_events": 256,
+           "rates": []}
+    with Server(w.config(), w.n_layers, w.n_sectors_z, w.n_sectors_phi, slots=3,
+                max_batch_events=256, max_event_hits=int(hits.max()) + 1,
+                memory_budget_bytes=24 << 30, keep_results=False) as srv:
+        # warm-up: every slot captures its graph
+        srv.replay(pool, np.arange(len(pool)) % len(pool),
+                   np.full(len(pool), srv.now_ns(), dtype=np.uint64))
+        srv.drain()
+        for rate in [float(r) for r in args.serve_rates.split(",") if r]:
+            srv.reset_stats()
+            n = max(1, int(rate * args.serve_seconds))
+            order = np.random.default_rng(int(rate)).integers(0, len(pool), n)
+            arr = poisson_arrivals(n, rate, srv.now_ns() + 5_000_000, seed=int(rate))
+            srv.replay(pool, order, arr)
+            srv.drain(timeout_ms=600_000)
+            st = srv.stats()
+            out["rates"].append({
+                "offered_events_per_s": rate, "events": st["events"],
+                "sustained_events_per_s": round(st["sustained_events_per_s"], 1),
+                "p50_ms": round(st["p50_ns"] / 1e6, 3), "p99_ms": round(st["p99_ns"] / 1e6, 3),
+                "max_ms": round(st["max_ns"] / 1e6, 3),
+                "mean_batch_events": round(st["batched_events"] / max(1, st["batches"]), 2),
+                "splits": st["splits"], "errors": st["errors"]})
+    return out
+
+
 def run_ours(args, dist):
     from trax_gb300 import Context, gen
     from trax_gb300.ops import Pipeline
@@ -396,6 +437,11 @@ def run_ours(args, dist):
                   "gbs": round(8 * n_scan / (scan_ms / 1000) / 1e9, 1),
                   "note": "in place, 4 B read + 4 B written per element"}
 
+    # ---- streaming serving load (config 5) --------------------------------
+    serving = None
+    if args.serve_rates and dist.world == 1:
+        serving = run_serving(args)
+
     # ---- CPU baseline (rank 0, N=1 only) ----------------------------------
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
@@ -428,6 +474,7 @@ def run_ours(args, dist):
             "kernels": kernels,
             "cpu_baseline": cpu,
             "prefix_sum_1mi": prefix_sum,
+            "serving": serving,
             "clocks": clocks,
             "gpu_launches": launches * args.steps,
             "counts_per_step": {k: counts[k] for k in ("n_hits", "n_pairs", "pair_slots",

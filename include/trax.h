@@ -323,6 +323,70 @@ trax_status trax_kernel_times(trax_ctx *ctx, float *ms, const char **names, int 
 /* Kernels launched by the last pipeline enqueue (graph capture or eager). */
 int trax_kernel_launches(const trax_ctx *ctx);
 
+/* ---- continuous-batching server -------------------------------------- */
+
+/* Requests are single events.  `slots` worker threads each own a context
+ * (stream, reserved buffers, graph); each takes every request that has
+ * arrived, up to its capacity, into its next batch, so batches of different
+ * slots overlap on the device.  The memory budget is split over the slots;
+ * a batch whose scanned pair / candidate / tracklet totals exceed the
+ * capacities is split in halves and rerun.  Results are per event and do not
+ * depend on the batch (tracklet hit indices are positions within the event). */
+typedef struct trax_server trax_server;
+
+typedef struct trax_server_opts {
+    uint32_t slots;                /* batches in flight, 1..16 */
+    uint32_t max_batch_events;     /* events per batch */
+    uint32_t max_event_hits;       /* largest event accepted */
+    uint32_t n_layers;             /* per-event grid */
+    uint32_t n_sectors_z;
+    uint32_t n_sectors_phi;
+    uint64_t memory_budget_bytes;  /* device memory for all slots */
+    int keep_results;              /* 0: results are only counted (load tests) */
+    uint32_t max_batch_hits;       /* hits per batch; 0: as many as the budget allows */
+    uint32_t pairs_per_hit;        /* capacity ratios; 0: 24 pairs, 12 candidates, */
+    uint32_t candidates_per_hit;   /*   4 tracklets per hit of the batch */
+    uint32_t tracklets_per_hit;
+} trax_server_opts;
+
+typedef struct trax_server_result {
+    uint64_t ticket;
+    int status;                    /* trax_status of this request */
+    uint64_t arrival_ns, start_ns, done_ns;   /* trax_now_ns clock */
+    uint32_t batch_events;         /* events in the batch that served it */
+    uint32_t *hit1, *hit2, *hit3;  /* caller buffers (host) */
+    uint32_t capacity;
+    uint32_t n_tracklets;
+    uint32_t offsets[TRAX_MAX_LAYER_TRIPLETS + 1];  /* per layer triplet, within the event */
+} trax_server_result;
+
+typedef struct trax_server_stats {
+    uint64_t submitted, events, batches, batched_events, splits, errors;
+    uint64_t slot_max_hits;        /* hit capacity of one slot's batch */
+    uint64_t p50_ns, p99_ns, max_ns;   /* arrival -> result latency */
+    double sustained_events_per_s;     /* events / (last result - first arrival) */
+} trax_server_stats;
+
+uint64_t trax_now_ns(void);  /* monotonic clock used for arrivals and latencies */
+trax_status trax_server_create(trax_server **out, int device, const trax_config *cfg,
+                               const trax_server_opts *opts);
+void trax_server_destroy(trax_server *srv);
+/* Queues one event (n_events == 1).  arrival_ns: when the request counts as
+ * arrived (0 = now); it is not admitted earlier.  borrow != 0: the host
+ * columns are used in place and must stay valid until the result is out. */
+trax_status trax_server_submit(trax_server *srv, const trax_event_batch *event,
+                               uint64_t arrival_ns, int borrow, uint64_t *ticket);
+/* Submits pool[order[i]] at arrival_ns[i] for i < n from a feeder thread
+ * (borrowed; the pool, order and arrivals must outlive trax_server_drain). */
+trax_status trax_server_replay(trax_server *srv, const trax_event_batch *pool,
+                               const uint32_t *order, const uint64_t *arrival_ns, uint32_t n);
+/* Next finished request (keep_results != 0), waiting up to timeout_ms. */
+trax_status trax_server_poll(trax_server *srv, trax_server_result *out, int timeout_ms);
+/* Waits until every submitted request has finished. */
+trax_status trax_server_drain(trax_server *srv, int timeout_ms);
+trax_status trax_server_get_stats(trax_server *srv, trax_server_stats *out);
+trax_status trax_server_reset_stats(trax_server *srv);
+
 #ifdef __cplusplus
 }
 #endif

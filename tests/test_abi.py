@@ -44,7 +44,8 @@ def test_every_declared_symbol_is_exported(lib):
     ("trax_sorted_hits", A.TraxSortedHits), ("trax_layout", A.TraxLayout),
     ("trax_pairs", A.TraxPairs), ("trax_tracklets", A.TraxTracklets),
     ("trax_counts", A.TraxCounts), ("trax_event_batch", A.TraxEventBatch),
-    ("trax_batch_result", A.TraxBatchResult)])
+    ("trax_batch_result", A.TraxBatchResult), ("trax_server_opts", A.TraxServerOpts),
+    ("trax_server_result", A.TraxServerResult), ("trax_server_stats", A.TraxServerStats)])
 def test_struct_layout(lib, name, cls):
     assert lib.trax_abi_sizeof(name.encode()) == C.sizeof(cls)
 

@@ -1,0 +1,74 @@
+"""Continuous batching: events arriving as a Poisson stream are batched
+while other batches run, and every event's result equals the event run
+alone (config 5's determinism requirement)."""
+import numpy as np
+import pytest
+
+from trax_gb300 import gen
+from trax_gb300.ops import Pipeline
+from trax_gb300.serve import Server, poisson_arrivals
+
+pytestmark = pytest.mark.gpu
+
+
+def small_stream_workload():
+    w = gen.WORKLOADS["stream-pileup-u200"]
+    return gen.Workload("stream-pileup-u20", 5, w.n_layers, w.noise, w.pt_range,
+                        w.n_sectors_z, w.n_sectors_phi, w.n_triplets, pileup_uniform=20)
+
+
+def test_results_equal_alone_and_in_mix(gpu_ctx):
+    w = small_stream_workload()
+    events = [gen.generate_batch(w, 1, first_event=i) for i in range(48)]
+    cfg = w.config()
+    # each event alone through the batched pipeline, as input positions
+    p = Pipeline(gpu_ctx, cfg, w.grid(1), 1, max(e.n_hits for e in events) + 1,
+                 2_000_000, 2_000_000, 400_000)
+    alone = [p.seed(e, input_indices=True)[0] for e in events]
+    with Server(cfg, w.n_layers, w.n_sectors_z, w.n_sectors_phi, slots=2,
+                max_batch_events=16, memory_budget_bytes=2 << 30) as srv:
+        t0 = srv.now_ns() + 20_000_000
+        arrivals = poisson_arrivals(len(events), 5000.0, t0, seed=3)
+        tickets = [srv.submit(e, int(a)) for e, a in zip(events, arrivals)]
+        got = {}
+        while len(got) < len(events):
+            r = srv.poll(timeout_ms=10_000)
+            assert r is not None, "server stalled"
+            assert r["status"] == 0
+            got[r["ticket"]] = r
+        stats = srv.stats()
+    for t, ref in zip(tickets, alone):
+        assert np.array_equal(got[t]["tracklets"], ref)
+    assert stats["events"] == len(events) and stats["errors"] == 0
+    assert stats["batches"] < len(events)  # requests were batched together
+    assert max(r["batch_events"] for r in got.values()) > 1
+    assert stats["p99_ns"] >= stats["p50_ns"] > 0
+
+
+def test_capacity_split_keeps_results(gpu_ctx):
+    """A tiny memory budget forces batches to overflow and split; results
+    stay identical."""
+    w = small_stream_workload()
+    events = [gen.generate_batch(w, 1, first_event=100 + i) for i in range(12)]
+    cfg = w.config()
+    p = Pipeline(gpu_ctx, cfg, w.grid(1), 1, max(e.n_hits for e in events) + 1,
+                 2_000_000, 2_000_000, 400_000)
+    alone = [p.seed(e, input_indices=True)[0] for e in events]
+    total = sum(e.n_hits for e in events)
+    # one pair per hit of capacity: a batch of all 12 events overflows (they
+    # make several pairs per hit) and is split until the pieces fit
+    with Server(cfg, w.n_layers, w.n_sectors_z, w.n_sectors_phi, slots=1,
+                max_batch_events=12, max_event_hits=total, max_batch_hits=total,
+                pairs_per_hit=1, memory_budget_bytes=1 << 30) as srv:
+        t0 = srv.now_ns()
+        tickets = [srv.submit(e, t0) for e in events]  # all arrive at once
+        got = {}
+        while len(got) < len(events):
+            r = srv.poll(timeout_ms=10_000)
+            assert r is not None and r["status"] == 0
+            got[r["ticket"]] = r
+        stats = srv.stats()
+    for t, ref in zip(tickets, alone):
+        assert np.array_equal(got[t]["tracklets"], ref)
+    assert stats["errors"] == 0
+    assert stats["splits"] > 0

@@ -104,3 +104,31 @@ def make_config(rows, min_radius, max_radius, min_pt, bz=0.0) -> TraxConfig:
     cfg.min_pt = float(min_pt)
     cfg.bz = float(bz)
     return cfg
+
+
+class TraxServerOpts(C.Structure):
+    _fields_ = [("slots", C.c_uint32), ("max_batch_events", C.c_uint32),
+                ("max_event_hits", C.c_uint32), ("n_layers", C.c_uint32),
+                ("n_sectors_z", C.c_uint32), ("n_sectors_phi", C.c_uint32),
+                ("memory_budget_bytes", C.c_uint64), ("keep_results", C.c_int),
+                ("max_batch_hits", C.c_uint32), ("pairs_per_hit", C.c_uint32),
+                ("candidates_per_hit", C.c_uint32), ("tracklets_per_hit", C.c_uint32)]
+
+
+class TraxServerResult(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("status", C.c_int), ("arrival_ns", C.c_uint64),
+                ("start_ns", C.c_uint64), ("done_ns", C.c_uint64), ("batch_events", C.c_uint32),
+                ("hit1", C.c_void_p), ("hit2", C.c_void_p), ("hit3", C.c_void_p),
+                ("capacity", C.c_uint32), ("n_tracklets", C.c_uint32),
+                ("offsets", C.c_uint32 * (MAX_LAYER_TRIPLETS + 1))]
+
+
+class TraxServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("events", C.c_uint64), ("batches", C.c_uint64),
+                ("batched_events", C.c_uint64), ("splits", C.c_uint64), ("errors", C.c_uint64),
+                ("slot_max_hits", C.c_uint64), ("p50_ns", C.c_uint64), ("p99_ns", C.c_uint64),
+                ("max_ns", C.c_uint64), ("sustained_events_per_s", C.c_double)]
+
+    def as_dict(self):
+        return {k: (float(getattr(self, k)) if t is C.c_double else int(getattr(self, k)))
+                for k, t in self._fields_}

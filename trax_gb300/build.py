@@ -14,7 +14,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libtrax_gb300.so")
-SOURCES = [os.path.join(CSRC, "trax_capi.cu")]
+SOURCES = [os.path.join(CSRC, "trax_capi.cu"), os.path.join(CSRC, "trax_serve.cpp")]
 DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("trax_kernels.cuh", "trax_math.h")] + [
     os.path.join(HERE, "..", "include", "trax.h")]
 
@@ -44,7 +44,7 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
     if not force and up_to_date():
         return LIB
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), *NVCC_FLAGS, *extra, "-o", tmp, *SOURCES]
+    cmd = [nvcc(), *NVCC_FLAGS, "-Xcompiler", "-pthread", *extra, "-o", tmp, *SOURCES]
     if verbose:
         print(" ".join(cmd), file=sys.stderr)
     subprocess.check_call(cmd, cwd=HERE)

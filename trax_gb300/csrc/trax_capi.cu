@@ -482,7 +482,10 @@ size_t trax_abi_sizeof(const char *name)
         {"trax_sorted_hits", sizeof(trax_sorted_hits)}, {"trax_layout", sizeof(trax_layout)},
         {"trax_pairs", sizeof(trax_pairs)}, {"trax_tracklets", sizeof(trax_tracklets)},
         {"trax_counts", sizeof(trax_counts)}, {"trax_event_batch", sizeof(trax_event_batch)},
-        {"trax_batch_result", sizeof(trax_batch_result)}};
+        {"trax_batch_result", sizeof(trax_batch_result)},
+        {"trax_server_opts", sizeof(trax_server_opts)},
+        {"trax_server_result", sizeof(trax_server_result)},
+        {"trax_server_stats", sizeof(trax_server_stats)}};
     for (const auto &e : t)
         if (strcmp(e.n, name) == 0) return e.s;
     return 0;

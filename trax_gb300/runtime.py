@@ -79,6 +79,18 @@ _SIGS = {
     "trax_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_char_p),
                                     C.c_int, C.POINTER(C.c_int)]),
     "trax_kernel_launches": (C.c_int, [C.c_void_p]),
+    "trax_now_ns": (C.c_uint64, []),
+    "trax_server_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(A.TraxConfig),
+                                     C.POINTER(A.TraxServerOpts)]),
+    "trax_server_destroy": (None, [C.c_void_p]),
+    "trax_server_submit": (C.c_int, [C.c_void_p, C.POINTER(A.TraxEventBatch), C.c_uint64, C.c_int,
+                                     C.POINTER(C.c_uint64)]),
+    "trax_server_replay": (C.c_int, [C.c_void_p, C.POINTER(A.TraxEventBatch), C.c_void_p,
+                                     C.c_void_p, C.c_uint32]),
+    "trax_server_poll": (C.c_int, [C.c_void_p, C.POINTER(A.TraxServerResult), C.c_int]),
+    "trax_server_drain": (C.c_int, [C.c_void_p, C.c_int]),
+    "trax_server_get_stats": (C.c_int, [C.c_void_p, C.POINTER(A.TraxServerStats)]),
+    "trax_server_reset_stats": (C.c_int, [C.c_void_p]),
 }
 
 EXPORTED_SYMBOLS = tuple(_SIGS)
