@@ -53,6 +53,9 @@ def parse():
                     help="Poisson arrival rates (events/s) for the streaming measurement")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--serve-pool", type=int, default=128)
+    ap.add_argument("--autotune", action="store_true",
+                    help="grid sweep on pile-up-200 events (config 4), reported under 'autotune'")
+    ap.add_argument("--autotune-events", type=int, default=64)
     return ap.parse_args()
 
 
@@ -262,6 +265,76 @@ def run_reference(args, dist):
 
 # --------------------------------------------------------------------------
 
+def run_autotune(args, ctx):
+    """Config 4: pile-up-200 events, grid sweep {8..64} x {16..128} with the
+    walk tuned per grid; per-kernel HBM fractions at the best grid and the
+    plain per-event form at that grid."""
+    import ctypes as C
+    from trax_gb300 import gen
+    from trax_gb300.autotune import sweep_grids, tune_walk, density_class
+    from trax_gb300.ops import Pipeline
+    w = gen.WORKLOADS["pileup200"]
+    b = gen.generate_batch(w, args.autotune_events)
+    from trax_gb300.autotune import GRID_Z, GRID_PHI
+    grids = [(z, ph) for z in GRID_Z for ph in GRID_PHI] + [(12, 32)]
+    rows = sweep_grids(ctx, w, b, grids=grids, reps=3)
+    best = rows[0]
+    wk = gen.Workload(w.name, w.config_id, w.n_layers, w.noise, w.pt_range,
+                      best["n_sectors_z"], best["n_sectors_phi"], w.n_triplets,
+                      pileup_mean=w.pileup_mean)
+    N = b.n_hits
+    p = Pipeline(ctx, wk.config(), wk.grid(b.n_events), b.n_events, N, 80 * N, 80 * N, 8 * N)
+    _, _, counts = p.seed(b)
+    ctx.set_tuning(*best["walk"])
+    p.stage(b)
+    ctx._check(ctx.lib.trax_set_profiling(ctx.h, 1))
+    p.run_staged()
+    kt = {}
+    for _ in range(5):
+        p.run_staged()
+        ms = (C.c_float * 64)()
+        names = (C.c_char_p * 64)()
+        n = C.c_int()
+        ctx._check(ctx.lib.trax_kernel_times(ctx.h, ms, names, 64, C.byref(n)))
+        for i in range(n.value):
+            kt.setdefault(names[i].decode(), []).append(ms[i])
+    ctx._check(ctx.lib.trax_set_profiling(ctx.h, 0))
+    peak, _ = hbm_peak()
+    kernels = {}
+    for k, v in kt.items():
+        m = statistics.median(v)
+        alg = algorithmic_bytes(k, b, wk, counts)
+        kernels[k] = {"ms": round(m, 4)}
+        if alg and m > 0:
+            kernels[k]["hbm_frac"] = round(alg / (m / 1000) / 1e9 / peak, 5)
+    # plain per-event form at the best grid
+    S = min(16, b.n_events)
+    singles = [b.slice_events(e, 1) for e in range(S)]
+    pe = Pipeline(ctx, wk.config(), wk.grid(1), 1, max(x.n_hits for x in singles) + 1,
+                  80 * N // b.n_events * 4, 80 * N // b.n_events * 4, 8 * N // b.n_events * 4)
+    ctx.set_tuning(*best["walk"])
+    for x in singles[:2]:
+        pe.stage(x)
+        ctx._check(ctx.lib.trax_run_staged_eager(ctx.h))
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for x in singles:
+        pe.stage(x)
+        ctx._check(ctx.lib.trax_run_staged_eager(ctx.h))
+        ctx.synchronize()
+    per_event = S / (time.perf_counter() - t0)
+    ctx.set_tuning(48, 16)
+    return {"workload": w.name, "events": b.n_events,
+            "hits_per_event": round(N / b.n_events, 1),
+            "class": density_class(N / b.n_events), "best": best,
+            "default_12x32": next((r for r in rows if r.get("grid") == "12x32"), None),
+            "kernels_at_best": kernels,
+            "per_event_form_events_per_s": round(per_event, 1),
+            "batched_over_per_event": round(best["events_per_s"] / per_event, 2),
+            "sweep": [{k: r[k] for k in ("grid", "events_per_s", "walk") if k in r}
+                      for r in rows]}
+
+
 def run_serving(args):
     """Poisson streams of pile-up ~ U{0..200} events through the
     continuous-batching server; p50/p99 arrival-to-result latency."""
@@ -321,6 +394,12 @@ def run_ours(args, dist):
             caps, (counts["n_pairs"], counts["n_candidates"], counts["n_tracklets"]))]
     if counts["status"] != 0:
         raise SystemExit(f"device status {counts}")
+
+    # ---- result-neutral walk tuning on the resident batch ------------------
+    from trax_gb300.autotune import tune_walk
+    best_walk, walk_ms = tune_walk(ctx, p, b, reps=3)
+    tuning = {"run_walk": best_walk[0], "index_min": best_walk[1],
+              "candidates_ms": {f"{k[0]}/{k[1]}": round(v, 4) for k, v in walk_ms.items()}}
 
     # ---- device-resident value: graph replay on staged inputs -------------
     p.stage(b)
@@ -437,6 +516,11 @@ def run_ours(args, dist):
                   "gbs": round(8 * n_scan / (scan_ms / 1000) / 1e9, 1),
                   "note": "in place, 4 B read + 4 B written per element"}
 
+    # ---- autotuned sweep (config 4), optional ------------------------------
+    autotune = None
+    if args.autotune and dist.world == 1:
+        autotune = run_autotune(args, ctx)
+
     # ---- streaming serving load (config 5) --------------------------------
     serving = None
     if args.serve_rates and dist.world == 1:
@@ -475,6 +559,8 @@ def run_ours(args, dist):
             "cpu_baseline": cpu,
             "prefix_sum_1mi": prefix_sum,
             "serving": serving,
+            "tuning": tuning,
+            "autotune": autotune,
             "clocks": clocks,
             "gpu_launches": launches * args.steps,
             "counts_per_step": {k: counts[k] for k in ("n_hits", "n_pairs", "pair_slots",

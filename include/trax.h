@@ -194,6 +194,19 @@ trax_status trax_configure(trax_ctx *ctx, const trax_config *cfg);
 /* TripletConfigurations::minRadiusCurvature(minPt, Bz) in cm. */
 float trax_min_radius_curvature(float min_pt, float bz);
 
+/* How the pair and prediction kernels visit a window's candidates.  Results
+ * never depend on it, only speed: a run of neighbouring cells with at most
+ * run_walk hits is walked hit by hit; in larger runs, every cell with more
+ * than index_min (<= 256) hits is searched through a per-cell z index.
+ * Sparse events favour walking, dense (pile-up) events the index.
+ * trax_configure installs run_walk 48, index_min 16. */
+typedef struct trax_tuning {
+    uint32_t run_walk;
+    uint32_t index_min;
+} trax_tuning;
+trax_status trax_set_tuning(trax_ctx *ctx, const trax_tuning *t);
+trax_status trax_get_tuning(const trax_ctx *ctx, trax_tuning *t);
+
 /* ---- device memory helpers (for hosts without their own CUDA binding) -- */
 
 trax_status trax_dev_alloc(trax_ctx *ctx, void **ptr, size_t bytes);

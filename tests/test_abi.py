@@ -40,6 +40,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 @pytest.mark.parametrize("name,cls", [
     ("trax_grid_cfg", A.TraxGridCfg), ("trax_layer_triplet", A.TraxLayerTriplet),
+    ("trax_tuning", A.TraxTuning),
     ("trax_config", A.TraxConfig), ("trax_hits", A.TraxHits),
     ("trax_sorted_hits", A.TraxSortedHits), ("trax_layout", A.TraxLayout),
     ("trax_pairs", A.TraxPairs), ("trax_tracklets", A.TraxTracklets),

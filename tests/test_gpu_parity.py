@@ -193,3 +193,25 @@ def test_bad_hit_flagged_without_fault(gpu_ctx):
     assert c["status"] == 6 and c["error_detail"] == 1
     d_ctx.reset_counts()
     assert d_ctx.counts()["status"] == 0
+
+
+def test_tuning_does_not_change_results(gpu_ctx):
+    """Walking vs index search of the candidates is a speed knob only: dense
+    pile-up events give bit-identical pipelines under every setting, equal to
+    the oracle."""
+    w = gen.WORKLOADS["pileup50-batch100"]
+    b = gen.generate_batch(w, 3)
+    ref = oracle.canonical(oracle.run(b, w.config(), w.grid(3), 4, n_threads=1))["tracklets"]
+    p = Pipeline(gpu_ctx, w.config(), w.grid(3), 3, b.n_hits, 60 * b.n_hits, 60 * b.n_hits,
+                 8 * b.n_hits)
+    outs = []
+    try:
+        for walk, imin in ((0, 0), (0, 16), (48, 16), (96, 32), (1 << 30, 256)):
+            gpu_ctx.set_tuning(walk, imin)
+            trk, off, counts = p.seed(b)
+            assert counts["status"] == 0
+            outs.append(trk)
+    finally:
+        gpu_ctx.set_tuning(48, 16)
+    for t in outs:
+        assert np.array_equal(t, ref)

@@ -36,6 +36,10 @@ class TraxConfig(C.Structure):
                 ("min_pt", C.c_float), ("bz", C.c_float)]
 
 
+class TraxTuning(C.Structure):
+    _fields_ = [("run_walk", C.c_uint32), ("index_min", C.c_uint32)]
+
+
 class TraxHits(C.Structure):
     _fields_ = [("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p),
                 ("layer", C.c_void_p), ("detector_id", C.c_void_p),

@@ -31,6 +31,8 @@ constexpr int kScanThreads = 256;
 constexpr int kFilterItems = 4;
 constexpr int kTileItems = 32;      /* items per fused pair / predict tile (one warp) */
 constexpr int kFusedThreads = 256;  /* threads per block of the fused kernels */
+constexpr uint32_t kDefaultRunWalk = 48;  /* see trax_set_tuning */
+constexpr uint32_t kDefaultIndexMin = 16;
 
 struct DevBuf {
     void *p = nullptr;
@@ -54,7 +56,7 @@ struct trax_ctx {
     uint32_t *h_stage = nullptr;          /* pinned staging for small uploads */
     size_t h_stage_words = 0;
     cudaEvent_t stage_free = nullptr;     /* last upload from h_stage done */
-    DevBuf seg, g_start, g_base, slots, pexcl, cexcl, st0, st1, st2, st3;
+    DevBuf seg, g_start, g_base, slots, pexcl, cexcl, st0, st1, st2, st3, zi;
     cudaEvent_t timers[kTimerSlots] = {};
     int blk_pair = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
 
@@ -272,6 +274,20 @@ trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *gr
     return mark(ctx, "pair_offsets");
 }
 
+/* Per-cell z index of the sorted hits (k_zindex) into ctx->zi. */
+trax_status enqueue_zindex(trax_ctx *ctx, const SortedCols &h, const uint32_t *grid,
+                           uint32_t max_hits)
+{
+    if (ctx->kp.zi_min >= 256) return TRAX_OK; /* no cell is searched: no index */
+    trax_status s = ensure(ctx, ctx->zi, (size_t)max_hits * 8 + 8);
+    if (s != TRAX_OK) return s;
+    k_zindex<<<ctx->blk_small * 4, 256, 0, ctx->stream>>>(
+        grid, ctx->kp.n_layers * ctx->kp.C, ctx->kp.zi_min, h.z, h.phi, (float2 *)ctx->zi.p,
+        ctx->d_state);
+    CK(cudaGetLastError());
+    return mark(ctx, "zindex");
+}
+
 trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *grid,
                             const uint2 *pairs, const uint32_t *pair_offsets, uint32_t pair_cap,
                             uint2 *cands, uint32_t *cand_offsets, uint32_t cand_cap,
@@ -289,8 +305,8 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
     CK(cudaMemsetAsync(&st->tile_ctr[1], 0, 4, ctx->stream));
     CK(cudaMemsetAsync(ctx->st1.p, 0, (size_t)ntile * 8, ctx->stream));
     k_predict_fused<<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
-        kp, grid, h.x, h.y, h.z, h.phi, h.event, h.layer, pairs, &st->n_pairs, pair_cap, cexcl,
-        cands, cand_cap, (unsigned long long *)ctx->st1.p, st);
+        kp, grid, h.x, h.y, h.z, h.phi, h.event, h.layer, (const float2 *)ctx->zi.p, pairs,
+        &st->n_pairs, pair_cap, cexcl, cands, cand_cap, (unsigned long long *)ctx->st1.p, st);
     if ((s = mark(ctx, "predict")) != TRAX_OK) return s;
     k_cand_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(pair_offsets, cexcl, cand_offsets,
                                                             kp.n_lt, pair_cap, &st->n_cands,
@@ -478,6 +494,7 @@ size_t trax_abi_sizeof(const char *name)
     if (!name) return 0;
     const struct { const char *n; size_t s; } t[] = {
         {"trax_grid_cfg", sizeof(trax_grid_cfg)}, {"trax_layer_triplet", sizeof(trax_layer_triplet)},
+        {"trax_tuning", sizeof(trax_tuning)},
         {"trax_config", sizeof(trax_config)}, {"trax_hits", sizeof(trax_hits)},
         {"trax_sorted_hits", sizeof(trax_sorted_hits)}, {"trax_layout", sizeof(trax_layout)},
         {"trax_pairs", sizeof(trax_pairs)}, {"trax_tracklets", sizeof(trax_tracklets)},
@@ -569,7 +586,7 @@ void trax_ctx_destroy(trax_ctx *ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
     DevBuf *bufs[] = {&ctx->seg, &ctx->g_start, &ctx->g_base, &ctx->slots, &ctx->pexcl,
-                      &ctx->cexcl, &ctx->st0, &ctx->st1, &ctx->st2, &ctx->st3, &ctx->grid_buf,
+                      &ctx->cexcl, &ctx->st0, &ctx->st1, &ctx->st2, &ctx->st3, &ctx->zi, &ctx->grid_buf,
                       &ctx->pairs_buf, &ctx->pair_off, &ctx->cands_buf, &ctx->cand_off, &ctx->trk_off,
                       &ctx->r_seg};
     for (DevBuf *b : bufs) if (b->p) cudaFree(b->p);
@@ -642,11 +659,37 @@ trax_status trax_configure(trax_ctx *ctx, const trax_config *cfg)
         kp.acos_rmin[l] = trax_acosf(kp.rmin[l] / (2 * kp.rmin_curv));
         kp.acos_rmax[l] = trax_acosf(kp.rmax[l] / (2 * kp.rmin_curv));
     }
+    if (kp.run_walk == 0 && kp.zi_min == 0) {
+        kp.run_walk = kDefaultRunWalk;
+        kp.zi_min = kDefaultIndexMin;
+    }
     ctx->configured = true;
     if (ctx->graph) {
         cudaGraphExecDestroy(ctx->graph);
         ctx->graph = nullptr;
     }
+    return TRAX_OK;
+}
+
+trax_status trax_set_tuning(trax_ctx *ctx, const trax_tuning *t)
+{
+    if (!ctx || !t) return TRAX_ERR_BAD_ARG;
+    if (t->index_min > 256) return fail(ctx, TRAX_ERR_BAD_ARG, "index_min must be <= 256");
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->kp.run_walk = t->run_walk;
+    ctx->kp.zi_min = t->index_min;
+    if (ctx->graph) {
+        cudaGraphExecDestroy(ctx->graph);
+        ctx->graph = nullptr;
+    }
+    return TRAX_OK;
+}
+
+trax_status trax_get_tuning(const trax_ctx *ctx, trax_tuning *t)
+{
+    if (!ctx || !t) return TRAX_ERR_BAD_ARG;
+    t->run_walk = ctx->kp.run_walk;
+    t->index_min = ctx->kp.zi_min;
     return TRAX_OK;
 }
 
@@ -863,10 +906,12 @@ trax_status trax_triplet_predict(trax_ctx *ctx, const trax_sorted_hits *hits,
     if (s != TRAX_OK) return s;
     fill_grid_params(ctx->kp, grid);
     const uint32_t G = grid->n_events * ctx->kp.n_lt;
+    if ((s = set_sizes(ctx, grid->n_events, hits->n)) != TRAX_OK) return s;
     /* the pair total is pairs->offsets[G]; copy it into the state word the
      * kernels read (device to device, stream ordered) */
     CK(cudaMemcpyAsync(&ctx->d_state->n_pairs, pairs->offsets + G, 4, cudaMemcpyDeviceToDevice,
                        ctx->stream));
+    if ((s = enqueue_zindex(ctx, sorted_from(hits), d_grid, hits->n)) != TRAX_OK) return s;
     return enqueue_predict(ctx, sorted_from(hits), d_grid, (const uint2 *)pairs->pairs,
                            pairs->offsets, pairs->capacity, (uint2 *)cands->pairs, cands->offsets,
                            cands->capacity, G);
@@ -924,6 +969,7 @@ trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers
     for (int i = 0; i < 3; ++i) if ((s = ensure(ctx, ctx->trk_map[i], (size_t)max_tracklets * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->trk_off, (size_t)(G + 1) * 4)) != TRAX_OK) return s;
     /* scratch at its maximum so the captured graph never reallocates */
+    if ((s = ensure(ctx, ctx->zi, (size_t)max_hits * 8 + 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->g_start, G * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->g_base, (G + 1) * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->slots, slot_cap * 8)) != TRAX_OK) return s;
@@ -975,6 +1021,8 @@ trax_status enqueue_pipeline(trax_ctx *ctx)
     if (s != TRAX_OK) return s;
     CK(cudaMemsetAsync(&ctx->d_state->n_outer, 0, sizeof(DevState) - 8, ctx->stream));
     s = enqueue_grid(ctx, ic, sc, seg, seg + nseg, grid, nseg, ctx->r_hits);
+    if (s != TRAX_OK) return s;
+    s = enqueue_zindex(ctx, sc, grid, ctx->r_hits);
     if (s != TRAX_OK) return s;
     const uint32_t slot_cap = ctx->r_hits * T + 1;
     s = enqueue_pairs(ctx, sc, grid, (uint2 *)ctx->pairs_buf.p, (uint32_t *)ctx->pair_off.p,

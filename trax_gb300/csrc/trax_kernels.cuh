@@ -44,6 +44,7 @@ struct KParams {
      * loop invariants of the phi windows, evaluated once on the host with the
      * same trax_acosf (host and device agree bit for bit) */
     float acos_rmin[kMaxLayers], acos_rmax[kMaxLayers];
+    uint32_t run_walk, zi_min;   /* candidate-walk tuning, see k_zindex */
 };
 
 /* Device-side sizes, counters and status of one pipeline run. */
@@ -786,6 +787,93 @@ __global__ void k_group_offsets(const uint32_t *g_base, const uint32_t *excl, ui
 /* ------------------------------------------------------------------------
  * Stage 3: triplet prediction.  One warp per pair.
  * ---------------------------------------------------------------------- */
+/* ------------------------------------------------------------------------
+ * Per-cell z index.  For every cell with zi_min..kZiMax hits, the (z, phi)
+ * of its hits sorted by z (ties by sorted position) at the cell's own
+ * positions.  The candidate loops binary-search a z window in it instead of
+ * walking the cell; each hit found still gets the reference's exact float
+ * tests, so accepted counts are unchanged.  Smaller and larger cells are
+ * walked.
+ * Sort key: float bits made unsigned-orderable, -0 folded onto +0 and every
+ * NaN last, so the order is total and agrees with float comparison on all
+ * values a window test can accept.
+ * ---------------------------------------------------------------------- */
+constexpr uint32_t kZiMax = 256;
+/* Runtime knobs (KParams::run_walk, KParams::zi_min; they never change a
+ * result): runs of cells with at most run_walk hits are walked whole, and
+ * only cells with more than zi_min hits are indexed and searched -- a walk
+ * pipelines its loads, a search wins once cells are dense. */
+
+__device__ __forceinline__ uint32_t zkey(float z)
+{
+    const uint32_t b = __float_as_uint(z);
+    if ((b & 0x7fffffffu) == 0u) return 0x80000000u;
+    if ((b & 0x7f800000u) == 0x7f800000u && (b & 0x007fffffu)) return 0xffffffffu;
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+/* Each lane probes one cell of a 32-cell group; the warp then ranks the
+ * hits of every indexable cell of the group together and scatters them. */
+__global__ void __launch_bounds__(256) k_zindex(const uint32_t *grid, uint32_t cells_per_event,
+                                                uint32_t zi_min, const float *Z, const float *PHI,
+                                                float2 *zi, DevState *st)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t total = st->n_events * cells_per_event;
+    const uint32_t n_hits = st->n_hits;
+    for (uint32_t q0 = gw * 32; q0 < total; q0 += nw * 32) {
+        const uint32_t q = q0 + lane;
+        uint32_t my_a = 0, my_cnt = 0;
+        if (q < total) {
+            my_a = grid[q];
+            const uint32_t b = q + 1 < total ? grid[q + 1] : n_hits;
+            my_cnt = b > my_a ? b - my_a : 0u;
+        }
+        uint32_t todo = __ballot_sync(kFull, my_cnt > zi_min && my_cnt <= kZiMax);
+        for (; todo; todo &= todo - 1) {
+        const int src = __ffs(todo) - 1;
+        const uint32_t a = __shfl_sync(kFull, my_a, src);
+        const uint32_t cnt = __shfl_sync(kFull, my_cnt, src);
+        uint32_t key[8], rank[8];
+        float zz[8], pp[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t i = k * 32 + lane;
+            key[k] = 0xffffffffu;
+            rank[k] = 0;
+            zz[k] = 0.f;
+            pp[k] = 0.f;
+            if (i < cnt) {
+                zz[k] = Z[a + i];
+                pp[k] = PHI[a + i];
+                key[k] = zkey(zz[k]);
+            }
+        }
+#pragma unroll
+        for (int ks = 0; ks < 8; ++ks) {
+            if ((uint32_t)ks * 32 >= cnt) break;
+            for (uint32_t t = 0; t < 32; ++t) {
+                const uint32_t s_idx = ks * 32 + t;
+                if (s_idx >= cnt) break;
+                const uint32_t ksrc = __shfl_sync(kFull, key[ks], t);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const uint32_t i = k * 32 + lane;
+                    rank[k] += (ksrc < key[k] || (ksrc == key[k] && s_idx < i)) ? 1u : 0u;
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t i = k * 32 + lane;
+            if (i < cnt) zi[a + rank[k]] = make_float2(zz[k], pp[k]);
+        }
+        }
+    }
+}
+
 struct PredWindow {
     float zLow[2], zHigh[2];
     uint32_t zLowSector[2], zHighSector[2];
@@ -874,23 +962,11 @@ __device__ __forceinline__ PredWindow pred_window(const KParams &kp, uint32_t lt
  * block barrier (so no warp waits for a slower warp); the store sweep writes
  * the first min(A, B) accepts of window B, the reference's truncation.
  */
-__device__ __forceinline__ void pred_row(const uint32_t *lGrid3, uint32_t P1, uint32_t zs,
-                                         uint32_t pLow, uint32_t pHigh, uint32_t wrap,
-                                         uint32_t &jlo, uint32_t &end2, uint32_t &rowEnd,
-                                         uint32_t &len)
-{
-    const uint32_t rowStart = lGrid3[zs * P1];
-    rowEnd = lGrid3[(zs + 1) * P1];
-    len = rowEnd - rowStart;
-    jlo = lGrid3[zs * P1 + pLow];
-    end2 = wrap * rowEnd + lGrid3[zs * P1 + pHigh] - wrap * rowStart;
-}
-
-__global__ void __launch_bounds__(256) k_predict_fused(
+__global__ void __launch_bounds__(256, 5) k_predict_fused(
     KParams kp, const uint32_t *grid, const float *X, const float *Y, const float *Z,
-    const float *PHI, const uint32_t *EVENT, const uint32_t *LAYER, const uint2 *pairs,
-    const uint32_t *n_pairs_ptr, uint32_t pair_cap, uint32_t *cexcl, uint2 *cands,
-    uint32_t cand_cap, unsigned long long *status, DevState *st)
+    const float *PHI, const uint32_t *EVENT, const uint32_t *LAYER, const float2 *zi,
+    const uint2 *pairs, const uint32_t *n_pairs_ptr, uint32_t pair_cap, uint32_t *cexcl,
+    uint2 *cands, uint32_t cand_cap, unsigned long long *status, DevState *st)
 {
     const uint32_t lane = threadIdx.x & 31;
     uint32_t n = *n_pairs_ptr;
@@ -941,15 +1017,53 @@ __global__ void __launch_bounds__(256) k_predict_fused(
             for (uint32_t zs = zlo; zs < zhi; ++zs) {
                 const bool inA = zs >= w.zLowSector[0] && zs < w.zHighSector[0];
                 const bool inB = zs >= w.zLowSector[1] && zs < w.zHighSector[1];
-                uint32_t j, end2, rowEnd, len;
-                pred_row(lGrid3, P1, zs, w.phiLowSector, w.phiHighSector, w.wrap, j, end2,
-                         rowEnd, len);
-                for (; j < end2; ++j) {
-                    const uint32_t idx = j - (j >= rowEnd ? len : 0u);
-                    const float zz = Z[idx];
-                    const bool ph = phi_in(PHI[idx], w.phiLow, w.phiHigh, w.wrap);
-                    cA += (inA && ph && w.zLow[0] <= zz && zz <= w.zHigh[0]) ? 1u : 0u;
-                    cB += (inB && ph && w.zLow[1] <= zz && zz <= w.zHigh[1]) ? 1u : 0u;
+                const uint32_t kA0 = zkey(w.zLow[0]), kA1 = zkey(w.zHigh[0]);
+                const uint32_t kB0 = zkey(w.zLow[1]), kB1 = zkey(w.zHigh[1]);
+                const uint32_t keyLo = min(inA ? kA0 : 0xffffffffu, inB ? kB0 : 0xffffffffu);
+                const uint32_t keyHi = max(inA ? kA1 : 0u, inB ? kB1 : 0u);
+                const uint32_t *row = lGrid3 + zs * P1;
+                /* the reference's visits, as runs of whole cells: columns
+                 * pLow..pHigh-1, or with wrap-around pLow..P then 0..pHigh-1 */
+                for (int run = 0; run < 2; ++run) {
+                    const uint32_t c0 = run == 0 ? w.phiLowSector : 0u;
+                    const uint32_t c1 = run == 0 ? (w.wrap ? P1 : w.phiHighSector)
+                                                 : (w.wrap ? w.phiHighSector : 0u);
+                    if (c1 <= c0) continue;
+                    const uint32_t ra = row[c0], rb = row[c1];
+                    if (rb - ra <= kp.run_walk) {
+                        /* a small run: walk its contiguous hits */
+                        for (uint32_t j = ra; j < rb; ++j) {
+                            const float zz = Z[j];
+                            const bool ph = phi_in(PHI[j], w.phiLow, w.phiHigh, w.wrap);
+                            cA += (inA && ph && w.zLow[0] <= zz && zz <= w.zHigh[0]) ? 1u : 0u;
+                            cB += (inB && ph && w.zLow[1] <= zz && zz <= w.zHigh[1]) ? 1u : 0u;
+                        }
+                        continue;
+                    }
+                    for (uint32_t c = c0; c < c1; ++c) {
+                        const uint32_t ca = row[c], cb = row[c + 1];
+                        if (cb - ca <= kp.zi_min || cb - ca > kZiMax) {
+                            for (uint32_t j = ca; j < cb; ++j) {
+                                const float zz = Z[j];
+                                const bool ph = phi_in(PHI[j], w.phiLow, w.phiHigh, w.wrap);
+                                cA += (inA && ph && w.zLow[0] <= zz && zz <= w.zHigh[0]) ? 1u : 0u;
+                                cB += (inB && ph && w.zLow[1] <= zz && zz <= w.zHigh[1]) ? 1u : 0u;
+                            }
+                            continue;
+                        }
+                        uint32_t lo = ca, hi = cb;
+                        while (lo < hi) {
+                            const uint32_t m = (lo + hi) >> 1;
+                            if (zkey(zi[m].x) < keyLo) lo = m + 1; else hi = m;
+                        }
+                        for (; lo < cb; ++lo) {
+                            const float2 v = zi[lo];
+                            if (zkey(v.x) > keyHi) break;
+                            const bool ph = phi_in(v.y, w.phiLow, w.phiHigh, w.wrap);
+                            cA += (inA && ph && w.zLow[0] <= v.x && v.x <= w.zHigh[0]) ? 1u : 0u;
+                            cB += (inB && ph && w.zLow[1] <= v.x && v.x <= w.zHigh[1]) ? 1u : 0u;
+                        }
+                    }
                 }
             }
             emitted = cA < cB ? cA : cB;
@@ -964,18 +1078,55 @@ __global__ void __launch_bounds__(256) k_predict_fused(
             st->n_cands = tile_end;
         }
         if (emitted) {
+            /* the first `emitted` accepts of window B in the reference's
+             * visit order: cells in run order, hits of a cell by position;
+             * the index only tells which cells hold accepts */
             uint32_t written = 0;
+            const uint32_t kB0 = zkey(w.zLow[1]), kB1 = zkey(w.zHigh[1]);
             for (uint32_t zs = w.zLowSector[1]; zs < w.zHighSector[1] && written < emitted; ++zs) {
-                uint32_t j, end2, rowEnd, len;
-                pred_row(lGrid3, P1, zs, w.phiLowSector, w.phiHighSector, w.wrap, j, end2,
-                         rowEnd, len);
-                for (; j < end2 && written < emitted; ++j) {
-                    const uint32_t idx = j - (j >= rowEnd ? len : 0u);
-                    const float zz = Z[idx];
-                    if (w.zLow[1] <= zz && zz <= w.zHigh[1] &&
-                        phi_in(PHI[idx], w.phiLow, w.phiHigh, w.wrap)) {
-                        if (pos + written < cand_cap) cands[pos + written] = make_uint2(p, idx);
-                        ++written;
+                const uint32_t *row = lGrid3 + zs * P1;
+                for (int run = 0; run < 2 && written < emitted; ++run) {
+                    const uint32_t c0 = run == 0 ? w.phiLowSector : 0u;
+                    const uint32_t c1 = run == 0 ? (w.wrap ? P1 : w.phiHighSector)
+                                                 : (w.wrap ? w.phiHighSector : 0u);
+                    if (c1 <= c0) continue;
+                    const uint32_t ra = row[c0], rb = row[c1];
+                    if (rb - ra <= kp.run_walk) {
+                        for (uint32_t j = ra; j < rb && written < emitted; ++j) {
+                            const float zz = Z[j];
+                            if (w.zLow[1] <= zz && zz <= w.zHigh[1] &&
+                                phi_in(PHI[j], w.phiLow, w.phiHigh, w.wrap)) {
+                                if (pos + written < cand_cap) cands[pos + written] = make_uint2(p, j);
+                                ++written;
+                            }
+                        }
+                        continue;
+                    }
+                    for (uint32_t c = c0; c < c1 && written < emitted; ++c) {
+                        const uint32_t ca = row[c], cb = row[c + 1];
+                        if (cb - ca > kp.zi_min && cb - ca <= kZiMax) {
+                            uint32_t lo = ca, hi = cb;
+                            while (lo < hi) {
+                                const uint32_t m = (lo + hi) >> 1;
+                                if (zkey(zi[m].x) < kB0) lo = m + 1; else hi = m;
+                            }
+                            bool any = false;
+                            for (; lo < cb && !any; ++lo) {
+                                const float2 v = zi[lo];
+                                if (zkey(v.x) > kB1) break;
+                                any = w.zLow[1] <= v.x && v.x <= w.zHigh[1] &&
+                                      phi_in(v.y, w.phiLow, w.phiHigh, w.wrap);
+                            }
+                            if (!any) continue;
+                        }
+                        for (uint32_t j = ca; j < cb && written < emitted; ++j) {
+                            const float zz = Z[j];
+                            if (w.zLow[1] <= zz && zz <= w.zHigh[1] &&
+                                phi_in(PHI[j], w.phiLow, w.phiHigh, w.wrap)) {
+                                if (pos + written < cand_cap) cands[pos + written] = make_uint2(p, j);
+                                ++written;
+                            }
+                        }
                     }
                 }
             }

@@ -37,6 +37,8 @@ _SIGS = {
     "trax_ctx_sm_count": (C.c_int, [C.c_void_p]),
     "trax_configure": (C.c_int, [C.c_void_p, C.POINTER(A.TraxConfig)]),
     "trax_min_radius_curvature": (C.c_float, [C.c_float, C.c_float]),
+    "trax_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(A.TraxTuning)]),
+    "trax_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(A.TraxTuning)]),
     "trax_dev_alloc": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_size_t]),
     "trax_dev_free": (C.c_int, [C.c_void_p, C.c_void_p]),
     "trax_host_alloc_pinned": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_size_t]),
@@ -232,6 +234,14 @@ class Context:
         self._check(self.lib.trax_configure(self.h, C.byref(cfg)))
         self.config = cfg
         return self
+
+    def set_tuning(self, run_walk: int, index_min: int):
+        self._check(self.lib.trax_set_tuning(self.h, C.byref(A.TraxTuning(run_walk, index_min))))
+
+    def get_tuning(self):
+        t = A.TraxTuning()
+        self._check(self.lib.trax_get_tuning(self.h, C.byref(t)))
+        return int(t.run_walk), int(t.index_min)
 
     def alloc(self, n, dtype=np.uint32) -> DeviceBuffer:
         return DeviceBuffer(self, int(n) * np.dtype(dtype).itemsize, dtype)
