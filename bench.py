@@ -98,6 +98,18 @@ class Dist:
             self.td.destroy_process_group()
 
 
+def replica_first_event(rank: int, events_per_rank: int) -> int:
+    """Replicas only: rank r seeds events [r*B, (r+1)*B) of the workload."""
+    return rank * events_per_rank
+
+
+def aggregate_rate(dist: "Dist", events_this_rank: int, steps: int, ms_this_rank: float):
+    """Whole-job rate: events of all ranks over the slowest rank's time."""
+    ms = dist.max(ms_this_rank)
+    events = dist.sum(events_this_rank)
+    return events * steps / (ms / 1000.0), ms, events
+
+
 # --------------------------------------------------------------------------
 # clocks sampled during the timed region
 
@@ -381,7 +393,7 @@ def run_ours(args, dist):
     w = gen.WORKLOADS[args.workload]
     ctx = Context(dist.local)
     B = args.events
-    b = gen.generate_batch(w, B, first_event=dist.rank * B)
+    b = gen.generate_batch(w, B, first_event=replica_first_event(dist.rank, B))
     cfg, grid = w.config(), w.grid(B)
     N = b.n_hits
     caps = [12 * N + 4096, 12 * N + 4096, 2 * N + 4096]
@@ -415,14 +427,12 @@ def run_ours(args, dist):
         ctx.timer_record(63)
         ctx.synchronize()
     dist.barrier()
-    ms_total = ctx.timer_elapsed_ms(62, 63)
-    ms_total = dist.max(ms_total)
+    value, ms_total, events_all = aggregate_rate(dist, B, args.steps,
+                                                 ctx.timer_elapsed_ms(62, 63))
     launches = int(ctx.lib.trax_kernel_launches(ctx.h))
     counts = ctx.counts()
     if counts["status"] != 0:
         raise SystemExit(f"device status after timed run {counts}")
-    events_all = dist.sum(B)
-    value = events_all * args.steps / (ms_total / 1000.0)
 
     # ---- per-kernel times (separate profiled run) ------------------------
     ctx._check(ctx.lib.trax_set_profiling(ctx.h, 1))
