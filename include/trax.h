@@ -278,6 +278,22 @@ trax_status trax_prefix_sum_noalloc(const uint32_t *d_in, uint32_t *d_out, uint3
                                     uint32_t *d_total, void *stream);
 const char *trax_prefix_sum_noalloc_error(void);
 
+/* TripletConnectivity::run (src/algorithms/TripletConnectivity.h:52-54,
+ * .cpp:21-71): following_con[f] += sum over base tracklets b that chain
+ * with f of (base_con[b] + 1).  Wide packing shares one hit (forward: base
+ * hit3 == follow hit1; iterate_backwards: base hit1 == follow hit3); tight
+ * packing shares two (base hit2, hit3 == follow hit1, hit2; forward only).
+ * The semantics are those the reference's own tests pin
+ * (src/algorithms/test/TripletConnectivityTest.h:147-259); its wide kernel
+ * as written swaps the base and following indices (TripletConnectivity.h:71-73)
+ * and would fail its multilayer test.  base_con may be NULL (all zero).
+ * Device pointers; asynchronous. */
+trax_status trax_triplet_connectivity(trax_ctx *ctx, const trax_tracklets *base,
+                                      uint32_t n_base, const uint32_t *base_con,
+                                      const trax_tracklets *following, uint32_t n_following,
+                                      uint32_t *following_con, int iterate_backwards,
+                                      int tight_packing);
+
 trax_status trax_read_counts(trax_ctx *ctx, trax_counts *out);  /* synchronises */
 
 /* Diagnostic: evaluates the path's FP32 math on the device for n inputs

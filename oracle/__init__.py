@@ -60,6 +60,12 @@ def lib():
                 getattr(L, f).argtypes = [C.c_float]
             L.or_math_batch.restype = None
             L.or_math_batch.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64]
+            L.or_connectivity.restype = None
+            L.or_connectivity.argtypes = [C.c_void_p] * 4 + [C.c_uint32] + [C.c_void_p] * 4 + \
+                [C.c_uint32, C.c_int, C.c_int]
+            L.or_connectivity_literal_wide.restype = None
+            L.or_connectivity_literal_wide.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32,
+                                                       C.c_void_p, C.c_void_p, C.c_uint32]
             L.or_min_radius_curvature.restype = C.c_float
             L.or_min_radius_curvature.argtypes = [C.c_float, C.c_float]
             _lib = L
@@ -126,3 +132,27 @@ def canonical(res):
         if cands.size else np.zeros((0, 3), np.uint32)
     trk = np.stack([res["trk_h1"], res["trk_h2"], res["trk_h3"]], axis=1)
     return {"pairs": pairs, "cand_hits": trip, "tracklets": trk}
+
+
+def connectivity(base, base_con, follow, follow_con, iterate_backwards=False,
+                 tight_packing=False):
+    """base/follow: (n, 3) hit rows; returns the updated following connectivity."""
+    b = np.ascontiguousarray(base, dtype=np.uint32).reshape(-1, 3)
+    f = np.ascontiguousarray(follow, dtype=np.uint32).reshape(-1, 3)
+    bc = np.ascontiguousarray(base_con, dtype=np.uint32)
+    fc = np.ascontiguousarray(follow_con, dtype=np.uint32).copy()
+    cols = [np.ascontiguousarray(b[:, i]) for i in range(3)] + \
+        [np.ascontiguousarray(f[:, i]) for i in range(3)]
+    lib().or_connectivity(_ptr(cols[0]), _ptr(cols[1]), _ptr(cols[2]), _ptr(bc), len(b),
+                          _ptr(cols[3]), _ptr(cols[4]), _ptr(cols[5]), _ptr(fc), len(f),
+                          int(iterate_backwards), int(tight_packing))
+    return fc
+
+
+def connectivity_literal_wide(base_hit, base_con, follow_hit, follow_con):
+    bh = np.ascontiguousarray(base_hit, dtype=np.uint32)
+    bc = np.ascontiguousarray(base_con, dtype=np.uint32)
+    fh = np.ascontiguousarray(follow_hit, dtype=np.uint32)
+    fc = np.ascontiguousarray(follow_con, dtype=np.uint32).copy()
+    lib().or_connectivity_literal_wide(_ptr(bh), _ptr(bc), len(bh), _ptr(fh), _ptr(fc), len(fh))
+    return fc

@@ -769,6 +769,41 @@ static void filter_stage(or_result *r, const trax_config *cfg, const trax_grid_c
     r->stats[ORS_TRACKLETS] = nFound;
 }
 
+/* ------------------------------------------------------------------------
+ * TripletConnectivity (TripletConnectivity.h:56-108, .cpp:21-71).
+ * ---------------------------------------------------------------------- */
+void or_connectivity(const uint32_t *b1, const uint32_t *b2, const uint32_t *b3,
+                     const uint32_t *base_con, uint32_t n_base, const uint32_t *f1,
+                     const uint32_t *f2, const uint32_t *f3, uint32_t *follow_con,
+                     uint32_t n_follow, int iterate_backwards, int tight_packing)
+{
+    for (uint32_t gid = 0; gid < n_follow; ++gid) {
+        for (uint32_t i = 0; i < n_base; ++i) {
+            int connected;
+            if (tight_packing) /* tripletConnectivityTight, :100-101 */
+                connected = b2[i] == f1[gid] && b3[i] == f2[gid];
+            else if (!iterate_backwards)
+                connected = b3[i] == f1[gid];
+            else
+                connected = b1[i] == f3[gid];
+            follow_con[gid] += (uint32_t)connected * ((base_con ? base_con[i] : 0u) + 1u);
+        }
+    }
+}
+
+void or_connectivity_literal_wide(const uint32_t *base_hit, const uint32_t *base_con,
+                                  uint32_t n_base, const uint32_t *follow_hit,
+                                  uint32_t *follow_con, uint32_t n_follow)
+{
+    /* :67-75; base_hit is read at the following index, so n_follow must not
+     * exceed n_base (the reference reads past the base buffer otherwise) */
+    for (uint32_t gid = 0; gid < n_follow && gid < n_base; ++gid)
+        for (uint32_t i = 0; i < n_base; ++i) {
+            const int connected = base_hit[gid] == follow_hit[i];
+            follow_con[gid] += (uint32_t)connected * (base_con[i] + 1u);
+        }
+}
+
 or_result *or_run(const trax_config *cfg, const trax_grid_cfg *grid, const float *x, const float *y,
                   const float *z, const uint32_t *layer, const uint32_t *det, const uint32_t *hitid,
                   const uint32_t *event, uint32_t n_hits, const uint32_t *event_offset,

@@ -77,6 +77,19 @@ void or_free(or_result *r);
  * in-place exclusive scan by recursive work-group scans. */
 void or_prefix_sum(uint32_t *data, uint32_t n, uint32_t wg);
 
+/* TripletConnectivity::run (TripletConnectivity.cpp:21-71) with the
+ * semantics its tests pin (TripletConnectivityTest.h:147-259):
+ * follow_con[f] += sum_b [key(b) == key(f)] * (base_con[b] + 1).
+ * or_connectivity_literal_wide restates the wide kernel exactly as written
+ * (TripletConnectivity.h:67-75: base indexed by the following id). */
+void or_connectivity(const uint32_t *b1, const uint32_t *b2, const uint32_t *b3,
+                     const uint32_t *base_con, uint32_t n_base, const uint32_t *f1,
+                     const uint32_t *f2, const uint32_t *f3, uint32_t *follow_con,
+                     uint32_t n_follow, int iterate_backwards, int tight_packing);
+void or_connectivity_literal_wide(const uint32_t *base_hit, const uint32_t *base_con,
+                                  uint32_t n_base, const uint32_t *follow_hit,
+                                  uint32_t *follow_con, uint32_t n_follow);
+
 /* Project math, exported so tests can compare against libm / CUDA. */
 float or_atan2f(float y, float x);
 float or_acosf(float x);

@@ -8,6 +8,7 @@ from ._abi import (TraxConfig, TraxGridCfg, TraxLayerTriplet, make_config)  # no
 from .runtime import Context, TraxError, load_library, LIB_PATH, EXPORTED_SYMBOLS  # noqa: F401
 from .ops import (EventSupplement, LayerSupplement, HitCollection, Grid, Pairing,  # noqa: F401
                   TrackletCollection, GridBuilder, PairGeneratorBeamspot,
-                  TripletThetaPhiPredictor, TripletThetaPhiFilter, Pipeline, build_triplets,
+                  TripletThetaPhiPredictor, TripletThetaPhiFilter, TripletConnectivity,
+                  Pipeline, build_triplets,
                   supplements)
 from . import gen  # noqa: F401

@@ -56,7 +56,7 @@ struct trax_ctx {
     uint32_t *h_stage = nullptr;          /* pinned staging for small uploads */
     size_t h_stage_words = 0;
     cudaEvent_t stage_free = nullptr;     /* last upload from h_stage done */
-    DevBuf seg, g_start, g_base, slots, pexcl, cexcl, st0, st1, st2, st3, zi;
+    DevBuf seg, g_start, g_base, slots, pexcl, cexcl, st0, st1, st2, st3, zi, conn_keys, conn_sums;
     cudaEvent_t timers[kTimerSlots] = {};
     int blk_pair = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
 
@@ -586,7 +586,8 @@ void trax_ctx_destroy(trax_ctx *ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
     DevBuf *bufs[] = {&ctx->seg, &ctx->g_start, &ctx->g_base, &ctx->slots, &ctx->pexcl,
-                      &ctx->cexcl, &ctx->st0, &ctx->st1, &ctx->st2, &ctx->st3, &ctx->zi, &ctx->grid_buf,
+                      &ctx->cexcl, &ctx->st0, &ctx->st1, &ctx->st2, &ctx->st3, &ctx->zi,
+                      &ctx->conn_keys, &ctx->conn_sums, &ctx->grid_buf,
                       &ctx->pairs_buf, &ctx->pair_off, &ctx->cands_buf, &ctx->cand_off, &ctx->trk_off,
                       &ctx->r_seg};
     for (DevBuf *b : bufs) if (b->p) cudaFree(b->p);
@@ -841,6 +842,48 @@ trax_status trax_prefix_sum_noalloc(const uint32_t *d_in, uint32_t *d_out, uint3
 }
 
 const char *trax_prefix_sum_noalloc_error(void) { return g_noalloc_error.c_str(); }
+
+trax_status trax_triplet_connectivity(trax_ctx *ctx, const trax_tracklets *base,
+                                      uint32_t n_base, const uint32_t *base_con,
+                                      const trax_tracklets *following, uint32_t n_following,
+                                      uint32_t *following_con, int iterate_backwards,
+                                      int tight_packing)
+{
+    if (!ctx || !base || !following || (n_following && !following_con)) return TRAX_ERR_BAD_ARG;
+    if (tight_packing && iterate_backwards)
+        return fail(ctx, TRAX_ERR_BAD_ARG, "tight packing runs forward only (TripletConnectivity.cpp:56)");
+    if (n_base == 0 || n_following == 0) return TRAX_OK;
+    /* keys: wide forward base hit3 / follow hit1; backward base hit1 /
+     * follow hit3; tight (base hit2, hit3) / (follow hit1, hit2) */
+    const uint32_t *ba, *bb = nullptr, *fa, *fb = nullptr;
+    if (tight_packing) {
+        ba = base->hit2; bb = base->hit3; fa = following->hit1; fb = following->hit2;
+    } else if (!iterate_backwards) {
+        ba = base->hit3; fa = following->hit1;
+    } else {
+        ba = base->hit1; fa = following->hit3;
+    }
+    uint32_t cap = 1024;
+    while (cap < 2ull * n_base) cap <<= 1;
+    trax_status s;
+    if ((s = ensure(ctx, ctx->conn_keys, (size_t)cap * 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->conn_sums, (size_t)cap * 4)) != TRAX_OK) return s;
+    CK(cudaMemsetAsync(ctx->conn_keys.p, 0xff, (size_t)cap * 8, ctx->stream));
+    CK(cudaMemsetAsync(ctx->conn_sums.p, 0, (size_t)cap * 4, ctx->stream));
+    const uint32_t blocks = std::max(1u, std::min((n_base + 255) / 256, (uint32_t)ctx->blk_small * 4));
+    k_conn_build<<<blocks, 256, 0, ctx->stream>>>(ba, bb, base_con, n_base,
+                                                  (unsigned long long *)ctx->conn_keys.p,
+                                                  (uint32_t *)ctx->conn_sums.p, cap - 1,
+                                                  ctx->d_state);
+    const uint32_t fblocks =
+        std::max(1u, std::min((n_following + 255) / 256, (uint32_t)ctx->blk_small * 4));
+    k_conn_probe<<<fblocks, 256, 0, ctx->stream>>>(fa, fb, n_following,
+                                                   (const unsigned long long *)ctx->conn_keys.p,
+                                                   (const uint32_t *)ctx->conn_sums.p, cap - 1,
+                                                   following_con);
+    CK(cudaGetLastError());
+    return TRAX_OK;
+}
 
 trax_status trax_read_counts(trax_ctx *ctx, trax_counts *out)
 {

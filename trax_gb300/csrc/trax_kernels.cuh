@@ -1308,4 +1308,65 @@ __global__ void __launch_bounds__(1024) k_monotonize(uint32_t *offsets, uint32_t
     }
 }
 
+/* ------------------------------------------------------------------------
+ * TripletConnectivity (src/algorithms/TripletConnectivity.h:56-108): each
+ * following tracklet gains sum(base connectivity + 1) over the base
+ * tracklets it chains with -- wide: one shared hit (base hit3 == follow
+ * hit1, or base hit1 == follow hit3 backwards), tight: two (base hit2, hit3
+ * == follow hit1, hit2).  A hash join instead of the reference's
+ * all-pairs loop: base keys accumulate their weights in an open-addressing
+ * table, then every following tracklet probes its key once.  Probes are
+ * bounded by the table size (it is never full: capacity >= 2 * n_base).
+ * ---------------------------------------------------------------------- */
+constexpr unsigned long long kEmptyKey = 0xffffffffffffffffull;
+
+__device__ __forceinline__ uint32_t conn_hash(unsigned long long k, uint32_t mask)
+{
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return (uint32_t)k & mask;
+}
+
+__global__ void k_conn_build(const uint32_t *ka, const uint32_t *kb, const uint32_t *con,
+                             uint32_t n, unsigned long long *keys, uint32_t *sums, uint32_t mask,
+                             DevState *st)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned long long key = kb ? (((unsigned long long)ka[i] << 32) | kb[i]) : ka[i];
+        const uint32_t w = (con ? con[i] : 0u) + 1u;
+        uint32_t h = conn_hash(key, mask);
+        for (uint32_t probe = 0; probe <= mask; ++probe) {
+            const unsigned long long prev = atomicCAS(&keys[h], kEmptyKey, key);
+            if (prev == kEmptyKey || prev == key) {
+                atomicAdd(&sums[h], w);
+                break;
+            }
+            if (probe == mask) set_fault(st, TRAX_ERR_CAPACITY, TRAX_DETAIL_TRACKLET_CAPACITY);
+            h = (h + 1) & mask;
+        }
+    }
+}
+
+__global__ void k_conn_probe(const uint32_t *ka, const uint32_t *kb, uint32_t n,
+                             const unsigned long long *keys, const uint32_t *sums, uint32_t mask,
+                             uint32_t *con)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned long long key = kb ? (((unsigned long long)ka[i] << 32) | kb[i]) : ka[i];
+        uint32_t h = conn_hash(key, mask);
+        for (uint32_t probe = 0; probe <= mask; ++probe) {
+            const unsigned long long k = keys[h];
+            if (k == key) {
+                con[i] += sums[h];
+                break;
+            }
+            if (k == kEmptyKey) break;
+            h = (h + 1) & mask;
+        }
+    }
+}
+
 }  // namespace trax

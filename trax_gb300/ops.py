@@ -146,7 +146,24 @@ class TrackletCollection:
         self.n_groups = int(n_events) * int(n_triplets)
         self.cols = [ctx.alloc(self.capacity) for _ in range(3)]
         self.offsets_buf = ctx.alloc(self.n_groups + 1).zero()
+        self.connectivity = ctx.alloc(self.capacity).zero()  # TrackletConnectivity item
         self.count = None
+
+    @classmethod
+    def from_host(cls, ctx: Context, hits: np.ndarray, connectivity=None):
+        """A collection from host (hit1, hit2, hit3) rows, e.g. test tables."""
+        hits = np.ascontiguousarray(hits, dtype=U32).reshape(-1, 3)
+        t = cls(ctx, max(len(hits), 1), 1, 1)
+        for i in range(3):
+            if len(hits):
+                t.cols[i].upload(hits[:, i])
+        if connectivity is not None and len(hits):
+            t.connectivity.upload(np.asarray(connectivity, dtype=U32))
+        t.count = len(hits)
+        return t
+
+    def get_connectivity(self):
+        return self.connectivity.download(self.count or 0)
 
     def struct(self):
         return A.TraxTracklets(self.cols[0].ptr, self.cols[1].ptr, self.cols[2].ptr,
@@ -265,6 +282,19 @@ class TripletThetaPhiFilter(_Op):
         cap = capacity or max(triplet_candidates.count or 0, 1024)
         return _grow(ctx, cap, lambda n: TrackletCollection(ctx, n, grid.config.n_events, T),
                      run_once)
+
+
+class TripletConnectivity(_Op):
+    """TripletConnectivity::run (TripletConnectivity.h:52-54)."""
+
+    def run(self, tracklets_base: TrackletCollection, tracklets_following: TrackletCollection,
+            iterate_backwards=False, tight_packing=False):
+        ctx = self.ctx
+        b, f = tracklets_base.struct(), tracklets_following.struct()
+        ctx._check(ctx.lib.trax_triplet_connectivity(
+            ctx.h, C.byref(b), tracklets_base.count or 0, tracklets_base.connectivity.ptr,
+            C.byref(f), tracklets_following.count or 0, tracklets_following.connectivity.ptr,
+            1 if iterate_backwards else 0, 1 if tight_packing else 0))
 
 
 def build_triplets(ctx: Context, batch: EventBatch, cfg: A.TraxConfig, n_sectors_z,

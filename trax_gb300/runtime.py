@@ -60,6 +60,9 @@ _SIGS = {
                                       C.POINTER(A.TraxGridCfg), C.POINTER(A.TraxPairs),
                                       C.POINTER(A.TraxPairs), C.POINTER(A.TraxTracklets)]),
     "trax_read_counts": (C.c_int, [C.c_void_p, C.POINTER(A.TraxCounts)]),
+    "trax_triplet_connectivity": (C.c_int, [C.c_void_p, C.POINTER(A.TraxTracklets), C.c_uint32,
+                                            C.c_void_p, C.POINTER(A.TraxTracklets), C.c_uint32,
+                                            C.c_void_p, C.c_int, C.c_int]),
     "trax_prefix_sum": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     "trax_prefix_sum_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                           C.c_void_p]),
