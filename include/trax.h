@@ -205,6 +205,15 @@ typedef struct trax_tuning {
     uint32_t index_min;
 } trax_tuning;
 trax_status trax_set_tuning(trax_ctx *ctx, const trax_tuning *t);
+
+/* Which pair generator the batched pipeline (trax_seed_batch,
+ * trax_run_staged) runs.  The reference's TripletBuilder runs the beam-spot
+ * generator (TripletBuilder.cpp:247-250; the sector one's include is
+ * commented out at :32).  Unlike the tuning, this changes results. */
+#define TRAX_PAIRS_BEAMSPOT 0
+#define TRAX_PAIRS_SECTOR 1
+trax_status trax_set_pair_generator(trax_ctx *ctx, int generator);
+int trax_get_pair_generator(const trax_ctx *ctx);
 trax_status trax_get_tuning(const trax_ctx *ctx, trax_tuning *t);
 
 /* ---- device memory helpers (for hosts without their own CUDA binding) -- */
@@ -237,6 +246,15 @@ trax_status trax_grid_build(trax_ctx *ctx, const trax_hits *in, const trax_layou
  * hit, then inner hit. */
 trax_status trax_pair_gen(trax_ctx *ctx, const trax_sorted_hits *hits, const uint32_t *d_grid,
                           const trax_grid_cfg *grid, trax_pairs *out);
+
+/* PairGeneratorSector::run (PairGeneratorSector.h:38-39, .cpp:5-151): no
+ * cut; every layer2 hit in the cells within pairSpreadZ rows and
+ * pairSpreadPhi columns of the layer1 hit's own cell (with the reference's
+ * unsigned z-underflow and phi wrap arithmetic, PairGeneratorSector.h:96-140).
+ * Writes distinct pairs (inner, outer) ordered by inner hit, then outer hit. */
+trax_status trax_pair_gen_sector(trax_ctx *ctx, const trax_sorted_hits *hits,
+                                 const uint32_t *d_grid, const trax_grid_cfg *grid,
+                                 trax_pairs *out);
 
 /* TripletThetaPhiPredictor::run (TripletThetaPhiPredictor.cpp:10-131):
  * per pair, the theta/phi window on layer3; writes candidates

@@ -46,6 +46,8 @@ def lib():
             L.or_run.restype = C.c_void_p
             L.or_run.argtypes = [C.POINTER(TraxConfig), C.POINTER(TraxGridCfg)] + [C.c_void_p] * 7 + \
                 [C.c_uint32] + [C.c_void_p] * 3 + [C.c_int, C.c_uint32, C.c_int]
+            L.or_run_ex.restype = C.c_void_p
+            L.or_run_ex.argtypes = L.or_run.argtypes + [C.c_int]
             L.or_size.restype = C.c_uint64
             L.or_size.argtypes = [C.c_void_p, C.c_int]
             L.or_data.restype = C.c_void_p
@@ -91,15 +93,22 @@ def prefix_sum(values, wg):
     return a
 
 
-def run(batch, cfg: TraxConfig, grid: TraxGridCfg, n_stages=4, n_threads=256, omp_threads=1):
-    """Runs the oracle on an EventBatch; returns a dict of numpy arrays."""
+PAIR_GENERATORS = {"beamspot": 0, "sector": 1}
+
+
+def run(batch, cfg: TraxConfig, grid: TraxGridCfg, n_stages=4, n_threads=256, omp_threads=1,
+        pair_gen="beamspot"):
+    """Runs the oracle on an EventBatch; returns a dict of numpy arrays.
+    pair_gen: "beamspot" (PairGeneratorBeamspot) or "sector"
+    (PairGeneratorSector)."""
     L = lib()
     cols = [np.ascontiguousarray(c) for c in batch.columns()]
     eo = np.ascontiguousarray(batch.event_offset, dtype=np.uint32)
     ln = np.ascontiguousarray(batch.layer_nhits.reshape(-1), dtype=np.uint32)
     lo = np.ascontiguousarray(batch.layer_offset.reshape(-1), dtype=np.uint32)
-    h = L.or_run(C.byref(cfg), C.byref(grid), *[_ptr(c) for c in cols], batch.n_hits,
-                 _ptr(eo), _ptr(ln), _ptr(lo), n_stages, n_threads, omp_threads)
+    h = L.or_run_ex(C.byref(cfg), C.byref(grid), *[_ptr(c) for c in cols], batch.n_hits,
+                    _ptr(eo), _ptr(ln), _ptr(lo), n_stages, n_threads, omp_threads,
+                    PAIR_GENERATORS[pair_gen])
     if not h:
         raise MemoryError("oracle allocation failed")
     out = {}

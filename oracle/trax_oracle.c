@@ -446,6 +446,142 @@ static void pair_stage(or_result *res, const trax_config *cfg, const trax_grid_c
 }
 
 /* ------------------------------------------------------------------------
+ * Stage 2, sector variant: PairGeneratorSector (pairCount
+ * PairGeneratorSector.h:43-147, pairStore :160-230, host
+ * PairGeneratorSector.cpp:5-151).  No cut: every layer-2 hit in the block of
+ * cells around the inner hit's own cell (pairSpreadZ rows, pairSpreadPhi
+ * columns each side) is paired with it.  Threads stride the INNER hits.
+ * ---------------------------------------------------------------------- */
+static void pair_stage_sector(or_result *res, const trax_config *cfg, const trax_grid_cfg *g,
+                              uint32_t nThreads, int omp)
+{
+    const uint32_t E = g->n_events, L = g->n_layers, Z = g->n_sectors_z, P = g->n_sectors_phi;
+    const uint32_t T = cfg->n_layer_triplets;
+    const uint32_t C = (Z + 1) * (P + 1);
+    const float minZ = TRAX_MIN_Z, minPhi = TRAX_MIN_PHI;
+    const float sectorSizeZ = trax_sector_size_z(Z), sectorSizePhi = trax_sector_size_phi(P);
+    const uint32_t *grid = (const uint32_t *)res->data[OR_GRID];
+    const float *hitGlobalY = (const float *)res->data[OR_SORTED_Y];
+    const float *hitGlobalX = (const float *)res->data[OR_SORTED_X];
+    const float *hitGlobalZ = (const float *)res->data[OR_SORTED_Z];
+    const long G = (long)E * T;
+
+    pair_group *pg = (pair_group *)calloc((size_t)(G ? G : 1), sizeof(pair_group));
+    uint32_t *prefixSum = (uint32_t *)calloc((size_t)G * nThreads + 1, 4);
+
+#pragma omp parallel for schedule(dynamic, 1) if (omp)
+    for (long gp = 0; gp < G; ++gp) {
+        const uint32_t event = (uint32_t)(gp / T), layerPair = (uint32_t)(gp % T);
+        const trax_layer_triplet *lt = &cfg->triplets[layerPair];
+        /* :63-67 inner layer range */
+        const uint32_t *lGrid1 = grid + (uint64_t)event * L * C + (uint64_t)(lt->layer1 - 1) * C;
+        const uint32_t layer1Offset = lGrid1[0];
+        const uint32_t end = lGrid1[C - 1];
+        /* :71-80 outer layer */
+        const uint32_t *lGrid2 = grid + (uint64_t)event * L * C + (uint64_t)(lt->layer2 - 1) * C;
+        const uint32_t nHits2 = lGrid2[C - 1] - lGrid2[0];
+        const uint32_t offset = lGrid2[0];
+        const uint32_t spreadZ = lt->pair_spread_z, spreadPhi = lt->pair_spread_phi;
+
+        const uint32_t nHits1 = end - layer1Offset;
+        const uint64_t nbits = (uint64_t)nHits1 * nHits2;
+        pg[gp].bits = (uint32_t *)calloc((size_t)((nbits + 31) / 32 + 1), 4);
+        pg[gp].nHits1 = nHits1; pg[gp].nHits2 = nHits2;
+        pg[gp].offset = layer1Offset; pg[gp].layer2Offset = offset;
+
+        for (uint32_t thread = 0; thread < nThreads; ++thread) {
+            uint32_t nFound = 0;
+            for (uint32_t i = layer1Offset + thread; i < end; i += nThreads) {
+                /* :96-98.  zLowSector is unsigned: max(0u, zLowSector -
+                 * spreadZ) is the plain difference, so an inner hit in a z
+                 * sector below spreadZ wraps to a huge start and visits no
+                 * row. */
+                uint32_t zLowSector = trax_f2u(floorf((hitGlobalZ[i] - minZ) / sectorSizeZ));
+                const uint32_t zh = zLowSector + spreadZ + 1u;
+                const uint32_t zHighSector = zh < Z ? zh : Z;
+                zLowSector = zLowSector - spreadZ;
+                /* :102-110 */
+                const float phi = trax_atan2f(hitGlobalY[i], hitGlobalX[i]);
+                int32_t phiLowSector = trax_f2i(floorf((phi - minPhi) / sectorSizePhi) - (float)spreadPhi);
+                uint32_t phiHighSector = (uint32_t)phiLowSector + 2u * spreadPhi + 1u;
+                const int wrapAround = phiLowSector < 0 || phiHighSector > P + 1;
+                phiLowSector = (int32_t)((uint32_t)phiLowSector + (uint32_t)(phiLowSector < 0) * P);
+                phiHighSector -= (uint32_t)(phiHighSector > P + 1) * P;
+                if (phiLowSector < 0 || (uint32_t)phiLowSector > P + 1 || phiHighSector > P + 1) {
+                    /* only for 2*pairSpreadPhi + 1 > nSectorsPhi: the reference
+                     * reads outside the grid row */
+                    set_fault(res, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_WINDOW_OUTSIDE_GRID);
+                    continue;
+                }
+                /* :114-142 */
+                for (uint32_t zSector = zLowSector; zSector < zHighSector; ++zSector) {
+                    const uint32_t zSectorStart = lGrid2[zSector * (P + 1)];
+                    const uint32_t zSectorEnd = lGrid2[(zSector + 1) * (P + 1) - 1];
+                    const uint32_t zSectorLength = zSectorEnd - zSectorStart;
+                    uint32_t j = lGrid2[zSector * (P + 1) + (uint32_t)phiLowSector];
+                    const uint32_t end2 = (uint32_t)wrapAround * zSectorEnd
+                                        + lGrid2[zSector * (P + 1) + phiHighSector]
+                                        - (uint32_t)wrapAround * zSectorStart;
+                    for (; j < end2; ++j) {
+                        ++nFound;
+                        const uint32_t hit2 = j - (uint32_t)(j >= zSectorEnd) * zSectorLength - offset;
+                        if (hit2 >= nHits2) { /* not reachable from a valid grid */
+                            set_fault(res, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_WINDOW_OUTSIDE_GRID);
+                            continue;
+                        }
+                        const uint64_t index = (uint64_t)(i - layer1Offset) * nHits2 + hit2;
+                        pg[gp].bits[index / 32] |= (1u << (index % 32));
+                    }
+                }
+            }
+            prefixSum[(uint64_t)event * T * nThreads + (uint64_t)layerPair * nThreads + thread] = nFound;
+        }
+    }
+
+    /* PairGeneratorSector.cpp:91-94 */
+    or_prefix_sum(prefixSum, (uint32_t)((uint64_t)G * nThreads + 1), nThreads);
+    const uint32_t nFoundPairs = prefixSum[(uint64_t)G * nThreads];
+
+    u2 *pairs = (u2 *)alloc_item(res, OR_PAIRS, (uint64_t)nFoundPairs * 2, 4);
+    uint8_t *valid_slot = (uint8_t *)alloc_item(res, OR_PAIR_VALID, nFoundPairs, 1);
+    uint32_t *pairOffsets = (uint32_t *)alloc_item(res, OR_PAIR_OFFSETS, (uint64_t)G + 1, 4);
+    uint64_t written_total = 0;
+
+    /* pairStore (:176-229): per thread, its inner hits in stride order and
+     * every outer hit in sorted order, while slots remain. */
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : written_total) if (omp)
+    for (long gp = 0; gp < G; ++gp) {
+        const uint32_t event = (uint32_t)(gp / T), layerPair = (uint32_t)(gp % T);
+        const pair_group *q = &pg[gp];
+        const uint32_t end = q->offset + q->nHits1;
+        for (uint32_t thread = 0; thread < nThreads; ++thread) {
+            const uint64_t slot = (uint64_t)event * T * nThreads + (uint64_t)layerPair * nThreads + thread;
+            uint32_t pos = prefixSum[slot];
+            const uint32_t nextThread = prefixSum[slot + 1];
+            for (uint32_t i = q->offset + thread; i < end; i += nThreads) {
+                for (uint32_t j = 0; j < q->nHits2 && pos < nextThread; ++j) {
+                    const uint64_t index = (uint64_t)(i - q->offset) * q->nHits2 + j;
+                    const int valid = (q->bits[index / 32] & (1u << (index % 32))) != 0;
+                    if (valid) {
+                        pairs[pos].x = i;
+                        pairs[pos].y = q->layer2Offset + j;
+                        valid_slot[pos] = 1;
+                        written_total += 1;
+                    }
+                    pos += valid;
+                }
+            }
+            if (thread == nThreads - 1) pairOffsets[(uint64_t)event * T + layerPair + 1] = nextThread;
+        }
+    }
+    for (long gp = 0; gp < G; ++gp) free(pg[gp].bits);
+    free(pg);
+    free(prefixSum);
+    res->stats[ORS_PAIR_SLOTS] = nFoundPairs;
+    res->stats[ORS_PAIRS] = written_total;
+}
+
+/* ------------------------------------------------------------------------
  * Stage 3: TripletThetaPhiPredictor (predictCount :46-248, predictStore
  * :250-481, predictOffsetMonotonizeStore :483-497; host .cpp:10-131).
  * ---------------------------------------------------------------------- */
@@ -810,6 +946,18 @@ or_result *or_run(const trax_config *cfg, const trax_grid_cfg *grid, const float
                   const uint32_t *layer_nhits, const uint32_t *layer_offset, int n_stages,
                   uint32_t n_threads, int n_omp_threads)
 {
+    return or_run_ex(cfg, grid, x, y, z, layer, det, hitid, event, n_hits, event_offset,
+                     layer_nhits, layer_offset, n_stages, n_threads, n_omp_threads,
+                     OR_PAIRS_BEAMSPOT);
+}
+
+or_result *or_run_ex(const trax_config *cfg, const trax_grid_cfg *grid, const float *x,
+                     const float *y, const float *z, const uint32_t *layer, const uint32_t *det,
+                     const uint32_t *hitid, const uint32_t *event, uint32_t n_hits,
+                     const uint32_t *event_offset, const uint32_t *layer_nhits,
+                     const uint32_t *layer_offset, int n_stages, uint32_t n_threads,
+                     int n_omp_threads, int pair_generator)
+{
     or_result *r = (or_result *)calloc(1, sizeof(or_result));
     if (!r) return NULL;
     if (n_threads == 0) n_threads = 256;
@@ -822,7 +970,12 @@ or_result *or_run(const trax_config *cfg, const trax_grid_cfg *grid, const float
     const float rmin = or_min_radius_curvature(cfg->min_pt, cfg->bz);
     grid_stage(r, grid, x, y, z, layer, det, hitid, event, n_hits, event_offset, layer_nhits,
                layer_offset, n_threads, omp);
-    if (n_stages >= 2) pair_stage(r, cfg, grid, rmin, n_threads, omp);
+    if (n_stages >= 2) {
+        if (pair_generator == OR_PAIRS_SECTOR)
+            pair_stage_sector(r, cfg, grid, n_threads, omp);
+        else
+            pair_stage(r, cfg, grid, rmin, n_threads, omp);
+    }
     if (n_stages >= 3) predict_stage(r, cfg, grid, rmin, n_threads, omp);
     if (n_stages >= 4) filter_stage(r, cfg, grid, rmin, n_threads, omp);
     r->size[OR_STATS] = OR_NSTATS;

@@ -69,6 +69,17 @@ or_result *or_run(const trax_config *cfg, const trax_grid_cfg *grid,
                   const uint32_t *event_offset, const uint32_t *layer_nhits,
                   const uint32_t *layer_offset, int n_stages, uint32_t n_threads,
                   int n_omp_threads);
+/* or_run with a choice of pair generator: OR_PAIRS_BEAMSPOT
+ * (PairGeneratorBeamspot, the one the reference's TripletBuilder runs) or
+ * OR_PAIRS_SECTOR (PairGeneratorSector). */
+enum { OR_PAIRS_BEAMSPOT = 0, OR_PAIRS_SECTOR = 1 };
+or_result *or_run_ex(const trax_config *cfg, const trax_grid_cfg *grid,
+                     const float *x, const float *y, const float *z,
+                     const uint32_t *layer, const uint32_t *det, const uint32_t *hitid,
+                     const uint32_t *event, uint32_t n_hits,
+                     const uint32_t *event_offset, const uint32_t *layer_nhits,
+                     const uint32_t *layer_offset, int n_stages, uint32_t n_threads,
+                     int n_omp_threads, int pair_generator);
 uint64_t or_size(const or_result *r, int item);  /* elements */
 const void *or_data(const or_result *r, int item);
 void or_free(or_result *r);

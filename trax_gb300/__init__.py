@@ -7,7 +7,7 @@ reference-shaped operator classes; there is no CPU fallback.
 from ._abi import (TraxConfig, TraxGridCfg, TraxLayerTriplet, make_config)  # noqa: F401
 from .runtime import Context, TraxError, load_library, LIB_PATH, EXPORTED_SYMBOLS  # noqa: F401
 from .ops import (EventSupplement, LayerSupplement, HitCollection, Grid, Pairing,  # noqa: F401
-                  TrackletCollection, GridBuilder, PairGeneratorBeamspot,
+                  TrackletCollection, GridBuilder, PairGeneratorBeamspot, PairGeneratorSector,
                   TripletThetaPhiPredictor, TripletThetaPhiFilter, TripletConnectivity,
                   Pipeline, build_triplets,
                   supplements)

@@ -7,6 +7,7 @@ MAX_LAYER_TRIPLETS = 16
 MAX_LAYERS = 16
 
 TRAX_OK = 0
+PAIR_GENERATORS = {"beamspot": 0, "sector": 1}
 STATUS_NAMES = {
     0: "TRAX_OK", 1: "TRAX_ERR_BAD_ARG", 2: "TRAX_ERR_OOM", 3: "TRAX_ERR_TIMEOUT",
     4: "TRAX_ERR_DEVICE", 5: "TRAX_ERR_CAPACITY", 6: "TRAX_ERR_BAD_INPUT",

@@ -49,6 +49,7 @@ struct trax_ctx {
     cudaStream_t stream = nullptr;
     std::string err;
     bool configured = false;
+    int pair_generator = TRAX_PAIRS_BEAMSPOT;  /* used by the batched pipeline */
     trax_config cfg{};
     KParams kp{};
     DevState *d_state = nullptr;
@@ -58,7 +59,7 @@ struct trax_ctx {
     cudaEvent_t stage_free = nullptr;     /* last upload from h_stage done */
     DevBuf seg, g_start, g_base, slots, pexcl, cexcl, st0, st1, st2, st3, zi, conn_keys, conn_sums;
     cudaEvent_t timers[kTimerSlots] = {};
-    int blk_pair = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
+    int blk_pair = 0, blk_sector = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
 
     /* batched pipeline */
     bool reserved = false;
@@ -140,9 +141,11 @@ void fill_grid_params(KParams &kp, const trax_grid_cfg *g)
     kp.sz_phi = trax_sector_size_phi(g->n_sectors_phi);
 }
 
-trax_status check_grid(trax_ctx *ctx, const trax_grid_cfg *g)
+/* The grid build needs no layer-triplet configuration (GridBuilder::run
+ * takes none, GridBuilder.h:42); the later stages do. */
+trax_status check_grid(trax_ctx *ctx, const trax_grid_cfg *g, bool need_cfg = true)
 {
-    if (!ctx->configured) return fail(ctx, TRAX_ERR_BAD_ARG, "trax_configure not called");
+    if (need_cfg && !ctx->configured) return fail(ctx, TRAX_ERR_BAD_ARG, "trax_configure not called");
     if (!g || g->n_sectors_z == 0 || g->n_sectors_phi == 0 || g->n_layers == 0 ||
         g->n_layers > TRAX_MAX_LAYERS)
         return fail(ctx, TRAX_ERR_BAD_ARG, "bad grid configuration");
@@ -240,10 +243,14 @@ trax_status enqueue_grid(trax_ctx *ctx, const InCols &in, const SortedCols &out,
     return mark(ctx, "grid_build");
 }
 
+/* Pair stage with either generator: TRAX_PAIRS_BEAMSPOT (items are the
+ * outer hits, k_pair_fused) or TRAX_PAIRS_SECTOR (items are the inner hits,
+ * k_pair_sector).  Both write pairs (inner, outer) and per-group offsets. */
 trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *grid, uint2 *pairs,
                           uint32_t *pair_offsets, uint32_t pair_cap, uint32_t slot_cap,
-                          uint32_t max_groups)
+                          uint32_t max_groups, int generator)
 {
+    const bool sector = generator == TRAX_PAIRS_SECTOR;
     const KParams &kp = ctx->kp;
     trax_status s;
     if ((s = ensure(ctx, ctx->g_start, (size_t)max_groups * 4)) != TRAX_OK) return s;
@@ -257,15 +264,20 @@ trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *gr
     uint32_t *pexcl = (uint32_t *)ctx->pexcl.p;
     DevState *st = ctx->d_state;
 
-    k_pair_groups<<<1, 1024, 0, ctx->stream>>>(kp, grid, g_start, g_base, st);
+    k_pair_groups<<<1, 1024, 0, ctx->stream>>>(kp, grid, g_start, g_base, st, sector);
     if ((s = mark(ctx, "pair_groups")) != TRAX_OK) return s;
     k_pair_slots<<<ctx->blk_small, 256, 0, ctx->stream>>>(kp, g_start, g_base, slots, slot_cap, st);
     if ((s = mark(ctx, "pair_slots")) != TRAX_OK) return s;
     CK(cudaMemsetAsync(&st->tile_ctr[0], 0, 4, ctx->stream));
     CK(cudaMemsetAsync(ctx->st0.p, 0, (size_t)ntile * 8, ctx->stream));
-    k_pair_fused<<<ctx->blk_pair, kFusedThreads, 0, ctx->stream>>>(
-        kp, grid, h.x, h.y, h.z, h.phi, slots, slot_cap, pexcl, pairs, pair_cap,
-        (unsigned long long *)ctx->st0.p, st);
+    if (sector)
+        k_pair_sector<<<ctx->blk_sector, kFusedThreads, 0, ctx->stream>>>(
+            kp, grid, h.z, h.phi, slots, slot_cap, pexcl, pairs, pair_cap,
+            (unsigned long long *)ctx->st0.p, st);
+    else
+        k_pair_fused<<<ctx->blk_pair, kFusedThreads, 0, ctx->stream>>>(
+            kp, grid, h.x, h.y, h.z, h.phi, slots, slot_cap, pexcl, pairs, pair_cap,
+            (unsigned long long *)ctx->st0.p, st);
     if ((s = mark(ctx, "pair_gen")) != TRAX_OK) return s;
     k_group_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(g_base, pexcl, pair_offsets, kp.n_lt,
                                                              slot_cap, &st->n_pairs, pair_cap,
@@ -567,6 +579,8 @@ trax_status trax_ctx_create(trax_ctx **out, int device)
     int b = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_fused, kFusedThreads, 0);
     ctx->blk_pair = ctx->sm_count * std::max(b, 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_sector, kFusedThreads, 0);
+    ctx->blk_sector = ctx->sm_count * std::max(b, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_predict_fused, kFusedThreads, 0);
     ctx->blk_pred = ctx->sm_count * std::max(b, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_filter, 256, 0);
@@ -649,6 +663,7 @@ trax_status trax_configure(trax_ctx *ctx, const trax_config *cfg)
         kp.l1[i] = t.layer1; kp.l2[i] = t.layer2; kp.l3[i] = t.layer3;
         kp.dtheta[i] = t.dtheta_cut; kp.sigma_z[i] = t.sigma_z; kp.dphi[i] = t.dphi_cut;
         kp.sigma_phi[i] = t.sigma_phi; kp.tip[i] = t.tip_cut; kp.z0[i] = t.z0;
+        kp.spread_z[i] = t.pair_spread_z;
         kp.spread_phi[i] = t.pair_spread_phi;
     }
     for (uint32_t l = 0; l < kMaxLayers; ++l) {
@@ -684,6 +699,25 @@ trax_status trax_set_tuning(trax_ctx *ctx, const trax_tuning *t)
         ctx->graph = nullptr;
     }
     return TRAX_OK;
+}
+
+trax_status trax_set_pair_generator(trax_ctx *ctx, int generator)
+{
+    if (!ctx) return TRAX_ERR_BAD_ARG;
+    if (generator != TRAX_PAIRS_BEAMSPOT && generator != TRAX_PAIRS_SECTOR)
+        return fail(ctx, TRAX_ERR_BAD_ARG, "unknown pair generator");
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->pair_generator = generator;
+    if (ctx->graph) {
+        cudaGraphExecDestroy(ctx->graph);
+        ctx->graph = nullptr;
+    }
+    return TRAX_OK;
+}
+
+int trax_get_pair_generator(const trax_ctx *ctx)
+{
+    return ctx ? ctx->pair_generator : -1;
 }
 
 trax_status trax_get_tuning(const trax_ctx *ctx, trax_tuning *t)
@@ -910,7 +944,7 @@ trax_status trax_grid_build(trax_ctx *ctx, const trax_hits *in, const trax_layou
                             const trax_grid_cfg *grid, trax_sorted_hits *out, uint32_t *d_grid)
 {
     if (!ctx || !in || !layout || !grid || !out || !d_grid) return TRAX_ERR_BAD_ARG;
-    trax_status s = check_grid(ctx, grid);
+    trax_status s = check_grid(ctx, grid, false);
     if (s != TRAX_OK) return s;
     if (layout->n_events != grid->n_events || layout->n_layers != grid->n_layers)
         return fail(ctx, TRAX_ERR_BAD_ARG, "layout and grid disagree on events or layers");
@@ -925,8 +959,8 @@ trax_status trax_grid_build(trax_ctx *ctx, const trax_hits *in, const trax_layou
                         grid->n_events * grid->n_layers, in->n);
 }
 
-trax_status trax_pair_gen(trax_ctx *ctx, const trax_sorted_hits *hits, const uint32_t *d_grid,
-                          const trax_grid_cfg *grid, trax_pairs *out)
+static trax_status pair_gen(trax_ctx *ctx, const trax_sorted_hits *hits, const uint32_t *d_grid,
+                            const trax_grid_cfg *grid, trax_pairs *out, int generator)
 {
     if (!ctx || !hits || !d_grid || !grid || !out) return TRAX_ERR_BAD_ARG;
     trax_status s = check_grid(ctx, grid);
@@ -937,7 +971,20 @@ trax_status trax_pair_gen(trax_ctx *ctx, const trax_sorted_hits *hits, const uin
     const uint64_t slot_cap = (uint64_t)hits->n * ctx->kp.n_lt + 1;
     if (slot_cap > 0xF0000000ull) return fail(ctx, TRAX_ERR_BAD_ARG, "too many hits");
     return enqueue_pairs(ctx, sorted_from(hits), d_grid, (uint2 *)out->pairs, out->offsets,
-                         out->capacity, (uint32_t)slot_cap, G);
+                         out->capacity, (uint32_t)slot_cap, G, generator);
+}
+
+trax_status trax_pair_gen(trax_ctx *ctx, const trax_sorted_hits *hits, const uint32_t *d_grid,
+                          const trax_grid_cfg *grid, trax_pairs *out)
+{
+    return pair_gen(ctx, hits, d_grid, grid, out, TRAX_PAIRS_BEAMSPOT);
+}
+
+trax_status trax_pair_gen_sector(trax_ctx *ctx, const trax_sorted_hits *hits,
+                                 const uint32_t *d_grid, const trax_grid_cfg *grid,
+                                 trax_pairs *out)
+{
+    return pair_gen(ctx, hits, d_grid, grid, out, TRAX_PAIRS_SECTOR);
 }
 
 trax_status trax_triplet_predict(trax_ctx *ctx, const trax_sorted_hits *hits,
@@ -1069,7 +1116,7 @@ trax_status enqueue_pipeline(trax_ctx *ctx)
     if (s != TRAX_OK) return s;
     const uint32_t slot_cap = ctx->r_hits * T + 1;
     s = enqueue_pairs(ctx, sc, grid, (uint2 *)ctx->pairs_buf.p, (uint32_t *)ctx->pair_off.p,
-                      ctx->r_pairs, slot_cap, G);
+                      ctx->r_pairs, slot_cap, G, ctx->pair_generator);
     if (s != TRAX_OK) return s;
     s = enqueue_predict(ctx, sc, grid, (const uint2 *)ctx->pairs_buf.p,
                         (const uint32_t *)ctx->pair_off.p, ctx->r_pairs, (uint2 *)ctx->cands_buf.p,

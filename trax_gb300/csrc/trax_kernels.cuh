@@ -38,7 +38,7 @@ struct KParams {
     uint32_t l1[kMaxLT], l2[kMaxLT], l3[kMaxLT];
     float dtheta[kMaxLT], sigma_z[kMaxLT], dphi[kMaxLT], sigma_phi[kMaxLT];
     float tip[kMaxLT], z0[kMaxLT];
-    uint32_t spread_phi[kMaxLT];
+    uint32_t spread_z[kMaxLT], spread_phi[kMaxLT];
     float rmin[kMaxLayers], rmax[kMaxLayers];
     /* acos(r / (2 * minRadiusCurvature)) of each layer's min / max radius:
      * loop invariants of the phi windows, evaluated once on the host with the
@@ -478,11 +478,14 @@ __global__ void __launch_bounds__(1024) k_grid_build(KParams kp, InCols in, Sort
  * Stage 2: pair generation.
  * ---------------------------------------------------------------------- */
 
-/* Group table: per (event, layer triplet) the first outer hit and the
- * exclusive prefix of outer-hit counts.  One CTA. */
+/* Group table: per (event, layer triplet) the first item hit and the
+ * exclusive prefix of item counts.  The items are the layer-2 (outer) hits
+ * for the beam-spot generator, which strides them (PairGeneratorBeamspot.h:
+ * 68-73), and the layer-1 (inner) hits for the sector generator
+ * (PairGeneratorSector.h:63-67).  One CTA. */
 __global__ void __launch_bounds__(1024) k_pair_groups(KParams kp, const uint32_t *grid,
                                                       uint32_t *g_outer_start, uint32_t *g_base,
-                                                      DevState *st)
+                                                      DevState *st, bool inner_items)
 {
     __shared__ uint32_t s_warp[33];
     __shared__ uint32_t s_carry;
@@ -495,7 +498,8 @@ __global__ void __launch_bounds__(1024) k_pair_groups(KParams kp, const uint32_t
         uint32_t n2 = 0;
         if (g < G) {
             const uint32_t e = g / kp.n_lt, lt = g % kp.n_lt;
-            const uint32_t *row = grid + ((size_t)e * kp.n_layers + (kp.l2[lt] - 1)) * C;
+            const uint32_t item_layer = inner_items ? kp.l1[lt] : kp.l2[lt];
+            const uint32_t *row = grid + ((size_t)e * kp.n_layers + (item_layer - 1)) * C;
             g_outer_start[g] = row[0];
             n2 = row[C - 1] - row[0];
         }
@@ -765,6 +769,156 @@ __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *
                              pairs, pk, pair_cap);
         }
     }
+    if (lane == 0 && my_visits) atomicAdd(&st->pair_slots, my_visits);
+}
+
+/* ------------------------------------------------------------------------
+ * Stage 2, sector variant (PairGeneratorSector.h:43-230).  No cut: every
+ * layer-2 hit in the block of pairSpreadZ rows and pairSpreadPhi columns on
+ * either side of the inner hit's own cell is paired with it.  The window is
+ * pure index arithmetic, so counts need no candidate loads and the kernel
+ * is bound by the 8-byte pair writes.
+ * ---------------------------------------------------------------------- */
+struct SectorWindow {
+    uint32_t zLowSector, zHighSector, phiLowSector, phiHighSector, wrap;
+    bool ok;
+};
+
+/* pairCount's cell block (PairGeneratorSector.h:96-110), same arithmetic. */
+__device__ __forceinline__ SectorWindow sector_window(const KParams &kp, uint32_t lt, float hz,
+                                                      float phi)
+{
+    SectorWindow w;
+    const uint32_t spreadZ = kp.spread_z[lt], spreadPhi = kp.spread_phi[lt];
+    const uint32_t zs = trax_f2u(floorf((hz - TRAX_MIN_Z) / kp.sz_z));
+    const uint32_t zh = zs + spreadZ + 1u;
+    w.zHighSector = zh < kp.nz ? zh : kp.nz;
+    /* max(0u, zLowSector - spreadZ) of unsigned values is the plain
+     * difference: below spreadZ it wraps and no row is visited (:98) */
+    w.zLowSector = zs - spreadZ;
+    int32_t lo = trax_f2i(floorf((phi - TRAX_MIN_PHI) / kp.sz_phi) - (float)spreadPhi);
+    uint32_t hi = (uint32_t)lo + 2u * spreadPhi + 1u;
+    const bool wrap = lo < 0 || hi > kp.nphi + 1;
+    lo = (int32_t)((uint32_t)lo + (uint32_t)(lo < 0) * kp.nphi);
+    hi -= (uint32_t)(hi > kp.nphi + 1) * kp.nphi;
+    w.ok = lo >= 0 && (uint32_t)lo <= kp.nphi + 1 && hi <= kp.nphi + 1;
+    w.phiLowSector = (uint32_t)lo;
+    w.phiHighSector = hi;
+    w.wrap = wrap ? 1u : 0u;
+    return w;
+}
+
+/* One row of the block (:114-140): the loop visits j in [jlo, end2) and maps
+ * j >= rowEnd back by the row length.  As index sets that is
+ * A = [jlo, min(end2, rowEnd)) and B = [max(jlo, rowEnd) - len, end2 - len);
+ * their union in ascending order is B, then A above B. */
+struct RowSpans {
+    uint32_t bLo, bHi, aLo, aHi, visits;
+};
+
+__device__ __forceinline__ RowSpans sector_row(const uint32_t *lGrid2, uint32_t P1,
+                                               const SectorWindow &w, uint32_t zs)
+{
+    RowSpans r;
+    const uint32_t rowStart = lGrid2[zs * P1];
+    const uint32_t rowEnd = lGrid2[(zs + 1) * P1 - 1];
+    const uint32_t len = rowEnd - rowStart;
+    const uint32_t jlo = lGrid2[zs * P1 + w.phiLowSector];
+    const uint32_t end2 = w.wrap * rowEnd + lGrid2[zs * P1 + w.phiHighSector] - w.wrap * rowStart;
+    const uint32_t jb = max(jlo, rowEnd);
+    r.bLo = jb - len;
+    r.bHi = end2 > jb ? end2 - len : r.bLo;
+    r.aHi = min(end2, rowEnd);
+    r.aLo = max(jlo, r.bHi);
+    if (r.aHi < r.aLo) r.aHi = r.aLo;
+    r.visits = end2 > jlo ? end2 - jlo : 0u;
+    return r;
+}
+
+/* Warp tiles of 32 inner-hit items: each lane counts its item's block by
+ * arithmetic, a warp scan plus look-back places the tile, then the warp
+ * writes each item's pairs with all lanes (coalesced 8-byte stores) in
+ * ascending outer-hit order -- the order of the reference's bitmap walk. */
+__global__ void __launch_bounds__(256) k_pair_sector(KParams kp, const uint32_t *grid,
+                                                     const float *Z, const float *PHI,
+                                                     const uint2 *slots, uint32_t slot_cap,
+                                                     uint32_t *pexcl, uint2 *pairs,
+                                                     uint32_t pair_cap, unsigned long long *status,
+                                                     DevState *st)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t P1 = kp.nphi + 1;
+    uint32_t n = st->n_outer;
+    if (n > slot_cap) n = slot_cap;
+    if (n == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            pexcl[0] = 0;
+            st->n_pairs = 0;
+        }
+        return;
+    }
+    const uint32_t ntiles = (n + 31) / 32;
+    unsigned long long my_visits = 0;
+    for (;;) {
+        uint32_t tile = 0;
+        if (lane == 0) tile = atomicAdd(&st->tile_ctr[0], 1u);
+        tile = __shfl_sync(kFull, tile, 0);
+        if (tile >= ntiles) break;
+        const uint32_t s = tile * 32 + lane;
+        bool live = s < n;
+        SectorWindow w{};
+        uint32_t inner = 0, lgoff = 0, mine = 0;
+        if (live) {
+            const uint2 sl = slots[s];
+            inner = sl.x;
+            const uint32_t e = sl.y / kp.n_lt, lt = sl.y % kp.n_lt;
+            lgoff = (e * kp.n_layers + (kp.l2[lt] - 1)) * kp.C;
+            w = sector_window(kp, lt, Z[inner], PHI[inner]);
+            if (!w.ok) {
+                set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_WINDOW_OUTSIDE_GRID);
+                live = false;
+            } else {
+                for (uint32_t zs = w.zLowSector; zs < w.zHighSector; ++zs) {
+                    const RowSpans r = sector_row(grid + lgoff, P1, w, zs);
+                    mine += (r.bHi - r.bLo) + (r.aHi - r.aLo);
+                    my_visits += r.visits;
+                }
+            }
+        }
+        uint32_t tile_end;
+        const uint32_t pos = warp_tile_position(mine, tile, status, st, &tile_end);
+        if (s < n) pexcl[s] = pos;
+        if (tile == ntiles - 1 && lane == 0) {
+            pexcl[n] = tile_end;
+            st->n_pairs = tile_end;
+        }
+        const uint32_t live_mask = __ballot_sync(kFull, live && mine != 0);
+        for (uint32_t m = live_mask; m; m &= m - 1) {
+            const int k = __ffs(m) - 1;
+            SectorWindow wk;
+            wk.zLowSector = __shfl_sync(kFull, w.zLowSector, k);
+            wk.zHighSector = __shfl_sync(kFull, w.zHighSector, k);
+            wk.phiLowSector = __shfl_sync(kFull, w.phiLowSector, k);
+            wk.phiHighSector = __shfl_sync(kFull, w.phiHighSector, k);
+            wk.wrap = __shfl_sync(kFull, w.wrap, k);
+            const uint32_t lgk = __shfl_sync(kFull, lgoff, k);
+            const uint32_t ik = __shfl_sync(kFull, inner, k);
+            uint32_t p = __shfl_sync(kFull, pos, k);
+            for (uint32_t zs = wk.zLowSector; zs < wk.zHighSector; ++zs) {
+                const RowSpans r = sector_row(grid + lgk, P1, wk, zs);
+                for (int part = 0; part < 2; ++part) {
+                    const uint32_t lo = part == 0 ? r.bLo : r.aLo;
+                    const uint32_t hi = part == 0 ? r.bHi : r.aHi;
+                    for (uint32_t idx = lo + lane; idx < hi; idx += 32) {
+                        const uint32_t q = p + (idx - lo);
+                        if (q < pair_cap) pairs[q] = make_uint2(ik, idx);
+                    }
+                    p += hi - lo;
+                }
+            }
+        }
+    }
+    for (int d = 16; d > 0; d >>= 1) my_visits += __shfl_xor_sync(kFull, my_visits, d);
     if (lane == 0 && my_visits) atomicAdd(&st->pair_slots, my_visits);
 }
 

@@ -237,6 +237,36 @@ class PairGeneratorBeamspot(_Op):
         return _grow(ctx, cap, lambda n: Pairing(ctx, n, grid.config.n_events, T), run_once)
 
 
+class PairGeneratorSector(_Op):
+    """PairGeneratorSector::run (PairGeneratorSector.h:38-39, .cpp:5-151):
+    every layer-2 hit in the cells within pairSpreadZ / pairSpreadPhi of the
+    layer-1 hit's own cell, no cut."""
+
+    def run(self, hits: HitCollection, geom_supplement, n_threads, layer_triplets, grid: Grid,
+            capacity=None):
+        ctx = self.ctx
+        self._configure(layer_triplets)
+        T = ctx.config.n_layer_triplets
+        sh = hits.sorted_struct()
+
+        def run_once(p: Pairing):
+            ctx.reset_counts()
+            ps = p.struct()
+            ctx._check(ctx.lib.trax_pair_gen_sector(ctx.h, C.byref(sh), grid.buf.ptr,
+                                                    C.byref(grid.config), C.byref(ps)))
+            c = ctx.counts()
+            if c["status"] not in (0, 5):
+                raise TraxError(c["status"], f"device fault detail {c['error_detail']}")
+            self.counts = c
+            return c["n_pairs"]
+
+        cap = capacity or max(256 * hits.n, 1024)
+        return _grow(ctx, cap, lambda n: Pairing(ctx, n, grid.config.n_events, T), run_once)
+
+
+PAIR_GENERATOR_CLASSES = {"beamspot": PairGeneratorBeamspot, "sector": PairGeneratorSector}
+
+
 class TripletThetaPhiPredictor(_Op):
     def run(self, hits: HitCollection, geom, geom_supplement, dictionary, n_threads,
             layer_triplets, grid: Grid, pairs: Pairing, capacity=None):
@@ -298,14 +328,14 @@ class TripletConnectivity(_Op):
 
 
 def build_triplets(ctx: Context, batch: EventBatch, cfg: A.TraxConfig, n_sectors_z,
-                   n_sectors_phi, n_threads=256):
+                   n_sectors_phi, n_threads=256, pair_generator="beamspot"):
     """The reference's call order (TripletBuilder.cpp:240-263) on one group."""
     ctx.configure(cfg)
     hits = HitCollection(ctx, batch)
     es, ls = supplements(batch)
     grid = Grid(ctx, batch.n_events, batch.n_layers, n_sectors_z, n_sectors_phi)
     GridBuilder(ctx).run(hits, n_threads, es, ls, grid)
-    pairs = PairGeneratorBeamspot(ctx).run(hits, cfg, n_threads, cfg, grid)
+    pairs = PAIR_GENERATOR_CLASSES[pair_generator](ctx).run(hits, cfg, n_threads, cfg, grid)
     cands = TripletThetaPhiPredictor(ctx).run(hits, None, cfg, None, n_threads, cfg, grid, pairs)
     trk = TripletThetaPhiFilter(ctx).run(hits, grid, pairs, cands, n_threads, cfg)
     return hits, grid, pairs, cands, trk
@@ -316,9 +346,10 @@ class Pipeline:
     inside the chain (trax_reserve / trax_seed_batch)."""
 
     def __init__(self, ctx: Context, cfg: A.TraxConfig, grid: A.TraxGridCfg, max_events,
-                 max_hits, max_pairs, max_candidates, max_tracklets):
+                 max_hits, max_pairs, max_candidates, max_tracklets, pair_generator="beamspot"):
         self.ctx = ctx
         ctx.configure(cfg)
+        ctx.set_pair_generator(pair_generator)
         self.n_triplets = cfg.n_layer_triplets
         self.max_tracklets = int(max_tracklets)
         self.n_layers = grid.n_layers

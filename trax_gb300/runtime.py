@@ -39,6 +39,8 @@ _SIGS = {
     "trax_min_radius_curvature": (C.c_float, [C.c_float, C.c_float]),
     "trax_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(A.TraxTuning)]),
     "trax_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(A.TraxTuning)]),
+    "trax_set_pair_generator": (C.c_int, [C.c_void_p, C.c_int]),
+    "trax_get_pair_generator": (C.c_int, [C.c_void_p]),
     "trax_dev_alloc": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_size_t]),
     "trax_dev_free": (C.c_int, [C.c_void_p, C.c_void_p]),
     "trax_host_alloc_pinned": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_size_t]),
@@ -53,6 +55,8 @@ _SIGS = {
                                   C.c_void_p]),
     "trax_pair_gen": (C.c_int, [C.c_void_p, C.POINTER(A.TraxSortedHits), C.c_void_p,
                                 C.POINTER(A.TraxGridCfg), C.POINTER(A.TraxPairs)]),
+    "trax_pair_gen_sector": (C.c_int, [C.c_void_p, C.POINTER(A.TraxSortedHits), C.c_void_p,
+                                       C.POINTER(A.TraxGridCfg), C.POINTER(A.TraxPairs)]),
     "trax_triplet_predict": (C.c_int, [C.c_void_p, C.POINTER(A.TraxSortedHits), C.c_void_p,
                                        C.POINTER(A.TraxGridCfg), C.POINTER(A.TraxPairs),
                                        C.POINTER(A.TraxPairs)]),
@@ -240,6 +244,10 @@ class Context:
 
     def set_tuning(self, run_walk: int, index_min: int):
         self._check(self.lib.trax_set_tuning(self.h, C.byref(A.TraxTuning(run_walk, index_min))))
+
+    def set_pair_generator(self, name: str):
+        """"beamspot" or "sector": the pair generator of the batched pipeline."""
+        self._check(self.lib.trax_set_pair_generator(self.h, A.PAIR_GENERATORS[name]))
 
     def get_tuning(self):
         t = A.TraxTuning()
