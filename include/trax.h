@@ -312,6 +312,96 @@ trax_status trax_triplet_connectivity(trax_ctx *ctx, const trax_tracklets *base,
                                       uint32_t *following_con, int iterate_backwards,
                                       int tight_packing);
 
+/* ---- event ingest ------------------------------------------------------
+ * The reference reads PEventContainer files (EventLoader.h:15-111) or event
+ * stores (PEventStore.h) with protobuf and selects hits with
+ * HitCollection::addEvent (HitCollection.cpp:20-149).  Here a native
+ * decoder fills flat columns on the host and trax_ingest runs addEvent for a
+ * whole batch of events on the GPU. */
+#define TRAX_PB_CONTAINER 0    /* one PEventContainer message (Event.proto:35-38) */
+#define TRAX_PB_EVENT_STORE 1  /* uint32 count, then (varint 1, varint size, PEvent)* */
+
+/* Decoded PEvent / PHit fields (Event.proto:9-33), host arrays sized by
+ * trax_pb_scan.  Integer fields are cut to the widths the reference stores
+ * them in (uint layer, detId and simTrackID); absent optional fields are 0. */
+typedef struct trax_pb_events {
+    uint32_t n_events;
+    uint64_t n_hits;
+    uint64_t *run, *lumi, *event_number;   /* [n_events] */
+    uint64_t *hit_offset;                  /* [n_events + 1] */
+    float *x, *y, *z;                      /* [n_hits] ... */
+    int32_t *detector_type;
+    uint32_t *layer;
+    uint32_t *detector_id;
+    uint64_t *hit_id;
+    uint32_t *sim_track_id;
+    float *sim_track_pt;
+} trax_pb_events;
+
+/* Counts the events and hits of a file image.  Malformed input or a missing
+ * required field returns TRAX_ERR_BAD_INPUT (message in trax_pb_error()). */
+trax_status trax_pb_scan(const uint8_t *buf, size_t len, int format, uint32_t *n_events,
+                         uint64_t *n_hits);
+/* Decodes into the arrays of *out (n_events / n_hits as scanned), on
+ * n_threads host threads (<= 0: all cores). */
+trax_status trax_pb_decode(const uint8_t *buf, size_t len, int format, trax_pb_events *out,
+                           int n_threads);
+const char *trax_pb_error(void);  /* last decoder error of the calling thread */
+
+/* Decoded hit columns on the device, event-major; event_offset[n_events]
+ * == n_hits. */
+typedef struct trax_raw_hits {
+    const float *x, *y, *z;
+    const uint32_t *layer, *detector_id, *sim_track_id;
+    const float *sim_track_pt;
+    const uint32_t *event_offset;  /* [n_events + 1], device */
+    uint32_t n_events, n_hits;
+} trax_raw_hits;
+
+/* addEvent's parameters: TripletConfigurations::minPt_, the layers the
+ * triplets use (bit l-1 for layer l) and the largest of them
+ * (loader.maxLayer), data.onlyTracks and data.tracks (-1 = all;
+ * TripletBuilder.cpp:337-338). */
+typedef struct trax_ingest_cfg {
+    float min_pt;
+    uint32_t max_layer;
+    uint32_t used_layers;
+    int only_tracks;
+    int32_t num_tracks;
+} trax_ingest_cfg;
+
+/* HitCollection columns written by trax_ingest (device, capacity hits). */
+typedef struct trax_hits_out {
+    float *x, *y, *z;
+    uint32_t *layer, *detector_id, *hit_id, *event;
+    uint32_t capacity;
+} trax_hits_out;
+
+/* The findable tracks addEvent returns (HitCollection::tTrackList), by
+ * event and ascending track id: per track the raw hit index (into the
+ * decoded columns) of its first, middle (index n/2) and last hit in layer
+ * order, which PhysicsRecord::fillData reads (PhysicsRecord.cpp:183-185).
+ * Device arrays; offsets [n_events + 1]. */
+typedef struct trax_track_list {
+    uint32_t *track_id, *inner, *middle, *outer;
+    uint32_t *offsets;
+    uint32_t capacity;
+} trax_track_list;
+
+/* HitCollection::addEvent for every event of the batch: drops hits below
+ * min_pt (and of track 0 with only_tracks), keeps the findable tracks (a hit
+ * on every used layer; with only_tracks 0 also the others), stops at the
+ * num_tracks-th findable track, and writes the hits layer-major per event in
+ * the reference's order with DetectorId resolved through the sorted detId
+ * table (DetectorGeometry.cpp:4-30; unresolved ids stay raw).  Writes
+ * d_layer_nhits[n_events * max_layer] (LayerSupplement) and, if tracks is
+ * not NULL, the track list.  Synchronous; *n_hits_out / *n_tracks_out get
+ * the totals (TRAX_ERR_CAPACITY when they exceed the capacities). */
+trax_status trax_ingest(trax_ctx *ctx, const trax_raw_hits *raw, const trax_ingest_cfg *cfg,
+                        const uint32_t *d_det_ids, uint32_t n_det_ids, trax_hits_out *out,
+                        uint32_t *d_layer_nhits, trax_track_list *tracks, uint32_t *n_hits_out,
+                        uint32_t *n_tracks_out);
+
 trax_status trax_read_counts(trax_ctx *ctx, trax_counts *out);  /* synchronises */
 
 /* Diagnostic: evaluates the path's FP32 math on the device for n inputs

@@ -68,6 +68,10 @@ def lib():
             L.or_connectivity_literal_wide.restype = None
             L.or_connectivity_literal_wide.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32,
                                                        C.c_void_p, C.c_void_p, C.c_uint32]
+            L.or_add_event.restype = C.c_uint32
+            L.or_add_event.argtypes = [C.c_void_p] * 3 + [C.c_uint32, C.c_uint32, C.c_float,
+                                                          C.c_uint32, C.c_uint32, C.c_int,
+                                                          C.c_int32] + [C.c_void_p] * 4
             L.or_min_radius_curvature.restype = C.c_float
             L.or_min_radius_curvature.argtypes = [C.c_float, C.c_float]
             _lib = L
@@ -165,3 +169,32 @@ def connectivity_literal_wide(base_hit, base_con, follow_hit, follow_con):
     fc = np.ascontiguousarray(follow_con, dtype=np.uint32).copy()
     lib().or_connectivity_literal_wide(_ptr(bh), _ptr(bc), len(bh), _ptr(fh), _ptr(fc), len(fh))
     return fc
+
+
+def add_events(layer, track, pt, hit_offset, min_pt, max_layer, used_mask, only_tracks=True,
+               num_tracks=-1):
+    """HitCollection::addEvent over every event of decoded columns.  Returns
+    (selected raw indices, layer_nhits [E, max_layer], tracks [(id, inner,
+    middle, outer)] as an (n, 4) array, track offsets [E + 1])."""
+    layer = np.ascontiguousarray(layer, np.uint32)
+    track = np.ascontiguousarray(track, np.uint32)
+    pt = np.ascontiguousarray(pt, np.float32)
+    off = np.asarray(hit_offset, np.int64)
+    E = len(off) - 1
+    idx_all, ln_all, trk_all, toff = [], np.zeros((E, max_layer), np.uint32), [], [0]
+    for e in range(E):
+        n = int(off[e + 1] - off[e])
+        out = np.zeros(max(n, 1), np.uint32)
+        ln = np.zeros(max_layer, np.uint32)
+        trk = np.zeros((max(n, 1), 4), np.uint32)
+        nt = C.c_uint32(0)
+        w = lib().or_add_event(_ptr(layer), _ptr(track), _ptr(pt), int(off[e]), n,
+                               float(min_pt), int(max_layer), int(used_mask), int(only_tracks),
+                               int(num_tracks), _ptr(out), _ptr(ln), _ptr(trk), C.byref(nt))
+        idx_all.append(out[:w])
+        ln_all[e] = ln
+        trk_all.append(trk[:nt.value])
+        toff.append(toff[-1] + nt.value)
+    cat = lambda a, shape: np.concatenate(a) if a else np.zeros(shape, np.uint32)
+    return (cat(idx_all, (0,)), ln_all, cat(trk_all, (0, 4)).reshape(-1, 4),
+            np.array(toff, np.uint32))

@@ -1000,3 +1000,103 @@ void or_free(or_result *r)
         if (i != OR_STATS) free(r->data[i]);
     free(r);
 }
+
+/* ------------------------------------------------------------------------
+ * HitCollection::addEvent (HitCollection.cpp:20-149) for one decoded event.
+ * ---------------------------------------------------------------------- */
+typedef struct { uint32_t track, idx; } ae_hit;
+
+static int ae_cmp_track(const void *a, const void *b)
+{
+    const ae_hit *x = (const ae_hit *)a, *y = (const ae_hit *)b;
+    if (x->track != y->track) return x->track < y->track ? -1 : 1;
+    return x->idx < y->idx ? -1 : x->idx > y->idx;
+}
+
+/* Stable sort by layer of one track's hits (insertion sort). */
+static void ae_sort_layer(uint32_t *idx, uint32_t n, const uint32_t *layer)
+{
+    for (uint32_t i = 1; i < n; ++i) {
+        const uint32_t v = idx[i];
+        uint32_t j = i;
+        while (j > 0 && layer[idx[j - 1]] > layer[v]) {
+            idx[j] = idx[j - 1];
+            --j;
+        }
+        idx[j] = v;
+    }
+}
+
+uint32_t or_add_event(const uint32_t *layer, const uint32_t *track, const float *pt,
+                      uint32_t first, uint32_t n, float min_pt, uint32_t max_layer,
+                      uint32_t used_mask, int only_tracks, int32_t num_tracks,
+                      uint32_t *out_idx, uint32_t *layer_nhits, uint32_t *trk,
+                      uint32_t *n_trk)
+{
+    /* :37-48 allTracks[simTrackID] gets every hit passing the filters, in
+     * file order; a std::map iterates the ids ascending */
+    ae_hit *h = (ae_hit *)malloc((size_t)(n ? n : 1) * sizeof(ae_hit));
+    uint32_t nk = 0;
+    for (uint32_t i = first; i < first + n; ++i) {
+        if (only_tracks && track[i] == 0) continue;
+        if (pt[i] < min_pt) continue;
+        h[nk].track = track[i];
+        h[nk].idx = i;
+        ++nk;
+    }
+    qsort(h, nk, sizeof(ae_hit), ae_cmp_track);
+    uint32_t *sorted = (uint32_t *)malloc((size_t)(nk ? nk : 1) * 4);
+    for (uint32_t i = 0; i < nk; ++i) sorted[i] = h[i].idx;
+
+    /* layers[l]: bucket lists; built as (track start, count, findable)
+     * records replayed below in the reference's push order */
+    uint32_t *bucket_of = (uint32_t *)malloc((size_t)(nk ? nk : 1) * 4); /* 0 none, 1 early, 2 late */
+    memset(bucket_of, 0, (size_t)(nk ? nk : 1) * 4);
+    uint32_t nf = 0;
+    int foundTracks = 0;
+    uint32_t b = 0;
+    while (b < nk && foundTracks != num_tracks) {   /* :61 */
+        uint32_t e = b;
+        while (e < nk && h[e].track == h[b].track) ++e;
+        uint32_t *t = sorted + b;
+        const uint32_t cnt = e - b;
+        ae_sort_layer(t, cnt, layer); /* :51-56 */
+        if (!(only_tracks && h[b].track == 0)) {
+            uint32_t cov = 0; /* :66-78 */
+            for (uint32_t k = 0; k < cnt; ++k)
+                if (layer[t[k]] >= 1 && layer[t[k]] <= max_layer) cov |= 1u << (layer[t[k]] - 1);
+            const int missingHits = (cov & used_mask) != used_mask;
+            if (!(pt[t[0]] < min_pt)) { /* :81-82 */
+                for (uint32_t k = 0; k < cnt; ++k) /* :85-90 */
+                    if (!missingHits) bucket_of[b + k] = 2;
+                    else if (!only_tracks) bucket_of[b + k] = 1;
+                if (!missingHits) {
+                    if (trk) {
+                        trk[4 * nf + 0] = h[b].track;
+                        trk[4 * nf + 1] = t[0];
+                        trk[4 * nf + 2] = t[cnt / 2];
+                        trk[4 * nf + 3] = t[cnt - 1];
+                    }
+                    ++nf;
+                    ++foundTracks;
+                }
+            }
+        }
+        b = e;
+    }
+    /* :96-146: per layer, the early (non-findable) hits in loop order, then
+     * the findable tracks' hits with layer <= maxLayer */
+    uint32_t w = 0;
+    for (uint32_t l = 1; l <= max_layer; ++l) {
+        const uint32_t start = w;
+        for (int pass = 1; pass <= 2; ++pass)
+            for (uint32_t k = 0; k < nk; ++k)
+                if (bucket_of[k] == (uint32_t)pass && layer[sorted[k]] == l) out_idx[w++] = sorted[k];
+        layer_nhits[l - 1] = w - start;
+    }
+    if (n_trk) *n_trk = nf;
+    free(bucket_of);
+    free(sorted);
+    free(h);
+    return w;
+}

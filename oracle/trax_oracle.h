@@ -101,6 +101,17 @@ void or_connectivity_literal_wide(const uint32_t *base_hit, const uint32_t *base
                                   uint32_t n_base, const uint32_t *follow_hit,
                                   uint32_t *follow_con, uint32_t n_follow);
 
+/* HitCollection::addEvent (HitCollection.cpp:20-149) on one event of
+ * decoded columns [first, first + n): writes the selected hits' indices in
+ * the reference's order (layer-major) to out_idx, layer_nhits[max_layer],
+ * and per findable track (track id, first, middle, last hit in layer order)
+ * to trk (4 words each, may be NULL).  Returns the number of hits. */
+uint32_t or_add_event(const uint32_t *layer, const uint32_t *track, const float *pt,
+                      uint32_t first, uint32_t n, float min_pt, uint32_t max_layer,
+                      uint32_t used_mask, int only_tracks, int32_t num_tracks,
+                      uint32_t *out_idx, uint32_t *layer_nhits, uint32_t *trk,
+                      uint32_t *n_trk);
+
 /* Project math, exported so tests can compare against libm / CUDA. */
 float or_atan2f(float y, float x);
 float or_acosf(float x);

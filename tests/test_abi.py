@@ -46,7 +46,10 @@ def test_every_declared_symbol_is_exported(lib):
     ("trax_pairs", A.TraxPairs), ("trax_tracklets", A.TraxTracklets),
     ("trax_counts", A.TraxCounts), ("trax_event_batch", A.TraxEventBatch),
     ("trax_batch_result", A.TraxBatchResult), ("trax_server_opts", A.TraxServerOpts),
-    ("trax_server_result", A.TraxServerResult), ("trax_server_stats", A.TraxServerStats)])
+    ("trax_server_result", A.TraxServerResult), ("trax_server_stats", A.TraxServerStats),
+    ("trax_pb_events", A.TraxPbEvents), ("trax_raw_hits", A.TraxRawHits),
+    ("trax_ingest_cfg", A.TraxIngestCfg), ("trax_hits_out", A.TraxHitsOut),
+    ("trax_track_list", A.TraxTrackList)])
 def test_struct_layout(lib, name, cls):
     assert lib.trax_abi_sizeof(name.encode()) == C.sizeof(cls)
 

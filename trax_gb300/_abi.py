@@ -137,3 +137,38 @@ class TraxServerStats(C.Structure):
     def as_dict(self):
         return {k: (float(getattr(self, k)) if t is C.c_double else int(getattr(self, k)))
                 for k, t in self._fields_}
+
+
+PB_CONTAINER, PB_EVENT_STORE = 0, 1
+
+
+class TraxPbEvents(C.Structure):
+    _fields_ = [("n_events", C.c_uint32), ("n_hits", C.c_uint64),
+                ("run", C.c_void_p), ("lumi", C.c_void_p), ("event_number", C.c_void_p),
+                ("hit_offset", C.c_void_p), ("x", C.c_void_p), ("y", C.c_void_p),
+                ("z", C.c_void_p), ("detector_type", C.c_void_p), ("layer", C.c_void_p),
+                ("detector_id", C.c_void_p), ("hit_id", C.c_void_p),
+                ("sim_track_id", C.c_void_p), ("sim_track_pt", C.c_void_p)]
+
+
+class TraxRawHits(C.Structure):
+    _fields_ = [("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p),
+                ("layer", C.c_void_p), ("detector_id", C.c_void_p),
+                ("sim_track_id", C.c_void_p), ("sim_track_pt", C.c_void_p),
+                ("event_offset", C.c_void_p), ("n_events", C.c_uint32), ("n_hits", C.c_uint32)]
+
+
+class TraxIngestCfg(C.Structure):
+    _fields_ = [("min_pt", C.c_float), ("max_layer", C.c_uint32), ("used_layers", C.c_uint32),
+                ("only_tracks", C.c_int), ("num_tracks", C.c_int32)]
+
+
+class TraxHitsOut(C.Structure):
+    _fields_ = [("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p),
+                ("layer", C.c_void_p), ("detector_id", C.c_void_p), ("hit_id", C.c_void_p),
+                ("event", C.c_void_p), ("capacity", C.c_uint32)]
+
+
+class TraxTrackList(C.Structure):
+    _fields_ = [("track_id", C.c_void_p), ("inner", C.c_void_p), ("middle", C.c_void_p),
+                ("outer", C.c_void_p), ("offsets", C.c_void_p), ("capacity", C.c_uint32)]

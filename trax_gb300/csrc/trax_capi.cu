@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "trax_kernels.cuh"
+#include "trax_ingest.cuh"
 
 using namespace trax;
 
@@ -58,6 +59,7 @@ struct trax_ctx {
     size_t h_stage_words = 0;
     cudaEvent_t stage_free = nullptr;     /* last upload from h_stage done */
     DevBuf seg, g_start, g_base, slots, pexcl, cexcl, st0, st1, st2, st3, zi, conn_keys, conn_sums;
+    DevBuf ing;  /* event ingest scratch */
     cudaEvent_t timers[kTimerSlots] = {};
     int blk_pair = 0, blk_sector = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
 
@@ -514,7 +516,10 @@ size_t trax_abi_sizeof(const char *name)
         {"trax_batch_result", sizeof(trax_batch_result)},
         {"trax_server_opts", sizeof(trax_server_opts)},
         {"trax_server_result", sizeof(trax_server_result)},
-        {"trax_server_stats", sizeof(trax_server_stats)}};
+        {"trax_server_stats", sizeof(trax_server_stats)},
+        {"trax_pb_events", sizeof(trax_pb_events)}, {"trax_raw_hits", sizeof(trax_raw_hits)},
+        {"trax_ingest_cfg", sizeof(trax_ingest_cfg)}, {"trax_hits_out", sizeof(trax_hits_out)},
+        {"trax_track_list", sizeof(trax_track_list)}};
     for (const auto &e : t)
         if (strcmp(e.n, name) == 0) return e.s;
     return 0;
@@ -876,6 +881,84 @@ trax_status trax_prefix_sum_noalloc(const uint32_t *d_in, uint32_t *d_out, uint3
 }
 
 const char *trax_prefix_sum_noalloc_error(void) { return g_noalloc_error.c_str(); }
+
+trax_status trax_ingest(trax_ctx *ctx, const trax_raw_hits *raw, const trax_ingest_cfg *cfg,
+                        const uint32_t *d_det_ids, uint32_t n_det_ids, trax_hits_out *out,
+                        uint32_t *d_layer_nhits, trax_track_list *tracks, uint32_t *n_hits_out,
+                        uint32_t *n_tracks_out)
+{
+    if (!ctx || !raw || !cfg || !out || !d_layer_nhits || !n_hits_out) return TRAX_ERR_BAD_ARG;
+    if (cfg->max_layer == 0 || cfg->max_layer > TRAX_MAX_LAYERS)
+        return fail(ctx, TRAX_ERR_BAD_ARG, "max_layer must be 1..16");
+    if (cfg->used_layers == 0 || (cfg->used_layers >> cfg->max_layer) != 0)
+        return fail(ctx, TRAX_ERR_BAD_ARG, "used_layers must be a non-empty subset of 1..max_layer");
+    if (n_det_ids && !d_det_ids) return TRAX_ERR_BAD_ARG;
+    const uint32_t E = raw->n_events, N = raw->n_hits;
+    *n_hits_out = 0;
+    if (n_tracks_out) *n_tracks_out = 0;
+    if (E == 0) {
+        if (tracks && tracks->offsets) CK(cudaMemsetAsync(tracks->offsets, 0, 4, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        return TRAX_OK;
+    }
+    if (!raw->event_offset || (N && (!raw->x || !raw->y || !raw->z || !raw->layer ||
+                                     !raw->detector_id || !raw->sim_track_id || !raw->sim_track_pt)))
+        return TRAX_ERR_BAD_ARG;
+    /* the per-event CTAs index scratch by these offsets: check them first */
+    std::vector<uint32_t> hoff(E + 1);
+    CK(cudaMemcpyAsync(hoff.data(), raw->event_offset, (size_t)(E + 1) * 4, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (hoff[0] != 0 || hoff[E] != N)
+        return fail(ctx, TRAX_ERR_BAD_INPUT, "event offsets must start at 0 and end at n_hits");
+    for (uint32_t e = 0; e < E; ++e)
+        if (hoff[e + 1] < hoff[e]) return fail(ctx, TRAX_ERR_BAD_INPUT, "event offsets decrease");
+
+    const size_t words = 12ull * N + 2ull * E + 2ull * (E + 1) + 64;
+    trax_status s = ensure(ctx, ctx->ing, words * 4);
+    if (s != TRAX_OK) return s;
+    uint32_t *w = (uint32_t *)ctx->ing.p;
+    IngestScratch sc;
+    uint32_t **cols[12] = {&sc.ka, &sc.va, &sc.kb, &sc.vb, &sc.rank, &sc.tstart,
+                           &sc.tflag, &sc.perm, &sc.tid, &sc.tin, &sc.tmid, &sc.tout};
+    for (int i = 0; i < 12; ++i) *cols[i] = w + (size_t)i * N;
+    sc.n_out = w + 12ull * N;
+    sc.n_trk = sc.n_out + E;
+    uint32_t *out_off = sc.n_trk + E, *trk_off = out_off + (E + 1);
+
+    IngestRaw r{raw->x, raw->y, raw->z, raw->layer, raw->detector_id, raw->sim_track_id,
+                raw->sim_track_pt, raw->event_offset, E};
+    IngestCfg c{cfg->min_pt, cfg->max_layer, cfg->used_layers, cfg->only_tracks ? 1u : 0u,
+                cfg->num_tracks};
+    int b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ingest_event, kIngThreads, 0);
+    const uint32_t blocks = std::min<uint32_t>(E, (uint32_t)(ctx->sm_count * std::max(b, 1)));
+    k_ingest_event<<<blocks, kIngThreads, 0, ctx->stream>>>(r, c, sc, d_layer_nhits);
+    if ((s = mark(ctx, "ingest_event")) != TRAX_OK) return s;
+    k_ingest_offsets<<<1, 1024, 0, ctx->stream>>>(sc.n_out, sc.n_trk, E, out_off, trk_off);
+    IngestOut o{out->x, out->y, out->z, out->layer, out->detector_id, out->hit_id, out->event,
+                out->capacity, nullptr, nullptr, nullptr, nullptr, 0};
+    if (tracks && tracks->track_id) {
+        o.tid = tracks->track_id; o.tin = tracks->inner; o.tmid = tracks->middle;
+        o.tout = tracks->outer; o.tcap = tracks->capacity;
+    }
+    k_ingest_gather<<<std::min<uint32_t>(E, (uint32_t)ctx->blk_small * 4), 256, 0, ctx->stream>>>(
+        r, sc, out_off, trk_off, d_det_ids, n_det_ids, o);
+    if ((s = mark(ctx, "ingest_gather")) != TRAX_OK) return s;
+    if (tracks && tracks->offsets)
+        CK(cudaMemcpyAsync(tracks->offsets, trk_off, (size_t)(E + 1) * 4, cudaMemcpyDeviceToDevice,
+                           ctx->stream));
+    uint32_t tot[2];
+    CK(cudaMemcpyAsync(&tot[0], out_off + E, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(&tot[1], trk_off + E, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    *n_hits_out = tot[0];
+    if (n_tracks_out) *n_tracks_out = tot[1];
+    if (tot[0] > out->capacity) return fail(ctx, TRAX_ERR_CAPACITY, "hit output smaller than the selected hits");
+    if (tracks && tracks->track_id && tot[1] > tracks->capacity)
+        return fail(ctx, TRAX_ERR_CAPACITY, "track list smaller than the findable tracks");
+    return TRAX_OK;
+}
 
 trax_status trax_triplet_connectivity(trax_ctx *ctx, const trax_tracklets *base,
                                       uint32_t n_base, const uint32_t *base_con,

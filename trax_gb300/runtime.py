@@ -55,6 +55,15 @@ _SIGS = {
                                   C.c_void_p]),
     "trax_pair_gen": (C.c_int, [C.c_void_p, C.POINTER(A.TraxSortedHits), C.c_void_p,
                                 C.POINTER(A.TraxGridCfg), C.POINTER(A.TraxPairs)]),
+    "trax_pb_scan": (C.c_int, [C.c_void_p, C.c_size_t, C.c_int, C.POINTER(C.c_uint32),
+                               C.POINTER(C.c_uint64)]),
+    "trax_pb_decode": (C.c_int, [C.c_void_p, C.c_size_t, C.c_int, C.POINTER(A.TraxPbEvents),
+                                 C.c_int]),
+    "trax_pb_error": (C.c_char_p, []),
+    "trax_ingest": (C.c_int, [C.c_void_p, C.POINTER(A.TraxRawHits), C.POINTER(A.TraxIngestCfg),
+                              C.c_void_p, C.c_uint32, C.POINTER(A.TraxHitsOut), C.c_void_p,
+                              C.POINTER(A.TraxTrackList), C.POINTER(C.c_uint32),
+                              C.POINTER(C.c_uint32)]),
     "trax_pair_gen_sector": (C.c_int, [C.c_void_p, C.POINTER(A.TraxSortedHits), C.c_void_p,
                                        C.POINTER(A.TraxGridCfg), C.POINTER(A.TraxPairs)]),
     "trax_triplet_predict": (C.c_int, [C.c_void_p, C.POINTER(A.TraxSortedHits), C.c_void_p,
