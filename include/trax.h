@@ -402,6 +402,56 @@ trax_status trax_ingest(trax_ctx *ctx, const trax_raw_hits *raw, const trax_inge
                         uint32_t *d_layer_nhits, trax_track_list *tracks, uint32_t *n_hits_out,
                         uint32_t *n_tracks_out);
 
+/* ---- physics evaluation (PhysicsRecord, PhysicsRecord.cpp:81-368) -------
+ * Efficiency, fake and clone rates and their eta / pT histograms per
+ * (event, layer triplet), merged per layer triplet (PhysicsRecords). */
+typedef struct trax_physics trax_physics;
+
+/* Per (event, layer triplet): tracklets; valid (first find of a findable
+ * track), clones (later finds), fakes (hits of different tracks), misc
+ * (valid but not findable); findable tracks of the event not found
+ * (missed); findable tracks of the event. */
+typedef struct trax_physics_counts {
+    uint32_t tracklets, valid, clones, fake, misc, missed, findable;
+} trax_physics_counts;
+
+trax_status trax_physics_create(trax_physics **out);
+void trax_physics_destroy(trax_physics *p);
+uint32_t trax_physics_n_records(const trax_physics *p);
+
+/* PhysicsRecord::fillData for every (event, layer triplet) of a batch, in
+ * the reference's order (events outer, triplets inner; TripletBuilder.cpp:
+ * 272-278), merged into rec.  hits: the sorted hit columns the tracklets
+ * index (HitId = simulated track); trk: tracklets with offsets
+ * [n_events * n_lt + 1]; mc: the findable-track list of trax_ingest with the
+ * decoded coordinates it indexes (d_raw_x/y/z).  Device pointers.  counts
+ * (host, [n_events * n_lt]) and categories (host, one per tracklet: 0 valid,
+ * 1 clone, 2 fake, 3 misc) may be NULL.  Synchronous.  Pseudorapidity uses
+ * the project's FP64 asinh (trax_math.h), which agrees with the C library's
+ * to an ulp or two; a histogram bin can differ only for a value within that
+ * distance of a bin edge. */
+trax_status trax_physics_eval(trax_ctx *ctx, trax_physics *rec, const trax_sorted_hits *hits,
+                              const trax_tracklets *trk, uint32_t n_events, uint32_t n_lt,
+                              const trax_track_list *mc, const float *d_raw_x,
+                              const float *d_raw_y, const float *d_raw_z,
+                              trax_physics_counts *counts, uint8_t *categories);
+
+/* Adds one (event, layer triplet) record from host arrays: the tracklets'
+ * categories and bin numbers floor(eta / 0.1), floor(pT / 0.1), and the
+ * missed tracks' bin numbers.  trax_physics_eval calls it per group. */
+trax_status trax_physics_add_group(trax_physics *rec, uint32_t event, uint32_t lt,
+                                   const trax_physics_counts *c, const uint8_t *cat,
+                                   const double *eta_bin, const double *pt_bin, uint32_t n_trk,
+                                   const double *miss_eta_bin, const double *miss_pt_bin,
+                                   uint32_t n_missed);
+
+/* PhysicsRecords::csvDump text (what 0) or one record's eta (1) / pT (2)
+ * histogram file text (tHistogram::csvDump); layer_triplet selects the
+ * record, records + 1 the merged total.  *len gets the full length; with
+ * buf the text is copied NUL-terminated (TRAX_ERR_CAPACITY if cut). */
+trax_status trax_physics_csv(const trax_physics *rec, int what, uint32_t layer_triplet,
+                             char *buf, size_t cap, size_t *len);
+
 trax_status trax_read_counts(trax_ctx *ctx, trax_counts *out);  /* synchronises */
 
 /* Diagnostic: evaluates the path's FP32 math on the device for n inputs

@@ -72,6 +72,11 @@ def lib():
             L.or_add_event.argtypes = [C.c_void_p] * 3 + [C.c_uint32, C.c_uint32, C.c_float,
                                                           C.c_uint32, C.c_uint32, C.c_int,
                                                           C.c_int32] + [C.c_void_p] * 4
+            L.or_physics.restype = None
+            L.or_physics.argtypes = [C.c_void_p] * 8 + [C.c_uint32, C.c_uint32] + \
+                [C.c_void_p] * 15
+            L.or_asinh.restype = C.c_double
+            L.or_asinh.argtypes = [C.c_double]
             L.or_min_radius_curvature.restype = C.c_float
             L.or_min_radius_curvature.argtypes = [C.c_float, C.c_float]
             _lib = L
@@ -198,3 +203,32 @@ def add_events(layer, track, pt, hit_offset, min_pt, max_layer, used_mask, only_
     cat = lambda a, shape: np.concatenate(a) if a else np.zeros(shape, np.uint32)
     return (cat(idx_all, (0,)), ln_all, cat(trk_all, (0, 4)).reshape(-1, 4),
             np.array(toff, np.uint32))
+
+
+def physics(hid, x, y, z, trk, toff, n_events, n_lt, tracks, rx, ry, rz):
+    """PhysicsRecord::fillData per (event, layer triplet).  trk: (K, 3)
+    sorted-hit indices; tracks: (M, 4) rows (id, inner, middle, outer) with
+    offsets tracks_off in tracks[1].  Returns dict of arrays."""
+    mc, moff = tracks
+    u = lambda a: np.ascontiguousarray(a, np.uint32)
+    f = lambda a: np.ascontiguousarray(a, np.float32)
+    trk = u(trk).reshape(-1, 3)
+    mc = u(mc).reshape(-1, 4)
+    K, M, G = len(trk), len(mc), n_events * n_lt
+    cols = [u(trk[:, i]) for i in range(3)] + [u(mc[:, i]) for i in range(4)]
+    out = {"counts": np.zeros((G, 7), np.uint32), "cat": np.zeros(max(K, 1), np.uint8),
+           "eta_bin": np.zeros(max(K, 1)), "pt_bin": np.zeros(max(K, 1)),
+           "missed": np.zeros(max(n_lt * M, 1), np.uint8),
+           "miss_eta_bin": np.zeros(max(n_lt * M, 1)), "miss_pt_bin": np.zeros(max(n_lt * M, 1))}
+    hid, x, y, z, toff, moff = u(hid), f(x), f(y), f(z), u(toff), u(moff)
+    rx, ry, rz = f(rx), f(ry), f(rz)
+    lib().or_physics(_ptr(hid), _ptr(x), _ptr(y), _ptr(z), _ptr(cols[0]), _ptr(cols[1]),
+                     _ptr(cols[2]), _ptr(toff), n_events, n_lt, _ptr(cols[3]), _ptr(cols[4]),
+                     _ptr(cols[5]), _ptr(cols[6]), _ptr(moff), _ptr(rx), _ptr(ry), _ptr(rz),
+                     *(_ptr(out[k]) for k in ("counts", "cat", "eta_bin", "pt_bin", "missed",
+                                               "miss_eta_bin", "miss_pt_bin")))
+    for k in ("cat", "eta_bin", "pt_bin"):
+        out[k] = out[k][:K]
+    for k in ("missed", "miss_eta_bin", "miss_pt_bin"):
+        out[k] = out[k][:n_lt * M]
+    return out

@@ -1100,3 +1100,88 @@ uint32_t or_add_event(const uint32_t *layer, const uint32_t *track, const float 
     free(h);
     return w;
 }
+
+/* ------------------------------------------------------------------------
+ * PhysicsRecord::fillData (PhysicsRecord.cpp:81-218) per (event, layer
+ * triplet), tracklet by tracklet.
+ * ---------------------------------------------------------------------- */
+/* PhysicsRecord::getEta(inner, outer), PhysicsRecord.h:147-155 */
+static double ph_eta(float x1, float y1, float z1, float x3, float y3, float z3)
+{
+    const double px = (double)(x3 - x1), py = (double)(y3 - y1), pz = (double)(z3 - z1);
+    const double t = pz / sqrt(px * px + py * py);
+    return trax_asinh_d(t);
+}
+
+/* getPt(getCircleParams(p1, p2, p3)), PhysicsRecord.cpp:41-79 and
+ * PhysicsRecord.h:161-167 */
+static double ph_pt(float x1, float y1, float x2, float y2, float x3, float y3)
+{
+    const double p1[3] = {x1, y1, (double)(x1 * x1 + y1 * y1)};
+    const double p2[3] = {x2, y2, (double)(x2 * x2 + y2 * y2)};
+    const double p3[3] = {x3, y3, (double)(x3 * x3 + y3 * y3)};
+    const double a[3] = {p2[0] - p1[0], p2[1] - p1[1], p2[2] - p1[2]};
+    const double b[3] = {p3[0] - p1[0], p3[1] - p1[1], p3[2] - p1[2]};
+    double n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+    const double value = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    n[0] /= value;
+    n[1] /= value;
+    n[2] /= value;
+    const double c = -(n[0] * p1[0] + n[1] * p1[1] + n[2] * p1[2]);
+    const double radius = sqrt((1 - n[2] * n[2] - 4 * c * n[2]) / (4 * n[2] * n[2]));
+    const double Q = 1.602177E-19, BZ = 3.8112, GEV_C = 5.344286E-19;
+    return Q * BZ * (radius * 1E-2) / GEV_C;
+}
+
+void or_physics(const uint32_t *hid, const float *x, const float *y, const float *z,
+                const uint32_t *h1, const uint32_t *h2, const uint32_t *h3, const uint32_t *toff,
+                uint32_t n_events, uint32_t n_lt, const uint32_t *mc_id, const uint32_t *mc_in,
+                const uint32_t *mc_mid, const uint32_t *mc_out, const uint32_t *mc_off,
+                const float *rx, const float *ry, const float *rz, uint32_t *counts,
+                uint8_t *cat, double *eta_bin, double *pt_bin, uint8_t *missed,
+                double *miss_eta_bin, double *miss_pt_bin)
+{
+    const uint32_t M = mc_off[n_events];
+    uint8_t *found = (uint8_t *)malloc(M ? M : 1);
+    for (uint32_t e = 0; e < n_events; ++e)
+        for (uint32_t lt = 0; lt < n_lt; ++lt) {
+            const uint32_t g = e * n_lt + lt;
+            uint32_t *c = counts + (size_t)g * 7;
+            memset(c, 0, 7 * 4);
+            memset(found, 0, M ? M : 1);
+            for (uint32_t i = toff[g]; i < toff[g + 1]; ++i) { /* :97-174 */
+                const uint32_t a = h1[i], b = h2[i], d = h3[i];
+                eta_bin[i] = floor(ph_eta(x[a], y[a], z[a], x[d], y[d], z[d]) / 0.1);
+                pt_bin[i] = floor(ph_pt(x[a], y[a], x[b], y[b], x[d], y[d]) / 0.1);
+                if (hid[a] == hid[b] && hid[a] == hid[d]) {
+                    uint32_t k = mc_off[e + 1];
+                    for (uint32_t j = mc_off[e]; j < mc_off[e + 1]; ++j)
+                        if (mc_id[j] == hid[a]) { k = j; break; }
+                    if (k < mc_off[e + 1]) {
+                        if (!found[k]) { found[k] = 1; cat[i] = 0; c[1]++; }
+                        else { cat[i] = 1; c[2]++; }
+                    } else {
+                        cat[i] = 3; c[4]++;
+                    }
+                } else {
+                    cat[i] = 2; c[3]++;
+                }
+                c[0]++;
+            }
+            for (uint32_t k = mc_off[e]; k < mc_off[e + 1]; ++k) { /* :179-202 */
+                const size_t q = (size_t)lt * M + k;
+                c[6]++;
+                missed[q] = !found[k];
+                miss_eta_bin[q] = miss_pt_bin[q] = 0.0;
+                if (!found[k]) {
+                    c[5]++;
+                    const uint32_t a = mc_in[k], m = mc_mid[k], d = mc_out[k];
+                    miss_eta_bin[q] = floor(ph_eta(rx[a], ry[a], rz[a], rx[d], ry[d], rz[d]) / 0.1);
+                    miss_pt_bin[q] = floor(ph_pt(rx[a], ry[a], rx[m], ry[m], rx[d], ry[d]) / 0.1);
+                }
+            }
+        }
+    free(found);
+}
+
+double or_asinh(double t) { return trax_asinh_d(t); }

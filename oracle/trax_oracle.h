@@ -112,6 +112,20 @@ uint32_t or_add_event(const uint32_t *layer, const uint32_t *track, const float 
                       uint32_t *out_idx, uint32_t *layer_nhits, uint32_t *trk,
                       uint32_t *n_trk);
 
+/* PhysicsRecord::fillData (PhysicsRecord.cpp:81-218) for every (event,
+ * layer triplet): counts[g][7] = tracklets, valid, clones, fake, misc,
+ * missed, findable; per tracklet its category (0 valid, 1 clone, 2 fake,
+ * 3 misc) and bin numbers floor(eta / 0.1), floor(pT / 0.1); per (layer
+ * triplet, findable track) whether it was missed and its bin numbers. */
+void or_physics(const uint32_t *hid, const float *x, const float *y, const float *z,
+                const uint32_t *h1, const uint32_t *h2, const uint32_t *h3, const uint32_t *toff,
+                uint32_t n_events, uint32_t n_lt, const uint32_t *mc_id, const uint32_t *mc_in,
+                const uint32_t *mc_mid, const uint32_t *mc_out, const uint32_t *mc_off,
+                const float *rx, const float *ry, const float *rz, uint32_t *counts,
+                uint8_t *cat, double *eta_bin, double *pt_bin, uint8_t *missed,
+                double *miss_eta_bin, double *miss_pt_bin);
+double or_asinh(double t);
+
 /* Project math, exported so tests can compare against libm / CUDA. */
 float or_atan2f(float y, float x);
 float or_acosf(float x);

@@ -14,9 +14,10 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libtrax_gb300.so")
-SOURCES = [os.path.join(CSRC, f) for f in ("trax_capi.cu", "trax_serve.cpp", "trax_pb.cpp")]
+SOURCES = [os.path.join(CSRC, f) for f in ("trax_capi.cu", "trax_serve.cpp", "trax_pb.cpp",
+                                           "trax_physics.cpp")]
 DEPS = SOURCES + [os.path.join(CSRC, f) for f in ("trax_kernels.cuh", "trax_ingest.cuh",
-                                                   "trax_math.h")] + [
+                                                   "trax_physics.cuh", "trax_math.h")] + [
     os.path.join(HERE, "..", "include", "trax.h")]
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"

@@ -21,6 +21,7 @@
 
 #include "trax_kernels.cuh"
 #include "trax_ingest.cuh"
+#include "trax_physics.cuh"
 
 using namespace trax;
 
@@ -59,7 +60,8 @@ struct trax_ctx {
     size_t h_stage_words = 0;
     cudaEvent_t stage_free = nullptr;     /* last upload from h_stage done */
     DevBuf seg, g_start, g_base, slots, pexcl, cexcl, st0, st1, st2, st3, zi, conn_keys, conn_sums;
-    DevBuf ing;  /* event ingest scratch */
+    DevBuf ing;   /* event ingest scratch */
+    DevBuf phys;  /* physics evaluation scratch */
     cudaEvent_t timers[kTimerSlots] = {};
     int blk_pair = 0, blk_sector = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
 
@@ -519,7 +521,8 @@ size_t trax_abi_sizeof(const char *name)
         {"trax_server_stats", sizeof(trax_server_stats)},
         {"trax_pb_events", sizeof(trax_pb_events)}, {"trax_raw_hits", sizeof(trax_raw_hits)},
         {"trax_ingest_cfg", sizeof(trax_ingest_cfg)}, {"trax_hits_out", sizeof(trax_hits_out)},
-        {"trax_track_list", sizeof(trax_track_list)}};
+        {"trax_track_list", sizeof(trax_track_list)},
+        {"trax_physics_counts", sizeof(trax_physics_counts)}};
     for (const auto &e : t)
         if (strcmp(e.n, name) == 0) return e.s;
     return 0;
@@ -957,6 +960,107 @@ trax_status trax_ingest(trax_ctx *ctx, const trax_raw_hits *raw, const trax_inge
     if (tot[0] > out->capacity) return fail(ctx, TRAX_ERR_CAPACITY, "hit output smaller than the selected hits");
     if (tracks && tracks->track_id && tot[1] > tracks->capacity)
         return fail(ctx, TRAX_ERR_CAPACITY, "track list smaller than the findable tracks");
+    return TRAX_OK;
+}
+
+trax_status trax_physics_eval(trax_ctx *ctx, trax_physics *rec, const trax_sorted_hits *hits,
+                              const trax_tracklets *trk, uint32_t n_events, uint32_t n_lt,
+                              const trax_track_list *mc, const float *d_raw_x,
+                              const float *d_raw_y, const float *d_raw_z,
+                              trax_physics_counts *counts, uint8_t *categories)
+{
+    if (!ctx || !rec || !hits || !trk || !mc || !trk->offsets || !mc->offsets || n_lt == 0)
+        return TRAX_ERR_BAD_ARG;
+    if (n_events == 0) return TRAX_OK;
+    const uint32_t G = n_events * n_lt;
+    std::vector<uint32_t> toff(G + 1), moff(n_events + 1);
+    CK(cudaMemcpyAsync(toff.data(), trk->offsets, (size_t)(G + 1) * 4, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(moff.data(), mc->offsets, (size_t)(n_events + 1) * 4,
+                       cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (uint32_t g = 0; g < G; ++g)
+        if (toff[g + 1] < toff[g] || toff[0] != 0)
+            return fail(ctx, TRAX_ERR_BAD_INPUT, "tracklet offsets must rise from 0");
+    for (uint32_t e = 0; e < n_events; ++e)
+        if (moff[e + 1] < moff[e] || moff[0] != 0)
+            return fail(ctx, TRAX_ERR_BAD_INPUT, "track list offsets must rise from 0");
+    const uint32_t K = toff[G], M = moff[n_events];
+    if (K && (!hits->hit_id || !hits->x || !hits->y || !hits->z || !trk->hit1 || !trk->hit2 || !trk->hit3))
+        return TRAX_ERR_BAD_ARG;
+    if (M && (!mc->track_id || !mc->inner || !mc->middle || !mc->outer || !d_raw_x || !d_raw_y || !d_raw_z))
+        return TRAX_ERR_BAD_ARG;
+    const size_t nf = (size_t)n_lt * M;
+    /* scratch: first[nf] u32, mc_index[K] u32, counts[G*kPcN] u32, cat[K] u8,
+     * eta/pt bins [K] f64, missed bins [nf] f64 */
+    const size_t b_u32 = (nf + K + (size_t)G * kPcN) * 4, b_f64 = (2 * (size_t)K + 2 * nf) * 8;
+    trax_status s = ensure(ctx, ctx->phys, b_f64 + b_u32 + K + nf + 64);
+    if (s != TRAX_OK) return s;
+    char *base = (char *)ctx->phys.p;
+    PhysOut o;
+    o.eta_bin = (double *)base;
+    o.pt_bin = o.eta_bin + K;
+    o.miss_eta_bin = o.pt_bin + K;
+    o.miss_pt_bin = o.miss_eta_bin + nf;
+    o.first = (uint32_t *)(o.miss_pt_bin + nf);
+    o.mc_index = o.first + nf;
+    o.counts = o.mc_index + K;
+    o.cat = (uint8_t *)(o.counts + (size_t)G * kPcN);
+    o.missed = o.cat + K;
+    CK(cudaMemsetAsync(o.first, 0xff, nf * 4, ctx->stream));
+    CK(cudaMemsetAsync(o.counts, 0, (size_t)G * kPcN * 4, ctx->stream));
+    PhysIn in{hits->hit_id, hits->x, hits->y, hits->z, trk->hit1, trk->hit2, trk->hit3,
+              trk->offsets, n_events, n_lt, mc->track_id, mc->inner, mc->middle, mc->outer,
+              mc->offsets, d_raw_x, d_raw_y, d_raw_z};
+    const uint32_t blocks = std::max(1u, std::min<uint32_t>((K + 255) / 256, ctx->blk_small * 4));
+    const uint32_t mblocks = std::max(1u, std::min<uint32_t>((uint32_t)((nf + 255) / 256), ctx->blk_small * 4));
+    k_phys_tracklets<<<blocks, 256, 0, ctx->stream>>>(in, o);
+    k_phys_classify<<<blocks, 256, 0, ctx->stream>>>(in, o);
+    k_phys_missed<<<mblocks, 256, 0, ctx->stream>>>(in, o);
+    CK(cudaGetLastError());
+    std::vector<uint32_t> hc((size_t)G * kPcN);
+    std::vector<uint8_t> hcat(K);
+    std::vector<double> heta(K), hpt(K), hmeta(nf), hmpt(nf);
+    std::vector<uint8_t> hmiss(nf);
+    CK(cudaMemcpyAsync(hc.data(), o.counts, hc.size() * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (K) {
+        CK(cudaMemcpyAsync(hcat.data(), o.cat, K, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(heta.data(), o.eta_bin, (size_t)K * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(hpt.data(), o.pt_bin, (size_t)K * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    if (nf) {
+        CK(cudaMemcpyAsync(hmeta.data(), o.miss_eta_bin, nf * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(hmpt.data(), o.miss_pt_bin, nf * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(hmiss.data(), o.missed, nf, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    /* records in the reference's order; missed tracks in track-id order */
+    std::vector<double> me, mp;
+    for (uint32_t e = 0; e < n_events; ++e)
+        for (uint32_t lt = 0; lt < n_lt; ++lt) {
+            const uint32_t g = e * n_lt + lt;
+            trax_physics_counts c;
+            const uint32_t *q = &hc[(size_t)g * kPcN];
+            c.tracklets = q[kPcTracklets]; c.valid = q[kPcValid]; c.clones = q[kPcClones];
+            c.fake = q[kPcFake]; c.misc = q[kPcMisc]; c.missed = q[kPcMissed];
+            c.findable = q[kPcFindable];
+            if (counts) counts[g] = c;
+            me.clear();
+            mp.clear();
+            for (uint32_t k = moff[e]; k < moff[e + 1]; ++k) {
+                const size_t qk = (size_t)lt * M + k;
+                if (hmiss[qk]) {
+                    me.push_back(hmeta[qk]);
+                    mp.push_back(hmpt[qk]);
+                }
+            }
+            const uint32_t t0 = toff[g];
+            trax_status r = trax_physics_add_group(rec, e, lt, &c, hcat.data() + t0, heta.data() + t0,
+                                                   hpt.data() + t0, toff[g + 1] - t0, me.data(),
+                                                   mp.data(), (uint32_t)me.size());
+            if (r != TRAX_OK) return r;
+        }
+    if (categories && K) memcpy(categories, hcat.data(), K);
     return TRAX_OK;
 }
 

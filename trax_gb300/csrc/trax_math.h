@@ -30,6 +30,7 @@
 
 #include <stdint.h>
 #include <math.h>
+#include <string.h>
 
 #if defined(__CUDACC__)
 #define TRAX_HD __host__ __device__ __forceinline__
@@ -170,6 +171,109 @@ TRAX_HD float trax_sector_size_z(uint32_t n_sectors_z)
 TRAX_HD float trax_sector_size_phi(uint32_t n_sectors_phi)
 {
     return (TRAX_MAX_PHI - TRAX_MIN_PHI) / (float)n_sectors_phi;
+}
+
+/* ------------------------------------------------------------------------
+ * FP64 asinh for the physics evaluation's pseudorapidity
+ * (PhysicsRecord.h:152-155).  The reference calls the C library's asinh; the
+ * project needs one definition that host and device evaluate to the same
+ * bits, so it is written here from identities:
+ *   log(x):    x = m * 2^k with m in [sqrt(1/2), sqrt(2)); with
+ *              s = (m - 1) / (m + 1), log(m) = 2 atanh(s) =
+ *              2 (s + s^3/3 + ... + s^21/21) (|s| < 0.172, truncation
+ *              below 2^-54); k ln2 with ln2 split into a 24-bit head
+ *              (exact products) and a tail.
+ *   log1p(y):  Goldberg's correction log(u) * y / (u - 1), u = 1 + y
+ *              ("What every computer scientist should know about
+ *              floating-point arithmetic", 1991, Theorem 4).
+ *   asinh(t):  odd; asinh(a) = log1p(a + a^2 / (1 + sqrt(1 + a^2))) for
+ *              a <= 2, log(2a + 1 / (a + sqrt(a^2 + 1))) above, log(a) + ln2
+ *              beyond 2^28, a itself below 2^-28.
+ * ---------------------------------------------------------------------- */
+TRAX_HD uint64_t trax_d2bits(double d)
+{
+#if defined(__CUDA_ARCH__)
+    return (uint64_t)__double_as_longlong(d);
+#else
+    uint64_t u;
+    memcpy(&u, &d, 8);
+    return u;
+#endif
+}
+
+TRAX_HD double trax_bits2d(uint64_t u)
+{
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)u);
+#else
+    double d;
+    memcpy(&d, &u, 8);
+    return d;
+#endif
+}
+
+#define TRAX_LN2_HI 0x1.62e43p-1
+#define TRAX_LN2_LO (-0x1.05c610ca86c39p-29)
+
+/* log(x) for finite x > 0 (subnormals scaled first); NaN, 0, inf and
+ * negatives follow log's special values. */
+TRAX_HD double trax_log_d(double x)
+{
+    if (!(x == x) || x < 0.0) return trax_bits2d(0x7ff8000000000000ull);
+    if (x == 0.0) return -trax_bits2d(0x7ff0000000000000ull);
+    if (x == trax_bits2d(0x7ff0000000000000ull)) return x;
+    int k = 0;
+    if (x < 0x1p-1022) {
+        x *= 0x1p54;
+        k = -54;
+    }
+    const uint64_t u = trax_d2bits(x);
+    k += (int)((u >> 52) & 0x7ff) - 1022;
+    double m = trax_bits2d((u & 0x000fffffffffffffull) | 0x3fe0000000000000ull); /* [0.5, 1) */
+    if (m < 0x1.6a09e667f3bcdp-1) {
+        m = m * 2.0;
+        k -= 1;
+    }
+    const double s = (m - 1.0) / (m + 1.0);
+    const double s2 = s * s;
+    double p = 1.0 / 21.0;
+    p = p * s2 + 1.0 / 19.0;
+    p = p * s2 + 1.0 / 17.0;
+    p = p * s2 + 1.0 / 15.0;
+    p = p * s2 + 1.0 / 13.0;
+    p = p * s2 + 1.0 / 11.0;
+    p = p * s2 + 1.0 / 9.0;
+    p = p * s2 + 1.0 / 7.0;
+    p = p * s2 + 1.0 / 5.0;
+    p = p * s2 + 1.0 / 3.0;
+    const double lm = 2.0 * s + 2.0 * s * (s2 * p);
+    const double kd = (double)k;
+    return kd * TRAX_LN2_HI + (lm + kd * TRAX_LN2_LO);
+}
+
+TRAX_HD double trax_log1p_d(double y)
+{
+    const double u = 1.0 + y;
+    if (u == 1.0) return y;
+    return trax_log_d(u) * (y / (u - 1.0));
+}
+
+TRAX_HD double trax_asinh_d(double t)
+{
+    if (!(t == t)) return t;
+    const double a = t < 0.0 ? -t : t;
+    double r;
+    if (a < 0x1p-28) {
+        r = a;
+    } else if (a > 0x1p28) {
+        r = trax_log_d(a) + (TRAX_LN2_HI + TRAX_LN2_LO);
+    } else if (a > 2.0) {
+        r = trax_log_d(2.0 * a + 1.0 / (sqrt(a * a + 1.0) + a));
+    } else {
+        const double a2 = a * a;
+        r = trax_log1p_d(a + a2 / (1.0 + sqrt(1.0 + a2)));
+    }
+    return t < 0.0 ? -r : r;
 }
 
 #endif /* TRAX_MATH_H */

@@ -64,6 +64,18 @@ _SIGS = {
                               C.c_void_p, C.c_uint32, C.POINTER(A.TraxHitsOut), C.c_void_p,
                               C.POINTER(A.TraxTrackList), C.POINTER(C.c_uint32),
                               C.POINTER(C.c_uint32)]),
+    "trax_physics_create": (C.c_int, [C.POINTER(C.c_void_p)]),
+    "trax_physics_destroy": (None, [C.c_void_p]),
+    "trax_physics_n_records": (C.c_uint32, [C.c_void_p]),
+    "trax_physics_eval": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(A.TraxSortedHits),
+                                    C.POINTER(A.TraxTracklets), C.c_uint32, C.c_uint32,
+                                    C.POINTER(A.TraxTrackList), C.c_void_p, C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.c_void_p]),
+    "trax_physics_add_group": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
+                                         C.c_void_p, C.c_void_p, C.c_uint32]),
+    "trax_physics_csv": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.c_char_p, C.c_size_t,
+                                   C.POINTER(C.c_size_t)]),
     "trax_pair_gen_sector": (C.c_int, [C.c_void_p, C.POINTER(A.TraxSortedHits), C.c_void_p,
                                        C.POINTER(A.TraxGridCfg), C.POINTER(A.TraxPairs)]),
     "trax_triplet_predict": (C.c_int, [C.c_void_p, C.POINTER(A.TraxSortedHits), C.c_void_p,
