@@ -88,7 +88,8 @@ def _ptr(a):
 
 
 def math_batch(fn, a, b=None):
-    """fn 0: atan2(a, b), 1: acos(a), 2: atan(a) with the project FP32 math."""
+    """fn 0: atan2(a, b), 1: acos(a), 2: atan(a) with the project FP32 math;
+    3 / 4: the float-to-uint / float-to-int casts (result bits as float32)."""
     a = np.ascontiguousarray(a, dtype=np.float32)
     bb = np.ascontiguousarray(b if b is not None else a, dtype=np.float32)
     out = np.empty_like(a)

@@ -65,7 +65,14 @@ float or_atanf(float x) { return trax_atanf(x); }
 void or_math_batch(int fn, const float *a, const float *b, float *out, uint64_t n)
 {
     for (uint64_t i = 0; i < n; ++i)
-        out[i] = fn == 0 ? trax_atan2f(a[i], b[i]) : fn == 1 ? trax_acosf(a[i]) : trax_atanf(a[i]);
+    {
+        if (fn <= 2) {
+            out[i] = fn == 0 ? trax_atan2f(a[i], b[i]) : fn == 1 ? trax_acosf(a[i]) : trax_atanf(a[i]);
+        } else {
+            const uint32_t u = fn == 3 ? trax_f2u(a[i]) : (uint32_t)trax_f2i(a[i]);
+            memcpy(&out[i], &u, 4);
+        }
+    }
 }
 
 /* TripletConfigurations::minRadiusCurvature (TripletConfiguration.cpp:145-152),

@@ -105,10 +105,17 @@ def test_device_math_bit_exact(gpu_ctx):
     u = rng.uniform(-1.05, 1.05, n).astype(np.float32)
     da, db, du = gpu_ctx.upload(a), gpu_ctx.upload(bb), gpu_ctx.upload(u)
     out = gpu_ctx.alloc(n, np.float32)
-    for fn, x, y in ((0, da, db), (1, du, du), (2, da, da)):
+    with np.errstate(over="ignore"):
+        scaled = (a * np.float32(1e9)).astype(np.float32)
+    big = np.concatenate([a, scaled,
+                          np.array([2.0**31, -2.0**31, 2.0**32, -3e9, 4.5e9, 2.0**40, 9.2233715e18,
+                                    -9.2233715e18, 9.3e18, 2.0**62, -(2.0**62)], np.float32)])[:n]
+    dbig = gpu_ctx.upload(big)
+    for fn, x, y in ((0, da, db), (1, du, du), (2, da, da), (3, dbig, dbig), (4, dbig, dbig)):
         gpu_ctx._check(gpu_ctx.lib.trax_eval_math(gpu_ctx.h, fn, x.ptr, y.ptr, out.ptr, n))
         got = out.download(n)
-        host = oracle.math_batch(fn, a if fn != 1 else u, bb if fn == 0 else None)
+        host = oracle.math_batch(fn, big if fn >= 3 else a if fn != 1 else u,
+                                 bb if fn == 0 else None)
         # NaN results may differ in payload bits (the GPU returns the
         # canonical NaN); every other result must match bit for bit
         same = (bits(got) == bits(host)) | (np.isnan(got) & np.isnan(host))

@@ -270,3 +270,26 @@ def test_empty_event_and_empty_layers():
     r = oracle.run(b, _cfg(), TraxGridCfg(1, 3, 8, 16), 4, 256)
     assert r["stats"]["tracklets"] == 0 and r["stats"]["pairs"] == 0
     assert r["trk_offsets"].tolist() == [0, 0]
+
+
+def test_float_to_int_casts_match_their_definition():
+    """trax_f2u / trax_f2i (the reference's implicit casts of floor results):
+    low 32 bits of the 64-bit truncation, 0 for NaN and beyond +-2^63;
+    int32 truncation, INT_MIN for NaN and out of range."""
+    rng = np.random.default_rng(3)
+    v = np.concatenate([rng.normal(0, 10, 20000), rng.normal(0, 1e9, 20000),
+                        10.0 ** rng.uniform(0, 19, 20000) * rng.choice([-1, 1], 20000),
+                        [0.0, -0.0, 0.5, -0.5, -1.0, 2.0**31, -2.0**31, 2.0**32, 2.0**63,
+                         -2.0**63, np.inf, -np.inf, np.nan, 1e-40]]).astype(np.float32)
+    u = oracle.math_batch(3, v).view(np.uint32)
+    i = oracle.math_batch(4, v).view(np.int32)
+    lim = np.float32(9.2233715e18)
+    for x, gu, gi in zip(v.tolist(), u.tolist(), i.tolist()):
+        if x != x or abs(x) >= lim:
+            assert gu == 0
+        else:
+            assert gu == (int(np.trunc(x)) & 0xFFFFFFFF), x
+        if x != x or x >= 2.0**31 or x < -2.0**31:
+            assert gi == -2**31
+        else:
+            assert gi == int(np.trunc(x)), x

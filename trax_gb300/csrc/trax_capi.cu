@@ -73,6 +73,7 @@ struct trax_ctx {
     DevBuf trk_cols[3], trk_off, trk_map[3], r_seg;
     uint32_t gb_C = 0, gb_avg = 0;        /* cached k_grid_build launch plan */
     int gb_warps = 0, gb_per_sm = 0;
+    uint32_t gb_stage = 0;                /* k_grid_build staged-segment capacity */
     cudaGraphExec_t graph = nullptr;
     uint32_t staged_events = 0, staged_hits = 0;
     /* per-kernel timing marks (events recorded between launches) */
@@ -166,10 +167,10 @@ trax_status check_grid(trax_ctx *ctx, const trax_grid_cfg *g, bool need_cfg = tr
 /* Dynamic shared memory plan of k_grid_build: W warps with (W+1)*C words.
  * A warp should own about 128 hits of its segment: fewer warps waste the
  * per-warp cell tables, more leave warps idle. */
-int grid_build_warps(const trax_ctx *ctx, uint32_t C, uint32_t avg_seg)
+int grid_build_warps(const trax_ctx *ctx, uint32_t C, uint32_t avg_seg, uint32_t stage)
 {
     const size_t budget = std::min<size_t>(ctx->smem_optin, 200 * 1024);
-    long w = (long)(budget / (4ull * C)) - 1;
+    long w = (long)((budget - 8ull * stage) / (4ull * C)) - 1;
     long want = 1;
     while (want < 32 && want * 128 < (long)avg_seg) want <<= 1;
     if (w > want) w = want;
@@ -181,11 +182,21 @@ int grid_build_warps(const trax_ctx *ctx, uint32_t C, uint32_t avg_seg)
 trax_status grid_plan(trax_ctx *ctx, uint32_t C, uint32_t avg_seg)
 {
     if (ctx->gb_C == C && ctx->gb_avg == avg_seg && ctx->gb_warps > 0) return TRAX_OK;
-    const int W = grid_build_warps(ctx, C, avg_seg);
+    /* staged segments up to 1.5x the average size (at least 512 hits), while
+     * the staging stays within a quarter of the shared-memory budget */
+    uint32_t stage = std::max<uint32_t>(512, (3 * avg_seg / 2 + 255) / 256 * 256);
+    const size_t budget = std::min<size_t>(ctx->smem_optin, 200 * 1024);
+    while (stage > 256 && 8ull * stage > budget / 4) stage -= 256;
+    int W = grid_build_warps(ctx, C, avg_seg, stage);
+    if (W < 1) {
+        stage = 0;
+        W = grid_build_warps(ctx, C, avg_seg, 0);
+    }
     if (W < 1) return fail(ctx, TRAX_ERR_BAD_ARG, "grid too large for shared memory");
     int per_sm = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_grid_build, W * 32,
-                                                     (size_t)(W + 1) * C * 4));
+                                                     ((size_t)(W + 1) * C + 2ull * stage) * 4));
+    ctx->gb_stage = stage;
     ctx->gb_C = C;
     ctx->gb_avg = avg_seg;
     ctx->gb_warps = W;
@@ -238,11 +249,11 @@ trax_status enqueue_grid(trax_ctx *ctx, const InCols &in, const SortedCols &out,
     trax_status s = grid_plan(ctx, kp.C, max_segs ? n_hits / max_segs : 0);
     if (s != TRAX_OK) return s;
     const int W = ctx->gb_warps, per_sm = ctx->gb_per_sm;
-    const size_t smem = (size_t)(W + 1) * kp.C * 4;
+    const size_t smem = ((size_t)(W + 1) * kp.C + 2ull * ctx->gb_stage) * 4;
     uint32_t blocks = std::min<uint32_t>(max_segs, (uint32_t)(ctx->sm_count * per_sm));
     if (blocks == 0) blocks = 1;
     k_grid_build<<<blocks, W * 32, smem, ctx->stream>>>(kp, in, out, seg_start, seg_n, grid,
-                                                        ctx->d_state);
+                                                        ctx->gb_stage, ctx->d_state);
     CK(cudaGetLastError());
     return mark(ctx, "grid_build");
 }
@@ -408,7 +419,9 @@ namespace {
 __global__ void k_eval_math(int fn, const float *a, const float *b, float *out, uint32_t n)
 {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        out[i] = fn == 0 ? trax_atan2f(a[i], b[i]) : fn == 1 ? trax_acosf(a[i]) : trax_atanf(a[i]);
+        out[i] = fn == 0 ? trax_atan2f(a[i], b[i]) : fn == 1 ? trax_acosf(a[i])
+               : fn == 2 ? trax_atanf(a[i]) : fn == 3 ? __uint_as_float(trax_f2u(a[i]))
+               : __int_as_float(trax_f2i(a[i]));
 }
 
 std::string g_create_error;
@@ -531,7 +544,7 @@ size_t trax_abi_sizeof(const char *name)
 trax_status trax_eval_math(trax_ctx *ctx, int fn, const float *d_a, const float *d_b,
                            float *d_out, uint32_t n)
 {
-    if (!ctx || fn < 0 || fn > 2 || !d_a || !d_out || (fn == 0 && !d_b)) return TRAX_ERR_BAD_ARG;
+    if (!ctx || fn < 0 || fn > 4 || !d_a || !d_out || (fn == 0 && !d_b)) return TRAX_ERR_BAD_ARG;
     if (n == 0) return TRAX_OK;
     k_eval_math<<<ctx->blk_small, 256, 0, ctx->stream>>>(fn, d_a, d_b, d_out, n);
     CK(cudaGetLastError());

@@ -371,18 +371,35 @@ __device__ __forceinline__ uint32_t hit_cell(const KParams &kp, float x, float y
     return zs * (kp.nphi + 1) + ps;
 }
 
-__global__ void __launch_bounds__(1024) k_grid_build(KParams kp, InCols in, SortedCols out,
+constexpr int kGridItems = 4; /* hits per lane held in registers across passes */
+
+/*
+ * One CTA per (event, layer) segment; W warps own contiguous sub-ranges.
+ *   pass 1  cell of every hit (one atan2), per-warp cell counts via
+ *           __match_any_sync into shared memory;
+ *   pass 2  prefix over warps per cell, block scan over cells -> the grid;
+ *   pass 3  each hit's sorted position: segments of at most `stage` hits
+ *           record the inverse permutation (and phi) in shared memory,
+ *   pass 4  and write every column out coalesced, reading the inputs
+ *           gathered from inside the segment (L1/L2 resident).
+ * Larger segments scatter each column directly (4-byte stores to random
+ * positions: one L2 sector per store).  Within a cell, hits keep input order.
+ * Dynamic shared memory: (W + 1) * C + 2 * stage words.
+ */
+__global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols out,
                                                      const uint32_t *seg_start,
                                                      const uint32_t *seg_n, uint32_t *grid,
-                                                     DevState *st)
+                                                     uint32_t stage, DevState *st)
 {
     extern __shared__ uint32_t smem[];
     __shared__ uint32_t s_warp[33];
     const uint32_t C = kp.C;
     const int W = blockDim.x >> 5;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    uint32_t *s_cnt = smem;           /* [W][C] */
-    uint32_t *s_tot = smem + W * C;   /* [C] */
+    uint32_t *s_cnt = smem;                 /* [W][C] */
+    uint32_t *s_tot = smem + W * C;         /* [C] */
+    uint32_t *s_src = s_tot + C;            /* [stage] segment-relative input index */
+    float *s_phi = (float *)(s_src + stage);  /* [stage] */
     const uint32_t nseg = st->n_events * kp.n_layers;
     const uint32_t lt_mask = lanemask_lt();
 
@@ -393,22 +410,64 @@ __global__ void __launch_bounds__(1024) k_grid_build(KParams kp, InCols in, Sort
         __syncthreads();
         const uint32_t chunk = (n + W - 1) / W;
         const uint32_t lo = min(n, w * chunk), hi = min(n, lo + chunk);
+        /* chunks of at most kGridItems * 32 hits keep cell, phi and peer mask
+         * in registers from pass 1 to pass 3 */
+        const bool cached = chunk <= (uint32_t)(kGridItems * 32);
+        const bool staged = n <= stage;
+        float cphi[kGridItems];
+        uint32_t ccell[kGridItems], cpeers[kGridItems];
 
-        /* pass 1 */
-        for (uint32_t b = lo; b < hi; b += 32) {
-            const uint32_t i = b + lane;
-            const bool valid = i < hi;
-            const uint32_t act = __ballot_sync(kFull, valid);
-            if (valid) {
-                const uint32_t h = start + i;
-                float phi;
-                bool bad;
-                const uint32_t cell = hit_cell(kp, in.x[h], in.y[h], in.z[h], &phi, &bad);
-                if (bad) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_OUTSIDE_GRID);
-                const uint32_t peers = __match_any_sync(act, cell);
-                if (lane == __ffs(peers) - 1) s_cnt[w * C + cell] += __popc(peers);
+        /* pass 1: per-warp cell counts */
+        if (cached) {
+            float cx[kGridItems], cy[kGridItems], cz[kGridItems];
+#pragma unroll
+            for (int j = 0; j < kGridItems; ++j) {
+                const uint32_t i = lo + j * 32 + lane;
+                if (i < hi) {
+                    const uint32_t h = start + i;
+                    cx[j] = in.x[h]; cy[j] = in.y[h]; cz[j] = in.z[h];
+                }
             }
-            __syncwarp();
+            /* independent atan2 chains first (ILP), then the warp votes */
+            bool anybad = false;
+#pragma unroll
+            for (int j = 0; j < kGridItems; ++j) {
+                bool bad = false;
+                ccell[j] = 0;
+                cphi[j] = 0.f;
+                if (lo + j * 32 + lane < hi) ccell[j] = hit_cell(kp, cx[j], cy[j], cz[j], &cphi[j], &bad);
+                anybad |= bad;
+            }
+            if (anybad) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_OUTSIDE_GRID);
+#pragma unroll
+            for (int j = 0; j < kGridItems; ++j) {
+                const uint32_t b = lo + j * 32;
+                if (b < hi) {  /* warp-uniform */
+                    const bool valid = b + lane < hi;
+                    const uint32_t act = __ballot_sync(kFull, valid);
+                    if (valid) {
+                        cpeers[j] = __match_any_sync(act, ccell[j]);
+                        if (lane == __ffs(cpeers[j]) - 1) s_cnt[w * C + ccell[j]] += __popc(cpeers[j]);
+                    }
+                    __syncwarp();
+                }
+            }
+        } else {
+            for (uint32_t b = lo; b < hi; b += 32) {
+                const uint32_t i = b + lane;
+                const bool valid = i < hi;
+                const uint32_t act = __ballot_sync(kFull, valid);
+                if (valid) {
+                    const uint32_t h = start + i;
+                    float phi;
+                    bool bad;
+                    const uint32_t cell = hit_cell(kp, in.x[h], in.y[h], in.z[h], &phi, &bad);
+                    if (bad) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_OUTSIDE_GRID);
+                    const uint32_t peers = __match_any_sync(act, cell);
+                    if (lane == __ffs(peers) - 1) s_cnt[w * C + cell] += __popc(peers);
+                }
+                __syncwarp();
+            }
         }
         __syncthreads();
 
@@ -428,7 +487,7 @@ __global__ void __launch_bounds__(1024) k_grid_build(KParams kp, InCols in, Sort
             const uint32_t c0 = min(C, threadIdx.x * per), c1 = min(C, c0 + per);
             uint32_t sum = 0;
             for (uint32_t c = c0; c < c1; ++c) sum += s_tot[c];
-            uint32_t run = block_exclusive_scan(sum, s_warp, nullptr) + start;
+            uint32_t run = block_exclusive_scan(sum, s_warp, nullptr);
             for (uint32_t c = c0; c < c1; ++c) {
                 const uint32_t t = s_tot[c];
                 s_tot[c] = run;
@@ -437,40 +496,82 @@ __global__ void __launch_bounds__(1024) k_grid_build(KParams kp, InCols in, Sort
         }
         __syncthreads();
         for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
-            const uint32_t b = s_tot[c];
-            grid[(size_t)seg * C + c] = b;
+            const uint32_t b = s_tot[c];  /* segment-relative */
+            grid[(size_t)seg * C + c] = start + b;
             for (int q = 0; q < W; ++q) s_cnt[q * C + c] += b;
         }
         __syncthreads();
 
-        /* pass 3 */
-        for (uint32_t b = lo; b < hi; b += 32) {
-            const uint32_t i = b + lane;
-            const bool valid = i < hi;
-            const uint32_t act = __ballot_sync(kFull, valid);
-            uint32_t pos = 0, peers = 0, cell = 0;
-            float x = 0.f, y = 0.f, z = 0.f, phi = 0.f;
-            uint32_t h = 0;
-            if (valid) {
-                h = start + i;
-                x = in.x[h]; y = in.y[h]; z = in.z[h];
-                bool bad;
-                cell = hit_cell(kp, x, y, z, &phi, &bad);
-                peers = __match_any_sync(act, cell);
-                pos = s_cnt[w * C + cell] + __popc(peers & lt_mask);
+        /* pass 3: positions (segment-relative) */
+        if (staged && cached) {
+#pragma unroll
+            for (int j = 0; j < kGridItems; ++j) {
+                const uint32_t b = lo + j * 32;
+                if (b < hi) {  /* warp-uniform */
+                    const bool valid = b + lane < hi;
+                    uint32_t pos = 0;
+                    if (valid) pos = s_cnt[w * C + ccell[j]] + __popc(cpeers[j] & lt_mask);
+                    __syncwarp();
+                    if (valid && lane == __ffs(cpeers[j]) - 1) s_cnt[w * C + ccell[j]] += __popc(cpeers[j]);
+                    __syncwarp();
+                    if (valid) {
+                        s_src[pos] = b + lane;
+                        s_phi[pos] = cphi[j];
+                    }
+                }
             }
-            __syncwarp();
-            if (valid && lane == __ffs(peers) - 1) s_cnt[w * C + cell] += __popc(peers);
-            __syncwarp();
-            if (valid) {
-                const uint32_t ly = in.layer[h], ev = in.event[h];
-                if (ly != l + 1 || ev != e) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_LAYER_MISMATCH);
-                out.x[pos] = x; out.y[pos] = y; out.z[pos] = z; out.phi[pos] = phi;
-                out.layer[pos] = ly; out.det[pos] = in.det[h]; out.hitid[pos] = in.hitid[h];
-                out.event[pos] = ev; out.orig[pos] = h;
+        } else {
+            for (uint32_t b = lo; b < hi; b += 32) {
+                const uint32_t i = b + lane;
+                const bool valid = i < hi;
+                const uint32_t act = __ballot_sync(kFull, valid);
+                uint32_t pos = 0, peers = 0, cell = 0;
+                float x = 0.f, y = 0.f, z = 0.f, phi = 0.f;
+                uint32_t h = 0;
+                if (valid) {
+                    h = start + i;
+                    x = in.x[h]; y = in.y[h]; z = in.z[h];
+                    bool bad;
+                    cell = hit_cell(kp, x, y, z, &phi, &bad);
+                    peers = __match_any_sync(act, cell);
+                    pos = s_cnt[w * C + cell] + __popc(peers & lt_mask);
+                }
+                __syncwarp();
+                if (valid && lane == __ffs(peers) - 1) s_cnt[w * C + cell] += __popc(peers);
+                __syncwarp();
+                if (valid) {
+                    if (staged) {
+                        s_src[pos] = i;
+                        s_phi[pos] = phi;
+                    } else {
+                        const uint32_t ly = in.layer[h], ev = in.event[h];
+                        if (ly != l + 1 || ev != e) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_LAYER_MISMATCH);
+                        const uint32_t d = start + pos;
+                        out.x[d] = x; out.y[d] = y; out.z[d] = z; out.phi[d] = phi;
+                        out.layer[d] = ly; out.det[d] = in.det[h]; out.hitid[d] = in.hitid[h];
+                        out.event[d] = ev; out.orig[d] = h;
+                    }
+                }
             }
         }
         __syncthreads();
+
+        /* pass 4: coalesced column writes of a staged segment */
+        if (staged) {
+            bool mismatch = false;
+            for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+                const uint32_t h = start + s_src[k];
+                const float x = in.x[h], y = in.y[h], z = in.z[h];
+                const uint32_t ly = in.layer[h], dt = in.det[h], hd = in.hitid[h], ev = in.event[h];
+                mismatch |= ly != l + 1 || ev != e;
+                const uint32_t d = start + k;
+                out.x[d] = x; out.y[d] = y; out.z[d] = z; out.phi[d] = s_phi[k];
+                out.layer[d] = ly; out.det[d] = dt; out.hitid[d] = hd; out.event[d] = ev;
+                out.orig[d] = h;
+            }
+            if (mismatch) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_LAYER_MISMATCH);
+            __syncthreads();
+        }
     }
 }
 

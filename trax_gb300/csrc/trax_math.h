@@ -141,7 +141,20 @@ TRAX_HD uint32_t trax_f2u(float v)
 {
     if (!(v == v)) return 0u;
     if (v >= 9.2233715e18f || v <= -9.2233715e18f) return 0u;
-    return (uint32_t)(uint64_t)(int64_t)v;
+    if (v > -2147483648.0f && v < 2147483648.0f) return (uint32_t)(int32_t)v;
+    /* |v| >= 2^31 is an integer m * 2^s (24-bit m, s >= 8): the low 32 bits
+     * of its two's-complement value come from the bits, without the 64-bit
+     * conversion (a slow FP64-pipe instruction on the GPU) */
+    uint32_t bits;
+#if defined(__CUDA_ARCH__)
+    bits = __float_as_uint(v);
+#else
+    memcpy(&bits, &v, 4);
+#endif
+    const uint32_t m = (bits & 0x7FFFFFu) | 0x800000u;
+    const int sh = (int)((bits >> 23) & 0xFFu) - 150;
+    const uint32_t low = sh >= 32 ? 0u : m << sh;
+    return (bits >> 31) ? 0u - low : low;
 }
 
 TRAX_HD int32_t trax_f2i(float v)
