@@ -457,7 +457,8 @@ trax_status trax_read_counts(trax_ctx *ctx, trax_counts *out);  /* synchronises 
 /* Diagnostic: evaluates the path's FP32 math on the device for n inputs
  * (fn 0: atan2(a, b), 1: acos(a), 2: atan(a); 3 and 4: the float-to-uint /
  * float-to-int casts of the sector arithmetic, result bits stored in the
- * float output); device pointers. */
+ * float output; 5: floor(a / b) in the kernels' reciprocal form); device
+ * pointers. */
 trax_status trax_eval_math(trax_ctx *ctx, int fn, const float *d_a, const float *d_b,
                            float *d_out, uint32_t n);
 trax_status trax_reset_counts(trax_ctx *ctx);

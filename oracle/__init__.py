@@ -77,6 +77,8 @@ def lib():
                 [C.c_void_p] * 15
             L.or_asinh.restype = C.c_double
             L.or_asinh.argtypes = [C.c_double]
+            L.or_floor_div_mismatches.restype = C.c_uint64
+            L.or_floor_div_mismatches.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64]
             L.or_min_radius_curvature.restype = C.c_float
             L.or_min_radius_curvature.argtypes = [C.c_float, C.c_float]
             _lib = L

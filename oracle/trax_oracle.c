@@ -62,6 +62,19 @@ float or_atan2f(float y, float x) { return trax_atan2f(y, x); }
 float or_acosf(float x) { return trax_acosf(x); }
 float or_atanf(float x) { return trax_atanf(x); }
 
+/* trax_floor_div(x, d, 1/d) and floorf(x / d) for n pairs: the kernels'
+ * reciprocal form must equal the plain division everywhere. */
+uint64_t or_floor_div_mismatches(const float *x, const float *d, uint64_t n)
+{
+    uint64_t bad = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        const float a = trax_floor_div(x[i], d[i], 1.0f / d[i]);
+        const float b = floorf(x[i] / d[i]);
+        if (!(a == b || (a != a && b != b))) ++bad;
+    }
+    return bad;
+}
+
 void or_math_batch(int fn, const float *a, const float *b, float *out, uint64_t n)
 {
     for (uint64_t i = 0; i < n; ++i)

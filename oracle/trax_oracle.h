@@ -131,6 +131,7 @@ float or_atan2f(float y, float x);
 float or_acosf(float x);
 float or_atanf(float x);
 float or_min_radius_curvature(float min_pt, float bz);
+uint64_t or_floor_div_mismatches(const float *x, const float *d, uint64_t n);
 /* fn 0: atan2(a, b), 1: acos(a), 2: atan(a), 3: trax_f2u(a), 4: trax_f2i(a)
  * (3, 4: the integer's bits in the float output), over n floats. */
 void or_math_batch(int fn, const float *a, const float *b, float *out, uint64_t n);

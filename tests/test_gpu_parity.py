@@ -222,3 +222,19 @@ def test_tuning_does_not_change_results(gpu_ctx):
         gpu_ctx.set_tuning(48, 16)
     for t in outs:
         assert np.array_equal(t, ref)
+
+
+def test_device_reciprocal_floor_div(gpu_ctx):
+    """The kernels' sector floors through 1/d equal floorf(x / d) on the
+    device, next to every cell boundary of every grid size."""
+    from test_oracle import floor_div_cases
+    x, d = floor_div_cases()
+    n = x.size
+    dx, dd = gpu_ctx.upload(x), gpu_ctx.upload(d)
+    out = gpu_ctx.alloc(n, np.float32)
+    gpu_ctx._check(gpu_ctx.lib.trax_eval_math(gpu_ctx.h, 5, dx.ptr, dd.ptr, out.ptr, n))
+    got = out.download(n)
+    with np.errstate(all="ignore"):
+        want = np.floor(x / d).astype(np.float32)
+    same = (bits(got) == bits(want)) | (np.isnan(got) & np.isnan(want))
+    assert same.all(), x[~same][:8]

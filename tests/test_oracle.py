@@ -293,3 +293,34 @@ def test_float_to_int_casts_match_their_definition():
             assert gi == -2**31
         else:
             assert gi == int(np.trunc(x)), x
+
+
+def floor_div_cases(seed=9):
+    """Numerators around every sector boundary of every grid size the
+    autotuner and the configs use, plus random ones."""
+    rng = np.random.default_rng(seed)
+    xs, ds = [], []
+    for n in list(range(1, 130)) + [256, 512]:
+        for extent in (np.float32(600.0), np.float32(2 * np.float32(np.pi))):
+            d = np.float32(extent / np.float32(n))
+            k = np.arange(-2, n + 3, dtype=np.float32)
+            base = (k * d).astype(np.float32)
+            for ulps in range(-4, 5):
+                xs.append(np.nextafter(base, np.float32(np.inf) if ulps > 0 else np.float32(-np.inf))
+                          if ulps else base)
+                for _ in range(abs(ulps) - 1):
+                    xs[-1] = np.nextafter(xs[-1], np.float32(np.inf) if ulps > 0 else np.float32(-np.inf))
+                ds.append(np.full(len(k), d, np.float32))
+            xs.append(rng.uniform(-50, float(extent) + 50, 4000).astype(np.float32))
+            ds.append(np.full(4000, d, np.float32))
+    x = np.concatenate(xs + [np.array([np.nan, np.inf, -np.inf, 0.0, -0.0, 3e38, 1e-40],
+                                      np.float32)])
+    d = np.concatenate(ds + [np.full(7, np.float32(50.0), np.float32)])
+    return x.astype(np.float32), d.astype(np.float32)
+
+
+def test_reciprocal_floor_div_equals_division():
+    """trax_floor_div (the kernels' sector floors through 1/d) gives
+    floorf(x / d) bit for bit, including next to every cell boundary."""
+    x, d = floor_div_cases()
+    assert oracle.lib().or_floor_div_mismatches(oracle._ptr(x), oracle._ptr(d), x.size) == 0

@@ -62,6 +62,8 @@ struct trax_ctx {
     DevBuf seg, g_start, g_base, slots, pexcl, cexcl, st0, st1, st2, st3, zi, conn_keys, conn_sums;
     DevBuf ing;   /* event ingest scratch */
     DevBuf phys;  /* physics evaluation scratch */
+    DevBuf prec;  /* prediction store records */
+    DevBuf zp;    /* input position of each z-index entry */
     cudaEvent_t timers[kTimerSlots] = {};
     int blk_pair = 0, blk_sector = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
 
@@ -144,6 +146,8 @@ void fill_grid_params(KParams &kp, const trax_grid_cfg *g)
     kp.C = (g->n_sectors_z + 1) * (g->n_sectors_phi + 1);
     kp.sz_z = trax_sector_size_z(g->n_sectors_z);
     kp.sz_phi = trax_sector_size_phi(g->n_sectors_phi);
+    kp.inv_sz_z = 1.0f / kp.sz_z;
+    kp.inv_sz_phi = 1.0f / kp.sz_phi;
 }
 
 /* The grid build needs no layer-triplet configuration (GridBuilder::run
@@ -308,9 +312,10 @@ trax_status enqueue_zindex(trax_ctx *ctx, const SortedCols &h, const uint32_t *g
     if (ctx->kp.zi_min >= 256) return TRAX_OK; /* no cell is searched: no index */
     trax_status s = ensure(ctx, ctx->zi, (size_t)max_hits * 8 + 8);
     if (s != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->zp, (size_t)max_hits * 4 + 4)) != TRAX_OK) return s;
     k_zindex<<<ctx->blk_small * 4, 256, 0, ctx->stream>>>(
         grid, ctx->kp.n_layers * ctx->kp.C, ctx->kp.zi_min, h.z, h.phi, (float2 *)ctx->zi.p,
-        ctx->d_state);
+        (uint32_t *)ctx->zp.p, ctx->d_state);
     CK(cudaGetLastError());
     return mark(ctx, "zindex");
 }
@@ -323,18 +328,30 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
     const KParams &kp = ctx->kp;
     trax_status s;
     if ((s = ensure(ctx, ctx->cexcl, (size_t)(pair_cap + 1) * 4)) != TRAX_OK) return s;
-    const uint32_t ntile = tiles_for(pair_cap, kTileItems);
+    const uint32_t ntile = tiles_for(pair_cap, kScanItems * kScanThreads);
     if ((s = ensure(ctx, ctx->st1, (size_t)ntile * 8)) != TRAX_OK) return s;
+    const uint32_t rec_cap = cand_cap ? cand_cap : 1;
+    if ((s = ensure(ctx, ctx->prec, (size_t)rec_cap * sizeof(PredRec))) != TRAX_OK) return s;
     uint32_t *cexcl = (uint32_t *)ctx->cexcl.p;
+    PredRec *recs = (PredRec *)ctx->prec.p;
     DevState *st = ctx->d_state;
     /* the pair total is st->n_pairs: written by the pair stage, or copied
      * from pair_offsets[G] by trax_triplet_predict */
+    CK(cudaMemsetAsync(&st->n_prec, 0, 4, ctx->stream));
+    k_predict_count<<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
+        kp, grid, h.x, h.y, h.z, h.phi, h.event, h.layer, (const float2 *)ctx->zi.p, pairs,
+        &st->n_pairs, pair_cap, cexcl, recs, rec_cap, st);
+    if ((s = mark(ctx, "predict")) != TRAX_OK) return s;
     CK(cudaMemsetAsync(&st->tile_ctr[1], 0, 4, ctx->stream));
     CK(cudaMemsetAsync(ctx->st1.p, 0, (size_t)ntile * 8, ctx->stream));
-    k_predict_fused<<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
-        kp, grid, h.x, h.y, h.z, h.phi, h.event, h.layer, (const float2 *)ctx->zi.p, pairs,
-        &st->n_pairs, pair_cap, cexcl, cands, cand_cap, (unsigned long long *)ctx->st1.p, st);
-    if ((s = mark(ctx, "predict")) != TRAX_OK) return s;
+    k_scan<kScanItems><<<ctx->blk_scan, kScanThreads, 0, ctx->stream>>>(
+        cexcl, cexcl, &st->n_pairs, pair_cap, &st->n_cands, 1, (unsigned long long *)ctx->st1.p, st);
+    if ((s = mark(ctx, "predict_scan")) != TRAX_OK) return s;
+    k_predict_store<<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
+        kp, grid, h.z, h.phi, (const float2 *)ctx->zi.p, (const uint32_t *)ctx->zp.p, recs,
+        rec_cap, cexcl, &st->n_pairs,
+        pair_cap, &st->n_cands, cands, cand_cap, st);
+    if ((s = mark(ctx, "predict_store")) != TRAX_OK) return s;
     k_cand_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(pair_offsets, cexcl, cand_offsets,
                                                             kp.n_lt, pair_cap, &st->n_cands,
                                                             cand_cap, st);
@@ -421,7 +438,8 @@ __global__ void k_eval_math(int fn, const float *a, const float *b, float *out, 
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         out[i] = fn == 0 ? trax_atan2f(a[i], b[i]) : fn == 1 ? trax_acosf(a[i])
                : fn == 2 ? trax_atanf(a[i]) : fn == 3 ? __uint_as_float(trax_f2u(a[i]))
-               : __int_as_float(trax_f2i(a[i]));
+               : fn == 4 ? __int_as_float(trax_f2i(a[i]))
+               : trax_floor_div(a[i], b[i], 1.0f / b[i]);
 }
 
 std::string g_create_error;
@@ -544,7 +562,8 @@ size_t trax_abi_sizeof(const char *name)
 trax_status trax_eval_math(trax_ctx *ctx, int fn, const float *d_a, const float *d_b,
                            float *d_out, uint32_t n)
 {
-    if (!ctx || fn < 0 || fn > 4 || !d_a || !d_out || (fn == 0 && !d_b)) return TRAX_ERR_BAD_ARG;
+    if (!ctx || fn < 0 || fn > 5 || !d_a || !d_out || ((fn == 0 || fn == 5) && !d_b))
+        return TRAX_ERR_BAD_ARG;
     if (n == 0) return TRAX_OK;
     k_eval_math<<<ctx->blk_small, 256, 0, ctx->stream>>>(fn, d_a, d_b, d_out, n);
     CK(cudaGetLastError());
@@ -602,7 +621,7 @@ trax_status trax_ctx_create(trax_ctx **out, int device)
     ctx->blk_pair = ctx->sm_count * std::max(b, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_sector, kFusedThreads, 0);
     ctx->blk_sector = ctx->sm_count * std::max(b, 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_predict_fused, kFusedThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_predict_count, kFusedThreads, 0);
     ctx->blk_pred = ctx->sm_count * std::max(b, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_filter, 256, 0);
     ctx->blk_filter = ctx->sm_count * std::max(b, 1);
@@ -1260,13 +1279,15 @@ trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers
     if ((s = ensure(ctx, ctx->trk_off, (size_t)(G + 1) * 4)) != TRAX_OK) return s;
     /* scratch at its maximum so the captured graph never reallocates */
     if ((s = ensure(ctx, ctx->zi, (size_t)max_hits * 8 + 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->zp, (size_t)max_hits * 4 + 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->g_start, G * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->g_base, (G + 1) * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->slots, slot_cap * 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->pexcl, (slot_cap + 1) * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->st0, (size_t)tiles_for((uint32_t)slot_cap, kTileItems) * 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->cexcl, (size_t)(max_pairs + 1) * 4)) != TRAX_OK) return s;
-    if ((s = ensure(ctx, ctx->st1, (size_t)tiles_for(max_pairs, kTileItems) * 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->st1, (size_t)tiles_for(max_pairs, kScanItems * kScanThreads) * 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->prec, (size_t)(max_candidates ? max_candidates : 1) * sizeof(PredRec))) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->st2, (size_t)tiles_for(max_candidates, 256 * kFilterItems) * 8)) != TRAX_OK) return s;
     if ((s = ensure_stage(ctx, (size_t)max_events * max_layers * 2 + 4)) != TRAX_OK) return s;
     CK(cudaStreamSynchronize(ctx->stream));

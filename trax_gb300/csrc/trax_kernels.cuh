@@ -35,6 +35,7 @@ constexpr uint32_t kFull = 0xffffffffu;
 struct KParams {
     uint32_t n_layers, nz, nphi, C, n_lt;
     float sz_z, sz_phi, rmin_curv;
+    float inv_sz_z, inv_sz_phi;  /* 1.0f / sz_*: trax_floor_div */
     uint32_t l1[kMaxLT], l2[kMaxLT], l3[kMaxLT];
     float dtheta[kMaxLT], sigma_z[kMaxLT], dphi[kMaxLT], sigma_phi[kMaxLT];
     float tip[kMaxLT], z0[kMaxLT];
@@ -62,7 +63,8 @@ struct DevState {
     unsigned long long cand_truncated;
     uint32_t tile_ctr[4];    /* decoupled look-back tile tickets */
     uint32_t aux_n;          /* element count of a standalone prefix sum */
-    uint32_t pad[3];
+    uint32_t n_prec;         /* prediction store records */
+    uint32_t pad[2];
 };
 
 struct SortedCols {
@@ -336,13 +338,68 @@ __global__ void __launch_bounds__(256) k_scan(const uint32_t *in, uint32_t *out,
         if (blockIdx.x == 0 && threadIdx.x == 0 && total_out) *total_out = 0;
         return;
     }
-    lookback_scan<ITEMS>(
-        n, &st->tile_ctr[ctr_slot], status, st,
-        [&](uint32_t i) { return in[i]; },
-        [&](uint32_t i, uint32_t e, uint32_t) { out[i] = e; },
-        [&](uint32_t t) {
-            if (total_out) *total_out = t;
-        });
+    /* full tiles of 16-byte aligned arrays move 4 elements per access */
+    const bool vec = ITEMS % 4 == 0 && ((reinterpret_cast<uintptr_t>(in) |
+                                         reinterpret_cast<uintptr_t>(out)) & 15u) == 0;
+    __shared__ uint32_t s_warp[33];
+    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_prefix;
+    const uint32_t tileItems = blockDim.x * ITEMS;
+    const uint32_t ntiles = (n + tileItems - 1) / tileItems;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(&st->tile_ctr[ctr_slot], 1u);
+        __syncthreads();
+        const uint32_t tile = s_tile;
+        if (tile >= ntiles) break;
+        const uint32_t base = tile * tileItems + threadIdx.x * ITEMS;
+        const bool full = vec && (tile + 1) * tileItems <= n;
+        uint32_t v[ITEMS];
+        if (full) {
+#pragma unroll
+            for (int k = 0; k < ITEMS; k += 4) {
+                const uint4 q = *reinterpret_cast<const uint4 *>(in + base + k);
+                v[k] = q.x; v[k + 1] = q.y; v[k + 2] = q.z; v[k + 3] = q.w;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < ITEMS; ++k) v[k] = (base + k < n) ? in[base + k] : 0u;
+        }
+        uint32_t sum = 0;
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) sum += v[k];
+        uint32_t agg;
+        const uint32_t excl = block_exclusive_scan(sum, s_warp, &agg);
+        if (threadIdx.x == 0) {
+            uint32_t prefix = 0;
+            if (tile == 0) {
+                st_relaxed64(status, kFlagInc | agg);
+            } else {
+                st_relaxed64(status + tile, kFlagAgg | agg);
+                prefix = lookback_prefix(status, tile, st);
+                st_relaxed64(status + tile, kFlagInc | (uint32_t)(prefix + agg));
+            }
+            s_prefix = prefix;
+            if (tile == ntiles - 1 && total_out) *total_out = prefix + agg;
+        }
+        __syncthreads();
+        uint32_t run = s_prefix + excl;
+        uint32_t o[ITEMS];
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            o[k] = run;
+            run += v[k];
+        }
+        if (full) {
+#pragma unroll
+            for (int k = 0; k < ITEMS; k += 4)
+                *reinterpret_cast<uint4 *>(out + base + k) = make_uint4(o[k], o[k + 1], o[k + 2], o[k + 3]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < ITEMS; ++k)
+                if (base + k < n) out[base + k] = o[k];
+        }
+        __syncthreads();
+    }
 }
 
 /* ------------------------------------------------------------------------
@@ -361,9 +418,9 @@ __global__ void __launch_bounds__(256) k_scan(const uint32_t *in, uint32_t *out,
 __device__ __forceinline__ uint32_t hit_cell(const KParams &kp, float x, float y, float z,
                                              float *phi_out, bool *bad)
 {
-    uint32_t zs = trax_sector_z(z, kp.sz_z);
+    uint32_t zs = trax_f2u(trax_floor_div(z - TRAX_MIN_Z, kp.sz_z, kp.inv_sz_z));
     const float phi = trax_atan2f(y, x);
-    uint32_t ps = trax_sector_phi(phi, kp.sz_phi);
+    uint32_t ps = trax_f2u(trax_floor_div(phi - TRAX_MIN_PHI, kp.sz_phi, kp.inv_sz_phi));
     *bad = false;
     if (zs > kp.nz) { zs = kp.nz; *bad = true; }
     if (ps > kp.nphi) { ps = kp.nphi; *bad = true; }
@@ -665,9 +722,9 @@ __device__ __forceinline__ PairWindow pair_window(const KParams &kp, uint32_t lt
     zLow = (float)(tmp < zLow) * tmp + (float)(tmp > zLow) * zLow;
     zLow -= sigmaZ;
     zHigh += sigmaZ;
-    const int32_t zl = trax_f2i(floorf((zLow - TRAX_MIN_Z) / kp.sz_z));
+    const int32_t zl = trax_f2i(trax_floor_div(zLow - TRAX_MIN_Z, kp.sz_z, kp.inv_sz_z));
     w.zLowSector = (uint32_t)(zl > 0 ? zl : 0);
-    const uint32_t zh = trax_f2u(floorf((zHigh - TRAX_MIN_Z) / kp.sz_z)) + 1u;
+    const uint32_t zh = trax_f2u(trax_floor_div(zHigh - TRAX_MIN_Z, kp.sz_z, kp.inv_sz_z)) + 1u;
     w.zHighSector = zh < kp.nz ? zh : kp.nz;
 
     const float acos_r = trax_acosf(r / (2 * minRadiusCurvature));
@@ -684,18 +741,21 @@ __device__ __forceinline__ PairWindow pair_window(const KParams &kp, uint32_t lt
     phiLow += (float)((phiLow < -TRAX_PI_F) * 2) * TRAX_PI_F;
     phiHigh -= (float)((phiHigh > TRAX_PI_F) * 2) * TRAX_PI_F;
     phiHigh += (float)((phiHigh < -TRAX_PI_F) * 2) * TRAX_PI_F;
-    w.phiLowSector = trax_f2u(floorf((phiLow - TRAX_MIN_PHI) / kp.sz_phi));
-    w.phiHighSector = trax_f2u(floorf((phiHigh - TRAX_MIN_PHI) / kp.sz_phi)) + 1u;
+    w.phiLowSector = trax_f2u(trax_floor_div(phiLow - TRAX_MIN_PHI, kp.sz_phi, kp.inv_sz_phi));
+    w.phiHighSector = trax_f2u(trax_floor_div(phiHigh - TRAX_MIN_PHI, kp.sz_phi, kp.inv_sz_phi)) + 1u;
     w.zLow = zLow; w.zHigh = zHigh; w.phiLow = phiLow; w.phiHigh = phiHigh;
     w.wrap = wrap ? 1u : 0u;
     w.ok = w.phiLowSector <= kp.nphi + 1 && w.phiHighSector <= kp.nphi + 1;
     return w;
 }
 
+/* The reference's phi acceptance (PairGeneratorBeamspot.h:213-214,
+ * TripletThetaPhiPredictor.h:209-210, :420-421).  actPhi is always a sorted hit's phi,
+ * trax_atan2f in [-pi, pi] or NaN, so its wrap-around form
+ * (lo <= phi <= pi) || (-pi <= phi <= hi) is lo <= phi || phi <= hi. */
 __device__ __forceinline__ bool phi_in(float actPhi, float phiLow, float phiHigh, uint32_t wrap)
 {
-    return (!wrap && (phiLow <= actPhi && actPhi <= phiHigh))
-        || (wrap && ((phiLow <= actPhi && actPhi <= TRAX_PI_F) || (-TRAX_PI_F <= actPhi && actPhi <= phiHigh)));
+    return wrap ? (phiLow <= actPhi || actPhi <= phiHigh) : (phiLow <= actPhi && actPhi <= phiHigh);
 }
 
 /*
@@ -891,13 +951,13 @@ __device__ __forceinline__ SectorWindow sector_window(const KParams &kp, uint32_
 {
     SectorWindow w;
     const uint32_t spreadZ = kp.spread_z[lt], spreadPhi = kp.spread_phi[lt];
-    const uint32_t zs = trax_f2u(floorf((hz - TRAX_MIN_Z) / kp.sz_z));
+    const uint32_t zs = trax_f2u(trax_floor_div(hz - TRAX_MIN_Z, kp.sz_z, kp.inv_sz_z));
     const uint32_t zh = zs + spreadZ + 1u;
     w.zHighSector = zh < kp.nz ? zh : kp.nz;
     /* max(0u, zLowSector - spreadZ) of unsigned values is the plain
      * difference: below spreadZ it wraps and no row is visited (:98) */
     w.zLowSector = zs - spreadZ;
-    int32_t lo = trax_f2i(floorf((phi - TRAX_MIN_PHI) / kp.sz_phi) - (float)spreadPhi);
+    int32_t lo = trax_f2i(trax_floor_div(phi - TRAX_MIN_PHI, kp.sz_phi, kp.inv_sz_phi) - (float)spreadPhi);
     uint32_t hi = (uint32_t)lo + 2u * spreadPhi + 1u;
     const bool wrap = lo < 0 || hi > kp.nphi + 1;
     lo = (int32_t)((uint32_t)lo + (uint32_t)(lo < 0) * kp.nphi);
@@ -1071,7 +1131,7 @@ __device__ __forceinline__ uint32_t zkey(float z)
  * hits of every indexable cell of the group together and scatters them. */
 __global__ void __launch_bounds__(256) k_zindex(const uint32_t *grid, uint32_t cells_per_event,
                                                 uint32_t zi_min, const float *Z, const float *PHI,
-                                                float2 *zi, DevState *st)
+                                                float2 *zi, uint32_t *zpos, DevState *st)
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1123,7 +1183,10 @@ __global__ void __launch_bounds__(256) k_zindex(const uint32_t *grid, uint32_t c
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             const uint32_t i = k * 32 + lane;
-            if (i < cnt) zi[a + rank[k]] = make_float2(zz[k], pp[k]);
+            if (i < cnt) {
+                zi[a + rank[k]] = make_float2(zz[k], pp[k]);
+                zpos[a + rank[k]] = a + i;
+            }
         }
         }
     }
@@ -1173,9 +1236,9 @@ __device__ __forceinline__ PredWindow pred_window(const KParams &kp, uint32_t lt
         zLow = (float)(tmp > zLow) * zLow + (float)(tmp < zLow) * tmp;
         zLow -= sigmaZ;
         zHigh += v == 0 ? sigmaPhi : sigmaZ;
-        const int32_t zl = trax_f2i(floorf((zLow - TRAX_MIN_Z) / kp.sz_z));
+        const int32_t zl = trax_f2i(trax_floor_div(zLow - TRAX_MIN_Z, kp.sz_z, kp.inv_sz_z));
         w.zLowSector[v] = (uint32_t)(zl > 0 ? zl : 0);
-        const uint32_t zh = trax_f2u(floorf((zHigh - TRAX_MIN_Z) / kp.sz_z)) + 1u;
+        const uint32_t zh = trax_f2u(trax_floor_div(zHigh - TRAX_MIN_Z, kp.sz_z, kp.inv_sz_z)) + 1u;
         w.zHighSector[v] = zh < kp.nz ? zh : kp.nz;
         w.zLow[v] = zLow;
         w.zHigh[v] = zHigh;
@@ -1197,8 +1260,8 @@ __device__ __forceinline__ PredWindow pred_window(const KParams &kp, uint32_t lt
     phiLow += (float)((phiLow < -TRAX_PI_F) * 2) * TRAX_PI_F;
     phiHigh -= (float)((phiHigh > TRAX_PI_F) * 2) * TRAX_PI_F;
     phiHigh += (float)((phiHigh < -TRAX_PI_F) * 2) * TRAX_PI_F;
-    w.phiLowSector = trax_f2u(floorf((phiLow - TRAX_MIN_PHI) / kp.sz_phi));
-    const uint32_t ph = trax_f2u(floorf((phiHigh - TRAX_MIN_PHI) / kp.sz_phi)) + 1u;
+    w.phiLowSector = trax_f2u(trax_floor_div(phiLow - TRAX_MIN_PHI, kp.sz_phi, kp.inv_sz_phi));
+    const uint32_t ph = trax_f2u(trax_floor_div(phiHigh - TRAX_MIN_PHI, kp.sz_phi, kp.inv_sz_phi)) + 1u;
     w.phiHighSector = ph < kp.nphi ? ph : kp.nphi;
     w.phiLow = phiLow;
     w.phiHigh = phiHigh;
@@ -1208,44 +1271,110 @@ __device__ __forceinline__ PredWindow pred_window(const KParams &kp, uint32_t lt
 }
 
 /*
- * Prediction in one pass.  Warp-sized tiles of 32 pairs, one pair per thread (the
- * window math is the expensive part and ~20 candidates follow per pair).
- * Consecutive pairs share their outer hit, so a warp's windows overlap and
- * its candidate loads hit the same L1 lines.  The count sweep evaluates the
- * count window (A) and the store window (B) together; a warp scan plus
- * warp-wide decoupled look-back gives each pair its position without any
- * block barrier (so no warp waits for a slower warp); the store sweep writes
- * the first min(A, B) accepts of window B, the reference's truncation.
+ * Prediction in two passes and a scan, so that no warp waits for another:
+ *   k_predict_count   one pair per thread (grid-stride): both windows, the
+ *                     count walk over layer-3 cells (window A = the
+ *                     reference's predictCount, B = predictStore), the
+ *                     emitted count min(A, B) per pair, and for every pair
+ *                     that emits a 32-byte record of its store window
+ *                     (appended with a warp-aggregated atomic, any order);
+ *   k_scan            exclusive scan of the emitted counts (pair order);
+ *   k_predict_store   one record per thread: the first `emitted` accepts of
+ *                     window B in the reference's visit order at the pair's
+ *                     scanned position.
+ * Only pairs with candidates are walked twice, and no window is recomputed.
  */
-__global__ void __launch_bounds__(256, 5) k_predict_fused(
+struct PredRec {
+    float zLow, zHigh, phiLow, phiHigh;  /* window B */
+    uint32_t pair;
+    uint32_t grid_off;                   /* layer-3 grid of the pair's event */
+    uint32_t zsec;                       /* zLowSector | zHighSector << 16 */
+    uint32_t psec;                       /* phiLowSector | phiHighSector << 16 | wrap << 31 */
+};
+
+/* Count walk of one pair: accepts of window A (cA) and B (cB). */
+__device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_t *lGrid3,
+                                                const float *Z, const float *PHI,
+                                                const float2 *zi, const PredWindow &w,
+                                                uint32_t &cA, uint32_t &cB)
+{
+    const uint32_t P1 = kp.nphi + 1;
+    cA = 0;
+    cB = 0;
+    const uint32_t zlo = min(w.zLowSector[0], w.zLowSector[1]);
+    const uint32_t zhi = max(w.zHighSector[0], w.zHighSector[1]);
+    for (uint32_t zs = zlo; zs < zhi; ++zs) {
+        const bool inA = zs >= w.zLowSector[0] && zs < w.zHighSector[0];
+        const bool inB = zs >= w.zLowSector[1] && zs < w.zHighSector[1];
+        const uint32_t kA0 = zkey(w.zLow[0]), kA1 = zkey(w.zHigh[0]);
+        const uint32_t kB0 = zkey(w.zLow[1]), kB1 = zkey(w.zHigh[1]);
+        const uint32_t keyLo = min(inA ? kA0 : 0xffffffffu, inB ? kB0 : 0xffffffffu);
+        const uint32_t keyHi = max(inA ? kA1 : 0u, inB ? kB1 : 0u);
+        const uint32_t *row = lGrid3 + zs * P1;
+        /* the reference's visits, as runs of whole cells: columns
+         * pLow..pHigh-1, or with wrap-around pLow..P then 0..pHigh-1 */
+        for (int run = 0; run < 2; ++run) {
+            const uint32_t c0 = run == 0 ? w.phiLowSector : 0u;
+            const uint32_t c1 = run == 0 ? (w.wrap ? P1 : w.phiHighSector)
+                                         : (w.wrap ? w.phiHighSector : 0u);
+            if (c1 <= c0) continue;
+            const uint32_t ra = row[c0], rb = row[c1];
+            if (rb - ra <= kp.run_walk) {
+                /* a small run: walk its contiguous hits */
+                for (uint32_t j = ra; j < rb; ++j) {
+                    const float zz = Z[j];
+                    const bool ph = phi_in(PHI[j], w.phiLow, w.phiHigh, w.wrap);
+                    cA += (inA && ph && w.zLow[0] <= zz && zz <= w.zHigh[0]) ? 1u : 0u;
+                    cB += (inB && ph && w.zLow[1] <= zz && zz <= w.zHigh[1]) ? 1u : 0u;
+                }
+                continue;
+            }
+            for (uint32_t c = c0; c < c1; ++c) {
+                const uint32_t ca = row[c], cb = row[c + 1];
+                if (cb - ca <= kp.zi_min || cb - ca > kZiMax) {
+                    for (uint32_t j = ca; j < cb; ++j) {
+                        const float zz = Z[j];
+                        const bool ph = phi_in(PHI[j], w.phiLow, w.phiHigh, w.wrap);
+                        cA += (inA && ph && w.zLow[0] <= zz && zz <= w.zHigh[0]) ? 1u : 0u;
+                        cB += (inB && ph && w.zLow[1] <= zz && zz <= w.zHigh[1]) ? 1u : 0u;
+                    }
+                    continue;
+                }
+                uint32_t lo = ca, hi = cb;
+                while (lo < hi) {
+                    const uint32_t m = (lo + hi) >> 1;
+                    if (zkey(zi[m].x) < keyLo) lo = m + 1; else hi = m;
+                }
+                for (; lo < cb; ++lo) {
+                    const float2 v = zi[lo];
+                    if (zkey(v.x) > keyHi) break;
+                    const bool ph = phi_in(v.y, w.phiLow, w.phiHigh, w.wrap);
+                    cA += (inA && ph && w.zLow[0] <= v.x && v.x <= w.zHigh[0]) ? 1u : 0u;
+                    cB += (inB && ph && w.zLow[1] <= v.x && v.x <= w.zHigh[1]) ? 1u : 0u;
+                }
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256, 5) k_predict_count(
     KParams kp, const uint32_t *grid, const float *X, const float *Y, const float *Z,
     const float *PHI, const uint32_t *EVENT, const uint32_t *LAYER, const float2 *zi,
-    const uint2 *pairs, const uint32_t *n_pairs_ptr, uint32_t pair_cap, uint32_t *cexcl,
-    uint2 *cands, uint32_t cand_cap, unsigned long long *status, DevState *st)
+    const uint2 *pairs, const uint32_t *n_pairs_ptr, uint32_t pair_cap, uint32_t *emitted_out,
+    PredRec *recs, uint32_t rec_cap, DevState *st)
 {
     const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lt_mask = lanemask_lt();
     uint32_t n = *n_pairs_ptr;
     if (n > pair_cap) n = pair_cap;
-    if (n == 0) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            cexcl[0] = 0;
-            st->n_cands = 0;
-        }
-        return;
-    }
-    const uint32_t P1 = kp.nphi + 1;
     const uint32_t E = st->n_events;
-    const uint32_t ntiles = (n + 31) / 32;
     unsigned long long my_slots = 0, my_trunc = 0;
-    for (;;) {
-        uint32_t tile = 0;
-        if (lane == 0) tile = atomicAdd(&st->tile_ctr[1], 1u);
-        tile = __shfl_sync(kFull, tile, 0);
-        if (tile >= ntiles) break;
-        const uint32_t p = tile * 32 + lane;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t p0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; p0 < n; p0 += stride) {
+        const uint32_t p = p0 + lane;
         bool live = p < n;
         PredWindow w{};
-        const uint32_t *lGrid3 = grid;
+        uint32_t goff = 0;
         if (live) {
             const uint2 pr = pairs[p];
             const uint32_t h1 = pr.x, h2 = pr.y;
@@ -1255,7 +1384,7 @@ __global__ void __launch_bounds__(256, 5) k_predict_fused(
                 set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_BAD_TRIPLET_INDEX);
                 live = false;
             } else {
-                lGrid3 = grid + ((size_t)event * kp.n_layers + (kp.l3[lt] - 1)) * kp.C;
+                goff = (event * kp.n_layers + (kp.l3[lt] - 1)) * kp.C;
                 w = pred_window(kp, lt, X[h1], Y[h1], Z[h1], X[h2], Y[h2], Z[h2], PHI[h1],
                                 PHI[h2]);
                 if (!w.ok) {
@@ -1266,124 +1395,30 @@ __global__ void __launch_bounds__(256, 5) k_predict_fused(
         }
         uint32_t emitted = 0;
         if (live) {
-            uint32_t cA = 0, cB = 0;
-            const uint32_t zlo = min(w.zLowSector[0], w.zLowSector[1]);
-            const uint32_t zhi = max(w.zHighSector[0], w.zHighSector[1]);
-            for (uint32_t zs = zlo; zs < zhi; ++zs) {
-                const bool inA = zs >= w.zLowSector[0] && zs < w.zHighSector[0];
-                const bool inB = zs >= w.zLowSector[1] && zs < w.zHighSector[1];
-                const uint32_t kA0 = zkey(w.zLow[0]), kA1 = zkey(w.zHigh[0]);
-                const uint32_t kB0 = zkey(w.zLow[1]), kB1 = zkey(w.zHigh[1]);
-                const uint32_t keyLo = min(inA ? kA0 : 0xffffffffu, inB ? kB0 : 0xffffffffu);
-                const uint32_t keyHi = max(inA ? kA1 : 0u, inB ? kB1 : 0u);
-                const uint32_t *row = lGrid3 + zs * P1;
-                /* the reference's visits, as runs of whole cells: columns
-                 * pLow..pHigh-1, or with wrap-around pLow..P then 0..pHigh-1 */
-                for (int run = 0; run < 2; ++run) {
-                    const uint32_t c0 = run == 0 ? w.phiLowSector : 0u;
-                    const uint32_t c1 = run == 0 ? (w.wrap ? P1 : w.phiHighSector)
-                                                 : (w.wrap ? w.phiHighSector : 0u);
-                    if (c1 <= c0) continue;
-                    const uint32_t ra = row[c0], rb = row[c1];
-                    if (rb - ra <= kp.run_walk) {
-                        /* a small run: walk its contiguous hits */
-                        for (uint32_t j = ra; j < rb; ++j) {
-                            const float zz = Z[j];
-                            const bool ph = phi_in(PHI[j], w.phiLow, w.phiHigh, w.wrap);
-                            cA += (inA && ph && w.zLow[0] <= zz && zz <= w.zHigh[0]) ? 1u : 0u;
-                            cB += (inB && ph && w.zLow[1] <= zz && zz <= w.zHigh[1]) ? 1u : 0u;
-                        }
-                        continue;
-                    }
-                    for (uint32_t c = c0; c < c1; ++c) {
-                        const uint32_t ca = row[c], cb = row[c + 1];
-                        if (cb - ca <= kp.zi_min || cb - ca > kZiMax) {
-                            for (uint32_t j = ca; j < cb; ++j) {
-                                const float zz = Z[j];
-                                const bool ph = phi_in(PHI[j], w.phiLow, w.phiHigh, w.wrap);
-                                cA += (inA && ph && w.zLow[0] <= zz && zz <= w.zHigh[0]) ? 1u : 0u;
-                                cB += (inB && ph && w.zLow[1] <= zz && zz <= w.zHigh[1]) ? 1u : 0u;
-                            }
-                            continue;
-                        }
-                        uint32_t lo = ca, hi = cb;
-                        while (lo < hi) {
-                            const uint32_t m = (lo + hi) >> 1;
-                            if (zkey(zi[m].x) < keyLo) lo = m + 1; else hi = m;
-                        }
-                        for (; lo < cb; ++lo) {
-                            const float2 v = zi[lo];
-                            if (zkey(v.x) > keyHi) break;
-                            const bool ph = phi_in(v.y, w.phiLow, w.phiHigh, w.wrap);
-                            cA += (inA && ph && w.zLow[0] <= v.x && v.x <= w.zHigh[0]) ? 1u : 0u;
-                            cB += (inB && ph && w.zLow[1] <= v.x && v.x <= w.zHigh[1]) ? 1u : 0u;
-                        }
-                    }
-                }
-            }
+            uint32_t cA, cB;
+            pred_count_walk(kp, grid + goff, Z, PHI, zi, w, cA, cB);
             emitted = cA < cB ? cA : cB;
             my_slots += cA;
             my_trunc += cB - emitted;
         }
-        uint32_t tile_end;
-        const uint32_t pos = warp_tile_position(emitted, tile, status, st, &tile_end);
-        if (p < n) cexcl[p] = pos;
-        if (tile == ntiles - 1 && lane == 0) {
-            cexcl[n] = tile_end;
-            st->n_cands = tile_end;
-        }
+        if (p < n) emitted_out[p] = emitted;
+        const uint32_t want = __ballot_sync(kFull, emitted != 0);
+        uint32_t base = 0;
+        if (lane == 0 && want) base = atomicAdd(&st->n_prec, (uint32_t)__popc(want));
+        base = __shfl_sync(kFull, base, 0);
         if (emitted) {
-            /* the first `emitted` accepts of window B in the reference's
-             * visit order: cells in run order, hits of a cell by position;
-             * the index only tells which cells hold accepts */
-            uint32_t written = 0;
-            const uint32_t kB0 = zkey(w.zLow[1]), kB1 = zkey(w.zHigh[1]);
-            for (uint32_t zs = w.zLowSector[1]; zs < w.zHighSector[1] && written < emitted; ++zs) {
-                const uint32_t *row = lGrid3 + zs * P1;
-                for (int run = 0; run < 2 && written < emitted; ++run) {
-                    const uint32_t c0 = run == 0 ? w.phiLowSector : 0u;
-                    const uint32_t c1 = run == 0 ? (w.wrap ? P1 : w.phiHighSector)
-                                                 : (w.wrap ? w.phiHighSector : 0u);
-                    if (c1 <= c0) continue;
-                    const uint32_t ra = row[c0], rb = row[c1];
-                    if (rb - ra <= kp.run_walk) {
-                        for (uint32_t j = ra; j < rb && written < emitted; ++j) {
-                            const float zz = Z[j];
-                            if (w.zLow[1] <= zz && zz <= w.zHigh[1] &&
-                                phi_in(PHI[j], w.phiLow, w.phiHigh, w.wrap)) {
-                                if (pos + written < cand_cap) cands[pos + written] = make_uint2(p, j);
-                                ++written;
-                            }
-                        }
-                        continue;
-                    }
-                    for (uint32_t c = c0; c < c1 && written < emitted; ++c) {
-                        const uint32_t ca = row[c], cb = row[c + 1];
-                        if (cb - ca > kp.zi_min && cb - ca <= kZiMax) {
-                            uint32_t lo = ca, hi = cb;
-                            while (lo < hi) {
-                                const uint32_t m = (lo + hi) >> 1;
-                                if (zkey(zi[m].x) < kB0) lo = m + 1; else hi = m;
-                            }
-                            bool any = false;
-                            for (; lo < cb && !any; ++lo) {
-                                const float2 v = zi[lo];
-                                if (zkey(v.x) > kB1) break;
-                                any = w.zLow[1] <= v.x && v.x <= w.zHigh[1] &&
-                                      phi_in(v.y, w.phiLow, w.phiHigh, w.wrap);
-                            }
-                            if (!any) continue;
-                        }
-                        for (uint32_t j = ca; j < cb && written < emitted; ++j) {
-                            const float zz = Z[j];
-                            if (w.zLow[1] <= zz && zz <= w.zHigh[1] &&
-                                phi_in(PHI[j], w.phiLow, w.phiHigh, w.wrap)) {
-                                if (pos + written < cand_cap) cands[pos + written] = make_uint2(p, j);
-                                ++written;
-                            }
-                        }
-                    }
-                }
+            const uint32_t r = base + __popc(want & lt_mask);
+            if (r < rec_cap) {
+                PredRec rec;
+                rec.zLow = w.zLow[1];
+                rec.zHigh = w.zHigh[1];
+                rec.phiLow = w.phiLow;
+                rec.phiHigh = w.phiHigh;
+                rec.pair = p;
+                rec.grid_off = goff;
+                rec.zsec = w.zLowSector[1] | (w.zHighSector[1] << 16);
+                rec.psec = w.phiLowSector | (w.phiHighSector << 16) | (w.wrap << 31);
+                recs[r] = rec;
             }
         }
     }
@@ -1392,13 +1427,103 @@ __global__ void __launch_bounds__(256, 5) k_predict_fused(
         my_slots += __shfl_down_sync(kFull, my_slots, d);
         my_trunc += __shfl_down_sync(kFull, my_trunc, d);
     }
-    if ((threadIdx.x & 31) == 0 && (my_slots | my_trunc)) {
+    if (lane == 0 && (my_slots | my_trunc)) {
         atomicAdd(&st->cand_slots, my_slots);
         atomicAdd(&st->cand_truncated, my_trunc);
     }
 }
 
-/* cand_offsets[g+1] = candidates before the first pair of group g+1. */
+__global__ void __launch_bounds__(256) k_predict_store(
+    KParams kp, const uint32_t *grid, const float *Z, const float *PHI, const float2 *zi,
+    const uint32_t *zpos, const PredRec *recs, uint32_t rec_cap, const uint32_t *cexcl, const uint32_t *n_pairs_ptr,
+    uint32_t pair_cap, const uint32_t *total_ptr, uint2 *cands, uint32_t cand_cap,
+    DevState *st)
+{
+    uint32_t nrec = st->n_prec;
+    if (nrec > rec_cap) nrec = rec_cap;
+    uint32_t n = *n_pairs_ptr;
+    if (n > pair_cap) n = pair_cap;
+    const uint32_t P1 = kp.nphi + 1;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < nrec; r += gridDim.x * blockDim.x) {
+        const PredRec rec = recs[r];
+        const uint32_t p = rec.pair;
+        if (p >= n) continue;
+        const uint32_t pos = cexcl[p];
+        const uint32_t emitted = (p + 1 < n ? cexcl[p + 1] : *total_ptr) - pos;
+        const uint32_t *lGrid3 = grid + rec.grid_off;
+        const uint32_t zLowSector = rec.zsec & 0xffffu, zHighSector = rec.zsec >> 16;
+        const uint32_t phiLowSector = rec.psec & 0xffffu;
+        const uint32_t phiHighSector = (rec.psec >> 16) & 0x7fffu;
+        const uint32_t wrap = rec.psec >> 31;
+        const uint32_t kB0 = zkey(rec.zLow), kB1 = zkey(rec.zHigh);
+        /* the first `emitted` accepts of window B in the reference's visit
+         * order: cells in run order, hits of a cell by position.  An indexed
+         * cell yields its accepts from the z range of the index, smallest
+         * position first (selection over the few hits in that range). */
+        uint32_t written = 0;
+        for (uint32_t zs = zLowSector; zs < zHighSector && written < emitted; ++zs) {
+            const uint32_t *row = lGrid3 + zs * P1;
+            for (int run = 0; run < 2 && written < emitted; ++run) {
+                const uint32_t c0 = run == 0 ? phiLowSector : 0u;
+                const uint32_t c1 = run == 0 ? (wrap ? P1 : phiHighSector) : (wrap ? phiHighSector : 0u);
+                if (c1 <= c0) continue;
+                const uint32_t ra = row[c0], rb = row[c1];
+                if (rb - ra <= kp.run_walk) {
+                    for (uint32_t j = ra; j < rb && written < emitted; ++j) {
+                        const float zz = Z[j];
+                        if (rec.zLow <= zz && zz <= rec.zHigh &&
+                            phi_in(PHI[j], rec.phiLow, rec.phiHigh, wrap)) {
+                            if (pos + written < cand_cap) cands[pos + written] = make_uint2(p, j);
+                            ++written;
+                        }
+                    }
+                    continue;
+                }
+                for (uint32_t c = c0; c < c1 && written < emitted; ++c) {
+                    const uint32_t ca = row[c], cb = row[c + 1];
+                    if (cb - ca > kp.zi_min && cb - ca <= kZiMax) {
+                        uint32_t lo = ca, hi = cb;
+                        while (lo < hi) {
+                            const uint32_t m = (lo + hi) >> 1;
+                            if (zkey(zi[m].x) < kB0) lo = m + 1; else hi = m;
+                        }
+                        uint32_t last = 0;
+                        bool first = true;
+                        while (written < emitted) {
+                            uint32_t best = 0xffffffffu;
+                            for (uint32_t q = lo; q < cb; ++q) {
+                                const float2 v = zi[q];
+                                if (zkey(v.x) > kB1) break;
+                                if (rec.zLow <= v.x && v.x <= rec.zHigh &&
+                                    phi_in(v.y, rec.phiLow, rec.phiHigh, wrap)) {
+                                    const uint32_t j = zpos[q];
+                                    if ((first || j > last) && j < best) best = j;
+                                }
+                            }
+                            if (best == 0xffffffffu) break;
+                            if (pos + written < cand_cap) cands[pos + written] = make_uint2(p, best);
+                            ++written;
+                            last = best;
+                            first = false;
+                        }
+                        continue;
+                    }
+                    for (uint32_t j = ca; j < cb && written < emitted; ++j) {
+                        const float zz = Z[j];
+                        if (rec.zLow <= zz && zz <= rec.zHigh &&
+                            phi_in(PHI[j], rec.phiLow, rec.phiHigh, wrap)) {
+                            if (pos + written < cand_cap) cands[pos + written] = make_uint2(p, j);
+                            ++written;
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+/* cand_offsets[g+1] = candidates before the first pair of group g+1
+ * (cexcl holds the exclusive prefix of n pairs; the total is *total). */
 __global__ void k_cand_offsets(const uint32_t *pair_offsets, const uint32_t *cexcl,
                                uint32_t *cand_offsets, uint32_t n_lt, uint32_t pair_cap,
                                const uint32_t *total, uint32_t cap, DevState *st)
@@ -1409,7 +1534,7 @@ __global__ void k_cand_offsets(const uint32_t *pair_offsets, const uint32_t *cex
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g <= G; g += gridDim.x * blockDim.x) {
         uint32_t q = pair_offsets[g];
         if (q > n) q = n;
-        cand_offsets[g] = g == 0 ? 0u : cexcl[q];
+        cand_offsets[g] = g == 0 ? 0u : (q >= n ? *total : cexcl[q]);
         if (g == G && *total > cap) set_fault(st, TRAX_ERR_CAPACITY, TRAX_DETAIL_CAND_CAPACITY);
     }
 }

@@ -175,6 +175,25 @@ TRAX_HD uint32_t trax_sector_phi(float phi, float sector_size_phi)
     return trax_f2u(floorf((phi - TRAX_MIN_PHI) / sector_size_phi));
 }
 
+/*
+ * floorf(x / d) for a finite d > 0, from a multiply by inv_d = 1.0f / d
+ * (IEEE, computed once).  The rounded quotient RN(x / d) and q = x * inv_d
+ * are both within 2^-24 (1 + 2^-24)^2 relative of the exact x / d, so they
+ * differ by less than 1.5 * 2^-23 |q| as long as nothing is subnormal; when
+ * q lies more than 2^-20 |q| from every integer, both have the same floor.
+ * Otherwise (and for NaN, inf, |q| >= 2^22 and |q| < 2^-64) the division
+ * itself is done, so the result is always floorf(x / d) bit for bit.
+ */
+TRAX_HD float trax_floor_div(float x, float d, float inv_d)
+{
+    const float q = x * inv_d;
+    const float f = floorf(q);
+    const float aq = fabsf(q);
+    const float tol = aq * 0x1p-20f;
+    if (aq < 0x1p22f && aq >= 0x1p-64f && q - f > tol && (f + 1.0f) - q > tol) return f;
+    return floorf(x / d);
+}
+
 /* GridConfig::sectorSizeZ/Phi (Grid.h:9-15), evaluated in float. */
 TRAX_HD float trax_sector_size_z(uint32_t n_sectors_z)
 {
