@@ -64,6 +64,7 @@ struct trax_ctx {
     DevBuf phys;  /* physics evaluation scratch */
     DevBuf prec;  /* prediction store records */
     DevBuf zp;    /* input position of each z-index entry */
+    DevBuf ptile; /* prediction tile totals / prefixes */
     cudaEvent_t timers[kTimerSlots] = {};
     int blk_pair = 0, blk_sector = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
 
@@ -328,11 +329,14 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
     const KParams &kp = ctx->kp;
     trax_status s;
     if ((s = ensure(ctx, ctx->cexcl, (size_t)(pair_cap + 1) * 4)) != TRAX_OK) return s;
-    const uint32_t ntile = tiles_for(pair_cap, kScanItems * kScanThreads);
+    const uint32_t ptiles = tiles_for(pair_cap, 32) + 1;
+    const uint32_t ntile = tiles_for(ptiles, kScanItems * kScanThreads);
     if ((s = ensure(ctx, ctx->st1, (size_t)ntile * 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->ptile, (size_t)ptiles * 4)) != TRAX_OK) return s;
     const uint32_t rec_cap = cand_cap ? cand_cap : 1;
     if ((s = ensure(ctx, ctx->prec, (size_t)rec_cap * sizeof(PredRec))) != TRAX_OK) return s;
     uint32_t *cexcl = (uint32_t *)ctx->cexcl.p;
+    uint32_t *ptile = (uint32_t *)ctx->ptile.p;
     PredRec *recs = (PredRec *)ctx->prec.p;
     DevState *st = ctx->d_state;
     /* the pair total is st->n_pairs: written by the pair stage, or copied
@@ -340,21 +344,20 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
     CK(cudaMemsetAsync(&st->n_prec, 0, 4, ctx->stream));
     k_predict_count<<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
         kp, grid, h.x, h.y, h.z, h.phi, h.event, h.layer, (const float2 *)ctx->zi.p, pairs,
-        &st->n_pairs, pair_cap, cexcl, recs, rec_cap, st);
+        &st->n_pairs, pair_cap, cexcl, ptile, recs, rec_cap, st);
     if ((s = mark(ctx, "predict")) != TRAX_OK) return s;
     CK(cudaMemsetAsync(&st->tile_ctr[1], 0, 4, ctx->stream));
     CK(cudaMemsetAsync(ctx->st1.p, 0, (size_t)ntile * 8, ctx->stream));
-    k_scan<kScanItems><<<ctx->blk_scan, kScanThreads, 0, ctx->stream>>>(
-        cexcl, cexcl, &st->n_pairs, pair_cap, &st->n_cands, 1, (unsigned long long *)ctx->st1.p, st);
+    k_scan<kScanItems><<<std::min<uint32_t>(ctx->blk_scan, ntile), kScanThreads, 0, ctx->stream>>>(
+        ptile, ptile, &st->n_ptile, ptiles, &st->n_cands, 1, (unsigned long long *)ctx->st1.p, st);
     if ((s = mark(ctx, "predict_scan")) != TRAX_OK) return s;
     k_predict_store<<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
         kp, grid, h.z, h.phi, (const float2 *)ctx->zi.p, (const uint32_t *)ctx->zp.p, recs,
-        rec_cap, cexcl, &st->n_pairs,
-        pair_cap, &st->n_cands, cands, cand_cap, st);
+        rec_cap, cexcl, ptile, &st->n_pairs, pair_cap, &st->n_cands, cands, cand_cap, st);
     if ((s = mark(ctx, "predict_store")) != TRAX_OK) return s;
-    k_cand_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(pair_offsets, cexcl, cand_offsets,
-                                                            kp.n_lt, pair_cap, &st->n_cands,
-                                                            cand_cap, st);
+    k_cand_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(pair_offsets, cexcl, ptile,
+                                                            cand_offsets, kp.n_lt, pair_cap,
+                                                            &st->n_cands, cand_cap, st);
     CK(cudaGetLastError());
     return mark(ctx, "predict_offsets");
 }
@@ -643,7 +646,7 @@ void trax_ctx_destroy(trax_ctx *ctx)
                       &ctx->cexcl, &ctx->st0, &ctx->st1, &ctx->st2, &ctx->st3, &ctx->zi,
                       &ctx->conn_keys, &ctx->conn_sums, &ctx->grid_buf,
                       &ctx->pairs_buf, &ctx->pair_off, &ctx->cands_buf, &ctx->cand_off, &ctx->trk_off,
-                      &ctx->r_seg};
+                      &ctx->r_seg, &ctx->ing, &ctx->phys, &ctx->prec, &ctx->zp, &ctx->ptile};
     for (DevBuf *b : bufs) if (b->p) cudaFree(b->p);
     for (auto &b : ctx->in_cols) if (b.p) cudaFree(b.p);
     for (auto &b : ctx->srt_cols) if (b.p) cudaFree(b.p);
@@ -1286,7 +1289,8 @@ trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers
     if ((s = ensure(ctx, ctx->pexcl, (slot_cap + 1) * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->st0, (size_t)tiles_for((uint32_t)slot_cap, kTileItems) * 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->cexcl, (size_t)(max_pairs + 1) * 4)) != TRAX_OK) return s;
-    if ((s = ensure(ctx, ctx->st1, (size_t)tiles_for(max_pairs, kScanItems * kScanThreads) * 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->st1, (size_t)tiles_for(tiles_for(max_pairs, 32) + 1, kScanItems * kScanThreads) * 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->ptile, (size_t)(tiles_for(max_pairs, 32) + 1) * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->prec, (size_t)(max_candidates ? max_candidates : 1) * sizeof(PredRec))) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->st2, (size_t)tiles_for(max_candidates, 256 * kFilterItems) * 8)) != TRAX_OK) return s;
     if ((s = ensure_stage(ctx, (size_t)max_events * max_layers * 2 + 4)) != TRAX_OK) return s;

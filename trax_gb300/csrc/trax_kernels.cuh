@@ -64,7 +64,8 @@ struct DevState {
     uint32_t tile_ctr[4];    /* decoupled look-back tile tickets */
     uint32_t aux_n;          /* element count of a standalone prefix sum */
     uint32_t n_prec;         /* prediction store records */
-    uint32_t pad[2];
+    uint32_t n_ptile;        /* 32-pair tiles of the prediction count pass */
+    uint32_t pad[1];
 };
 
 struct SortedCols {
@@ -1094,7 +1095,7 @@ __global__ void k_group_offsets(const uint32_t *g_base, const uint32_t *excl, ui
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g <= G; g += gridDim.x * blockDim.x) {
         uint32_t q = g_base[g];
         if (q > n) q = n;
-        offsets[g] = g == 0 ? 0u : excl[q];
+        offsets[g] = g == 0 ? 0u : (q >= n ? *total : excl[q]);
         if (g == G && *total > cap) set_fault(st, TRAX_ERR_CAPACITY, detail);
     }
 }
@@ -1275,13 +1276,14 @@ __device__ __forceinline__ PredWindow pred_window(const KParams &kp, uint32_t lt
  *   k_predict_count   one pair per thread (grid-stride): both windows, the
  *                     count walk over layer-3 cells (window A = the
  *                     reference's predictCount, B = predictStore), the
- *                     emitted count min(A, B) per pair, and for every pair
- *                     that emits a 32-byte record of its store window
- *                     (appended with a warp-aggregated atomic, any order);
- *   k_scan            exclusive scan of the emitted counts (pair order);
+ *                     emitted count min(A, B) per pair, its exclusive prefix
+ *                     within the pair's 32-pair tile and the tile's total,
+ *                     and for every pair that emits a 32-byte record of its
+ *                     store window (warp-aggregated atomic append, any order);
+ *   k_scan            exclusive scan of the tile totals (pair order);
  *   k_predict_store   one record per thread: the first `emitted` accepts of
  *                     window B in the reference's visit order at the pair's
- *                     scanned position.
+ *                     position (tile prefix + in-tile prefix).
  * Only pairs with candidates are walked twice, and no window is recomputed.
  */
 struct PredRec {
@@ -1360,14 +1362,15 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
 __global__ void __launch_bounds__(256, 5) k_predict_count(
     KParams kp, const uint32_t *grid, const float *X, const float *Y, const float *Z,
     const float *PHI, const uint32_t *EVENT, const uint32_t *LAYER, const float2 *zi,
-    const uint2 *pairs, const uint32_t *n_pairs_ptr, uint32_t pair_cap, uint32_t *emitted_out,
-    PredRec *recs, uint32_t rec_cap, DevState *st)
+    const uint2 *pairs, const uint32_t *n_pairs_ptr, uint32_t pair_cap, uint32_t *in_tile,
+    uint32_t *tile_sum, PredRec *recs, uint32_t rec_cap, DevState *st)
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt_mask = lanemask_lt();
     uint32_t n = *n_pairs_ptr;
     if (n > pair_cap) n = pair_cap;
     const uint32_t E = st->n_events;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->n_ptile = (n + 31) / 32;
     unsigned long long my_slots = 0, my_trunc = 0;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t p0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; p0 < n; p0 += stride) {
@@ -1401,7 +1404,14 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
             my_slots += cA;
             my_trunc += cB - emitted;
         }
-        if (p < n) emitted_out[p] = emitted;
+        uint32_t incl = emitted;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFull, incl, d);
+            if (lane >= (uint32_t)d) incl += y;
+        }
+        if (p < n) in_tile[p] = incl - emitted;
+        if (lane == 31) tile_sum[p0 >> 5] = incl;
         const uint32_t want = __ballot_sync(kFull, emitted != 0);
         uint32_t base = 0;
         if (lane == 0 && want) base = atomicAdd(&st->n_prec, (uint32_t)__popc(want));
@@ -1435,9 +1445,9 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
 
 __global__ void __launch_bounds__(256) k_predict_store(
     KParams kp, const uint32_t *grid, const float *Z, const float *PHI, const float2 *zi,
-    const uint32_t *zpos, const PredRec *recs, uint32_t rec_cap, const uint32_t *cexcl, const uint32_t *n_pairs_ptr,
-    uint32_t pair_cap, const uint32_t *total_ptr, uint2 *cands, uint32_t cand_cap,
-    DevState *st)
+    const uint32_t *zpos, const PredRec *recs, uint32_t rec_cap, const uint32_t *in_tile,
+    const uint32_t *tile_prefix, const uint32_t *n_pairs_ptr, uint32_t pair_cap,
+    const uint32_t *total_ptr, uint2 *cands, uint32_t cand_cap, DevState *st)
 {
     uint32_t nrec = st->n_prec;
     if (nrec > rec_cap) nrec = rec_cap;
@@ -1448,8 +1458,9 @@ __global__ void __launch_bounds__(256) k_predict_store(
         const PredRec rec = recs[r];
         const uint32_t p = rec.pair;
         if (p >= n) continue;
-        const uint32_t pos = cexcl[p];
-        const uint32_t emitted = (p + 1 < n ? cexcl[p + 1] : *total_ptr) - pos;
+        const uint32_t pos = tile_prefix[p >> 5] + in_tile[p];
+        const uint32_t emitted =
+            (p + 1 < n ? tile_prefix[(p + 1) >> 5] + in_tile[p + 1] : *total_ptr) - pos;
         const uint32_t *lGrid3 = grid + rec.grid_off;
         const uint32_t zLowSector = rec.zsec & 0xffffu, zHighSector = rec.zsec >> 16;
         const uint32_t phiLowSector = rec.psec & 0xffffu;
@@ -1522,11 +1533,12 @@ __global__ void __launch_bounds__(256) k_predict_store(
     }
 }
 
-/* cand_offsets[g+1] = candidates before the first pair of group g+1
- * (cexcl holds the exclusive prefix of n pairs; the total is *total). */
-__global__ void k_cand_offsets(const uint32_t *pair_offsets, const uint32_t *cexcl,
-                               uint32_t *cand_offsets, uint32_t n_lt, uint32_t pair_cap,
-                               const uint32_t *total, uint32_t cap, DevState *st)
+/* cand_offsets[g+1] = candidates before the first pair of group g+1: the
+ * pair's tile prefix plus its in-tile prefix (the total past the last pair). */
+__global__ void k_cand_offsets(const uint32_t *pair_offsets, const uint32_t *in_tile,
+                               const uint32_t *tile_prefix, uint32_t *cand_offsets,
+                               uint32_t n_lt, uint32_t pair_cap, const uint32_t *total,
+                               uint32_t cap, DevState *st)
 {
     const uint32_t G = st->n_events * n_lt;
     uint32_t n = st->n_pairs;
@@ -1534,7 +1546,7 @@ __global__ void k_cand_offsets(const uint32_t *pair_offsets, const uint32_t *cex
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g <= G; g += gridDim.x * blockDim.x) {
         uint32_t q = pair_offsets[g];
         if (q > n) q = n;
-        cand_offsets[g] = g == 0 ? 0u : (q >= n ? *total : cexcl[q]);
+        cand_offsets[g] = g == 0 ? 0u : (q >= n ? *total : tile_prefix[q >> 5] + in_tile[q]);
         if (g == G && *total > cap) set_fault(st, TRAX_ERR_CAPACITY, TRAX_DETAIL_CAND_CAPACITY);
     }
 }
