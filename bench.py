@@ -182,9 +182,16 @@ def algorithmic_bytes(kernel, b, w, counts):
     n2 = sum(int(ln[:, cfg.triplets[t].layer2 - 1].sum()) for t in range(cfg.n_layer_triplets))
     n3 = sum(int(ln[:, cfg.triplets[t].layer3 - 1].sum()) for t in range(cfg.n_layer_triplets))
     table = {
+        # x, y, z read for the cells, 7 columns read and written, the grid
         "grid_build": N * (12 + 28 + 28) + E * L * C * 4 * 3,
+        # both layers' hits once, the per-outer-hit counts, the pairs
         "pair_gen": 12 * (n1 + n2) + 4 * n2 * 2 + 8 * M,
-        "predict": M * (8 + 24) + 12 * n3 + 4 * M * 2 + 8 * K,
+        # count pass: the pairs and their hits, the layer-3 hits, a count per pair
+        "predict": M * (8 + 24) + 12 * n3 + 4 * M,
+        # scan of the 32-pair tile totals
+        "predict_scan": 8 * ((M + 31) // 32),
+        # store pass: a position per pair read, the candidates written
+        "predict_store": 4 * M + 8 * K,
         "filter": K * (8 + 8 + 36) + 4 * ((K + 31) // 32) * 3 + 12 * R,
     }
     return table.get(kernel)
