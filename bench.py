@@ -423,8 +423,8 @@ def run_ours(args, dist):
     # ---- result-neutral walk tuning on the resident batch ------------------
     from trax_gb300.autotune import tune_walk
     best_walk, walk_ms = tune_walk(ctx, p, b, reps=3)
-    tuning = {"run_walk": best_walk[0], "index_min": best_walk[1],
-              "candidates_ms": {f"{k[0]}/{k[1]}": round(v, 4) for k, v in walk_ms.items()}}
+    tuning = {"run_walk": best_walk[0], "index_min": best_walk[1], "pair_record": best_walk[2],
+              "candidates_ms": {"/".join(map(str, k)): round(v, 4) for k, v in walk_ms.items()}}
 
     # ---- device-resident value: graph replay on staged inputs -------------
     p.stage(b)

@@ -198,11 +198,14 @@ float trax_min_radius_curvature(float min_pt, float bz);
  * never depend on it, only speed: a run of neighbouring cells with at most
  * run_walk hits is walked hit by hit; in larger runs, every cell with more
  * than index_min (<= 256) hits is searched through a per-cell z index.
- * Sparse events favour walking, dense (pile-up) events the index.
- * trax_configure installs run_walk 48, index_min 16. */
+ * pair_record 1 makes the pair stage keep its count sweep's ballots and
+ * replay them for the store, 0 sweeps twice.  Sparse events favour walking
+ * and recording, dense (pile-up) events the index and the double sweep.
+ * trax_configure installs run_walk 48, index_min 16, pair_record 1. */
 typedef struct trax_tuning {
     uint32_t run_walk;
     uint32_t index_min;
+    uint32_t pair_record;
 } trax_tuning;
 trax_status trax_set_tuning(trax_ctx *ctx, const trax_tuning *t);
 

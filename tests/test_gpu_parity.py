@@ -213,8 +213,9 @@ def test_tuning_does_not_change_results(gpu_ctx):
                  8 * b.n_hits)
     outs = []
     try:
-        for walk, imin in ((0, 0), (0, 16), (48, 16), (96, 32), (1 << 30, 256)):
-            gpu_ctx.set_tuning(walk, imin)
+        for walk, imin, rec in ((0, 0, 1), (0, 16, 0), (48, 16, 1), (96, 32, 0),
+                                (1 << 30, 256, 1), (1 << 30, 256, 0)):
+            gpu_ctx.set_tuning(walk, imin, rec)
             trk, off, counts = p.seed(b)
             assert counts["status"] == 0
             outs.append(trk)

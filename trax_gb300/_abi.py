@@ -38,7 +38,8 @@ class TraxConfig(C.Structure):
 
 
 class TraxTuning(C.Structure):
-    _fields_ = [("run_walk", C.c_uint32), ("index_min", C.c_uint32)]
+    _fields_ = [("run_walk", C.c_uint32), ("index_min", C.c_uint32),
+                ("pair_record", C.c_uint32)]
 
 
 class TraxHits(C.Structure):

@@ -2,9 +2,9 @@
 
 Two knobs, tuned differently:
 - how the candidate kernels visit a window (trax_set_tuning: walk runs of
-  cells or search a per-cell z index).  Results never depend on it, so
-  tune_walk() simply times the candidates on the resident batch and keeps the
-  fastest.
+  cells or search a per-cell z index; replay the pair stage's count ballots or
+  sweep twice).  Results never depend on it, so tune_walk() simply times the
+  candidates on the resident batch and keeps the fastest.
 - the grid granularity (z bins x phi bins).  It changes which candidates the
   reference visits first and therefore its truncation, so a tuned grid is a
   different (but equally reference-defined) configuration; sweep_grids()
@@ -42,12 +42,17 @@ def time_staged(ctx: Context, p: Pipeline, reps: int) -> float:
 
 def tune_walk(ctx: Context, p: Pipeline, batch: gen.EventBatch, reps=5,
               candidates=WALK_CANDIDATES):
-    """Stages `batch`, times each (run_walk, index_min) and installs the best."""
+    """Stages `batch`, times each (run_walk, index_min) with the pair stage
+    replaying its ballots, then the best of them with the pair stage sweeping
+    twice, and installs the fastest (run_walk, index_min, pair_record)."""
     p.stage(batch)
     timings = {}
     for cand in candidates:
-        ctx.set_tuning(*cand)
-        timings[cand] = time_staged(ctx, p, reps)
+        ctx.set_tuning(*cand, 1)
+        timings[(*cand, 1)] = time_staged(ctx, p, reps)
+    best = min(timings, key=timings.get)
+    ctx.set_tuning(best[0], best[1], 0)
+    timings[(best[0], best[1], 0)] = time_staged(ctx, p, reps)
     best = min(timings, key=timings.get)
     ctx.set_tuning(*best)
     return best, timings

@@ -32,7 +32,6 @@ constexpr int kScanItems = 8;       /* items per thread in k_scan */
 constexpr int kScanThreads = 256;
 constexpr int kFilterItems = 4;
 constexpr int kTileItems = 32;      /* items per fused pair / predict tile (one warp) */
-constexpr int kFusedThreads = 256;  /* threads per block of the fused kernels */
 constexpr uint32_t kDefaultRunWalk = 48;  /* see trax_set_tuning */
 constexpr uint32_t kDefaultIndexMin = 16;
 
@@ -66,7 +65,7 @@ struct trax_ctx {
     DevBuf zp;    /* input position of each z-index entry */
     DevBuf ptile; /* prediction tile totals / prefixes */
     cudaEvent_t timers[kTimerSlots] = {};
-    int blk_pair = 0, blk_sector = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
+    int blk_pair = 0, blk_pair0 = 0, blk_sector = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
 
     /* batched pipeline */
     bool reserved = false;
@@ -294,8 +293,12 @@ trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *gr
         k_pair_sector<<<ctx->blk_sector, kFusedThreads, 0, ctx->stream>>>(
             kp, grid, h.z, h.phi, slots, slot_cap, pexcl, pairs, pair_cap,
             (unsigned long long *)ctx->st0.p, st);
+    else if (kp.pair_record)
+        k_pair_fused<true><<<ctx->blk_pair, kFusedThreads, 0, ctx->stream>>>(
+            kp, grid, h.x, h.y, h.z, h.phi, slots, slot_cap, pexcl, pairs, pair_cap,
+            (unsigned long long *)ctx->st0.p, st);
     else
-        k_pair_fused<<<ctx->blk_pair, kFusedThreads, 0, ctx->stream>>>(
+        k_pair_fused<false><<<ctx->blk_pair0, kFusedThreads, 0, ctx->stream>>>(
             kp, grid, h.x, h.y, h.z, h.phi, slots, slot_cap, pexcl, pairs, pair_cap,
             (unsigned long long *)ctx->st0.p, st);
     if ((s = mark(ctx, "pair_gen")) != TRAX_OK) return s;
@@ -620,8 +623,10 @@ trax_status trax_ctx_create(trax_ctx **out, int device)
     if ((e = cudaFuncSetAttribute(k_grid_build, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)ctx->smem_optin)) != cudaSuccess) return bail(e);
     int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_fused, kFusedThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_fused<true>, kFusedThreads, 0);
     ctx->blk_pair = ctx->sm_count * std::max(b, 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_fused<false>, kFusedThreads, 0);
+    ctx->blk_pair0 = ctx->sm_count * std::max(b, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_sector, kFusedThreads, 0);
     ctx->blk_sector = ctx->sm_count * std::max(b, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_predict_count, kFusedThreads, 0);
@@ -721,6 +726,7 @@ trax_status trax_configure(trax_ctx *ctx, const trax_config *cfg)
     if (kp.run_walk == 0 && kp.zi_min == 0) {
         kp.run_walk = kDefaultRunWalk;
         kp.zi_min = kDefaultIndexMin;
+        kp.pair_record = 1;
     }
     ctx->configured = true;
     if (ctx->graph) {
@@ -737,6 +743,7 @@ trax_status trax_set_tuning(trax_ctx *ctx, const trax_tuning *t)
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->kp.run_walk = t->run_walk;
     ctx->kp.zi_min = t->index_min;
+    ctx->kp.pair_record = t->pair_record ? 1u : 0u;
     if (ctx->graph) {
         cudaGraphExecDestroy(ctx->graph);
         ctx->graph = nullptr;
@@ -768,6 +775,7 @@ trax_status trax_get_tuning(const trax_ctx *ctx, trax_tuning *t)
     if (!ctx || !t) return TRAX_ERR_BAD_ARG;
     t->run_walk = ctx->kp.run_walk;
     t->index_min = ctx->kp.zi_min;
+    t->pair_record = ctx->kp.pair_record;
     return TRAX_OK;
 }
 

@@ -30,6 +30,8 @@ namespace trax {
 constexpr int kMaxLT = TRAX_MAX_LAYER_TRIPLETS;
 constexpr int kMaxLayers = TRAX_MAX_LAYERS;
 constexpr uint32_t kFull = 0xffffffffu;
+constexpr int kPairSave = 8;  /* ballot chunks a pair-stage item keeps for its store */
+constexpr int kFusedThreads = 256;  /* threads per block of the tiled pair / predict kernels */
 
 /* Per-run constants, passed by value to every kernel. */
 struct KParams {
@@ -46,6 +48,7 @@ struct KParams {
      * same trax_acosf (host and device agree bit for bit) */
     float acos_rmin[kMaxLayers], acos_rmax[kMaxLayers];
     uint32_t run_walk, zi_min;   /* candidate-walk tuning, see k_zindex */
+    uint32_t pair_record;        /* pair stage replays its count ballots (trax_tuning) */
 };
 
 /* Device-side sizes, counters and status of one pipeline run. */
@@ -786,30 +789,7 @@ __device__ __forceinline__ void pair_visit(const KParams &kp, const uint32_t *lG
         const uint32_t jb = max(jlo, rowEnd);
         const uint32_t bLo = jb - len;
         const uint32_t bHi = end2 > jb ? end2 - len : bLo;
-        if (!STORE) {
-            for (uint32_t c = aLo; c < aHi; c += 32) {
-                const uint32_t idx = c + lane;
-                bool acc = false;
-                if (idx < aHi) {
-                    const float zz = Z[idx];
-                    acc = w.zLow <= zz && zz <= w.zHigh && phi_in(PHI[idx], w.phiLow, w.phiHigh, w.wrap);
-                }
-                const uint32_t b = __popc(__ballot_sync(kFull, acc));
-                visits += b;
-                distinct += b;
-            }
-            for (uint32_t c = bLo; c < bHi; c += 32) {
-                const uint32_t idx = c + lane;
-                bool acc = false, dup = false;
-                if (idx < bHi) {
-                    const float zz = Z[idx];
-                    acc = w.zLow <= zz && zz <= w.zHigh && phi_in(PHI[idx], w.phiLow, w.phiHigh, w.wrap);
-                    dup = idx >= aLo && idx < aHi;
-                }
-                visits += __popc(__ballot_sync(kFull, acc));
-                distinct += __popc(__ballot_sync(kFull, acc && !dup));
-            }
-        } else {
+        {
             /* ascending union: B, then A above B */
             const uint32_t a2 = max(aLo, bHi);
             for (int part = 0; part < 2; ++part) {
@@ -828,6 +808,57 @@ __device__ __forceinline__ void pair_visit(const KParams &kp, const uint32_t *lG
                         if (p < cap) pairs[p] = make_uint2(idx, outer);
                     }
                     distinct += __popc(b);
+                }
+            }
+        }
+    }
+}
+
+/*
+ * Count sweep of one outer hit in the store's order (per row: B, then the part
+ * of A above B).  With B's accepts that also lie in A counted twice, the
+ * visits equal the reference's (A and B walked in full) and the distinct
+ * accepts its bitmap bits.  Every chunk with accepts is recorded as (first
+ * index, ballot mask) while `cap` entries last, so that the store replays
+ * the ballots instead of sweeping again; *n_save counts all such chunks
+ * (> cap: the record is incomplete and the store sweeps again).
+ */
+__device__ __forceinline__ void pair_count_sweep(const KParams &kp, const uint32_t *lGrid1,
+                                                 const float *Z, const float *PHI,
+                                                 const PairWindow &w, uint32_t lane,
+                                                 uint32_t &visits, uint32_t &distinct,
+                                                 uint2 *save, uint32_t &n_save, uint32_t cap)
+{
+    const uint32_t P1 = kp.nphi + 1;
+    for (uint32_t zs = w.zLowSector; zs < w.zHighSector; ++zs) {
+        const uint32_t rowStart = lGrid1[zs * P1];
+        const uint32_t rowEnd = lGrid1[(zs + 1) * P1 - 1];
+        const uint32_t len = rowEnd - rowStart;
+        const uint32_t jlo = lGrid1[zs * P1 + w.phiLowSector];
+        const uint32_t end2 = w.wrap * rowEnd + lGrid1[zs * P1 + w.phiHighSector] - w.wrap * rowStart;
+        const uint32_t aLo = jlo, aHi = min(end2, rowEnd);
+        const uint32_t jb = max(jlo, rowEnd);
+        const uint32_t bLo = jb - len;
+        const uint32_t bHi = end2 > jb ? end2 - len : bLo;
+        const uint32_t a2 = max(aLo, bHi);
+        for (int part = 0; part < 2; ++part) {
+            const uint32_t lo = part == 0 ? bLo : a2;
+            const uint32_t hi = part == 0 ? bHi : aHi;
+            for (uint32_t c = lo; c < hi; c += 32) {
+                const uint32_t idx = c + lane;
+                bool acc = false;
+                if (idx < hi) {
+                    const float zz = Z[idx];
+                    acc = w.zLow <= zz && zz <= w.zHigh && phi_in(PHI[idx], w.phiLow, w.phiHigh, w.wrap);
+                }
+                const uint32_t m = __ballot_sync(kFull, acc);
+                const uint32_t nm = __popc(m);
+                visits += nm;
+                distinct += nm;
+                if (part == 0) visits += __popc(__ballot_sync(kFull, acc && idx >= aLo && idx < aHi));
+                if (m) {
+                    if (lane == 0 && n_save < cap) save[n_save] = make_uint2(c, m);
+                    ++n_save;
                 }
             }
         }
@@ -858,6 +889,7 @@ __device__ __forceinline__ PairWindow shfl_window(const PairWindow &w, int k)
     return r;
 }
 
+template <bool RECORD>
 __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *grid,
                                                     const float *X, const float *Y,
                                                     const float *Z, const float *PHI,
@@ -868,6 +900,10 @@ __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt_mask = lanemask_lt();
+    /* per warp and item: the count sweep's chunks with accepts (RECORD) */
+    __shared__ uint2 s_save[kFusedThreads / 32][32][RECORD ? kPairSave : 1];
+    __shared__ uint32_t s_nsave[kFusedThreads / 32][32];
+    const uint32_t wib = threadIdx.x >> 5;
     uint32_t n = st->n_outer;
     if (n > slot_cap) n = slot_cap;
     if (n == 0) {
@@ -906,12 +942,16 @@ __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *
             const int k = __ffs(m) - 1;
             const PairWindow wk = shfl_window(w, k);
             const uint32_t lgk = __shfl_sync(kFull, lgoff, k);
-            uint32_t visits = 0, distinct = 0;
-            pair_visit<false>(kp, grid + lgk, Z, PHI, wk, lane, lt_mask, 0, visits, distinct,
-                              nullptr, 0, 0);
+            uint32_t visits = 0, distinct = 0, nsave = 0;
+            pair_count_sweep(kp, grid + lgk, Z, PHI, wk, lane, visits, distinct,
+                             &s_save[wib][k][0], nsave, RECORD ? kPairSave : 0);
             if (lane == (uint32_t)k) mine = distinct;
-            if (lane == 0) my_visits += visits;
+            if (lane == 0) {
+                my_visits += visits;
+                s_nsave[wib][k] = nsave;
+            }
         }
+        __syncwarp();
         uint32_t tile_end;
         const uint32_t pos = warp_tile_position(mine, tile, status, st, &tile_end);
         if (s < n) pexcl[s] = pos;
@@ -919,17 +959,32 @@ __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *
             pexcl[n] = tile_end;
             st->n_pairs = tile_end;
         }
-        /* store sweep */
-        for (uint32_t m = live_mask; m; m &= m - 1) {
+        /* store: replay the recorded ballots (an item whose record
+         * overflowed sweeps again) */
+        for (uint32_t m = __ballot_sync(kFull, live && mine != 0); m; m &= m - 1) {
             const int k = __ffs(m) - 1;
-            const PairWindow wk = shfl_window(w, k);
-            const uint32_t lgk = __shfl_sync(kFull, lgoff, k);
             const uint32_t pk = __shfl_sync(kFull, pos, k);
             const uint32_t ok = __shfl_sync(kFull, outer, k);
-            uint32_t visits = 0, distinct = 0;
-            pair_visit<true>(kp, grid + lgk, Z, PHI, wk, lane, lt_mask, ok, visits, distinct,
-                             pairs, pk, pair_cap);
+            const uint32_t ns = s_nsave[wib][k];
+            if (RECORD && ns <= (uint32_t)kPairSave) {
+                uint32_t run = 0;
+                for (uint32_t q = 0; q < ns; ++q) {
+                    const uint2 e = s_save[wib][k][q];
+                    if ((e.y >> lane) & 1u) {
+                        const uint32_t p = pk + run + __popc(e.y & lt_mask);
+                        if (p < pair_cap) pairs[p] = make_uint2(e.x + lane, ok);
+                    }
+                    run += __popc(e.y);
+                }
+            } else {
+                const PairWindow wk = shfl_window(w, k);
+                const uint32_t lgk = __shfl_sync(kFull, lgoff, k);
+                uint32_t visits = 0, distinct = 0;
+                pair_visit<true>(kp, grid + lgk, Z, PHI, wk, lane, lt_mask, ok, visits, distinct,
+                                 pairs, pk, pair_cap);
+            }
         }
+        __syncwarp();
     }
     if (lane == 0 && my_visits) atomicAdd(&st->pair_slots, my_visits);
 }

@@ -263,8 +263,9 @@ class Context:
         self.config = cfg
         return self
 
-    def set_tuning(self, run_walk: int, index_min: int):
-        self._check(self.lib.trax_set_tuning(self.h, C.byref(A.TraxTuning(run_walk, index_min))))
+    def set_tuning(self, run_walk: int, index_min: int, pair_record: int = 1):
+        self._check(self.lib.trax_set_tuning(
+            self.h, C.byref(A.TraxTuning(run_walk, index_min, pair_record))))
 
     def set_pair_generator(self, name: str):
         """"beamspot" or "sector": the pair generator of the batched pipeline."""
@@ -273,7 +274,7 @@ class Context:
     def get_tuning(self):
         t = A.TraxTuning()
         self._check(self.lib.trax_get_tuning(self.h, C.byref(t)))
-        return int(t.run_walk), int(t.index_min)
+        return int(t.run_walk), int(t.index_min), int(t.pair_record)
 
     def alloc(self, n, dtype=np.uint32) -> DeviceBuffer:
         return DeviceBuffer(self, int(n) * np.dtype(dtype).itemsize, dtype)
