@@ -346,8 +346,8 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
      * from pair_offsets[G] by trax_triplet_predict */
     CK(cudaMemsetAsync(&st->n_prec, 0, 4, ctx->stream));
     k_predict_count<<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
-        kp, grid, h.x, h.y, h.z, h.phi, h.event, h.layer, (const float2 *)ctx->zi.p, pairs,
-        &st->n_pairs, pair_cap, cexcl, ptile, recs, rec_cap, st);
+        kp, grid, h.x, h.y, h.z, h.phi, h.event, h.layer, (const float2 *)ctx->zi.p,
+        (const uint32_t *)ctx->zp.p, pairs, &st->n_pairs, pair_cap, cexcl, ptile, recs, rec_cap, st);
     if ((s = mark(ctx, "predict")) != TRAX_OK) return s;
     CK(cudaMemsetAsync(&st->tile_ctr[1], 0, 4, ctx->stream));
     CK(cudaMemsetAsync(ctx->st1.p, 0, (size_t)ntile * 8, ctx->stream));

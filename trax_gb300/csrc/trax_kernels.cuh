@@ -1341,19 +1341,42 @@ __device__ __forceinline__ PredWindow pred_window(const KParams &kp, uint32_t lt
  *                     position (tile prefix + in-tile prefix).
  * Only pairs with candidates are walked twice, and no window is recomputed.
  */
+constexpr int kPredKeep = 8;  /* window-B accepts a store record carries */
+
 struct PredRec {
     float zLow, zHigh, phiLow, phiHigh;  /* window B */
     uint32_t pair;
     uint32_t grid_off;                   /* layer-3 grid of the pair's event */
     uint32_t zsec;                       /* zLowSector | zHighSector << 16 */
     uint32_t psec;                       /* phiLowSector | phiHighSector << 16 | wrap << 31 */
+    uint32_t hit[kPredKeep];             /* the first window-B accepts in visit order */
 };
 
-/* Count walk of one pair: accepts of window A (cA) and B (cB). */
+/* Adds window-B accept j (the n-th found) to keep[], the first kPredKeep
+ * accepts in visit order: position order within a cell, whose accepts begin
+ * at keep[cell0].  Accepts of an indexed cell arrive in z order, so a later
+ * one with a smaller position still displaces the cell's largest kept one. */
+__device__ __forceinline__ void pred_keep(uint32_t *keep, uint32_t n, uint32_t cell0, uint32_t j)
+{
+    uint32_t k = n;
+    if (k >= (uint32_t)kPredKeep) {
+        if (cell0 >= (uint32_t)kPredKeep || keep[kPredKeep - 1] < j) return;
+        k = kPredKeep - 1;  /* drop the cell's largest kept position */
+    }
+    while (k > cell0 && keep[k - 1] > j) {
+        keep[k] = keep[k - 1];
+        --k;
+    }
+    keep[k] = j;
+}
+
+/* Count walk of one pair: accepts of window A (cA) and B (cB), and the first
+ * kPredKeep window-B accepts in the reference's visit order. */
 __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_t *lGrid3,
                                                 const float *Z, const float *PHI,
-                                                const float2 *zi, const PredWindow &w,
-                                                uint32_t &cA, uint32_t &cB)
+                                                const float2 *zi, const uint32_t *zpos,
+                                                const PredWindow &w, uint32_t &cA,
+                                                uint32_t &cB, uint32_t *keep)
 {
     const uint32_t P1 = kp.nphi + 1;
     cA = 0;
@@ -1382,7 +1405,10 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
                     const float zz = Z[j];
                     const bool ph = phi_in(PHI[j], w.phiLow, w.phiHigh, w.wrap);
                     cA += (inA && ph && w.zLow[0] <= zz && zz <= w.zHigh[0]) ? 1u : 0u;
-                    cB += (inB && ph && w.zLow[1] <= zz && zz <= w.zHigh[1]) ? 1u : 0u;
+                    if (inB && ph && w.zLow[1] <= zz && zz <= w.zHigh[1]) {
+                        pred_keep(keep, cB, cB, j);
+                        ++cB;
+                    }
                 }
                 continue;
             }
@@ -1393,7 +1419,10 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
                         const float zz = Z[j];
                         const bool ph = phi_in(PHI[j], w.phiLow, w.phiHigh, w.wrap);
                         cA += (inA && ph && w.zLow[0] <= zz && zz <= w.zHigh[0]) ? 1u : 0u;
-                        cB += (inB && ph && w.zLow[1] <= zz && zz <= w.zHigh[1]) ? 1u : 0u;
+                        if (inB && ph && w.zLow[1] <= zz && zz <= w.zHigh[1]) {
+                            pred_keep(keep, cB, cB, j);
+                            ++cB;
+                        }
                     }
                     continue;
                 }
@@ -1402,12 +1431,16 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
                     const uint32_t m = (lo + hi) >> 1;
                     if (zkey(zi[m].x) < keyLo) lo = m + 1; else hi = m;
                 }
+                const uint32_t cell0 = cB;
                 for (; lo < cb; ++lo) {
                     const float2 v = zi[lo];
                     if (zkey(v.x) > keyHi) break;
                     const bool ph = phi_in(v.y, w.phiLow, w.phiHigh, w.wrap);
                     cA += (inA && ph && w.zLow[0] <= v.x && v.x <= w.zHigh[0]) ? 1u : 0u;
-                    cB += (inB && ph && w.zLow[1] <= v.x && v.x <= w.zHigh[1]) ? 1u : 0u;
+                    if (inB && ph && w.zLow[1] <= v.x && v.x <= w.zHigh[1]) {
+                        pred_keep(keep, cB, cell0, zpos[lo]);
+                        ++cB;
+                    }
                 }
             }
         }
@@ -1417,7 +1450,8 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
 __global__ void __launch_bounds__(256, 5) k_predict_count(
     KParams kp, const uint32_t *grid, const float *X, const float *Y, const float *Z,
     const float *PHI, const uint32_t *EVENT, const uint32_t *LAYER, const float2 *zi,
-    const uint2 *pairs, const uint32_t *n_pairs_ptr, uint32_t pair_cap, uint32_t *in_tile,
+    const uint32_t *zpos, const uint2 *pairs, const uint32_t *n_pairs_ptr, uint32_t pair_cap,
+    uint32_t *in_tile,
     uint32_t *tile_sum, PredRec *recs, uint32_t rec_cap, DevState *st)
 {
     const uint32_t lane = threadIdx.x & 31;
@@ -1452,9 +1486,10 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
             }
         }
         uint32_t emitted = 0;
+        uint32_t keep[kPredKeep];
         if (live) {
             uint32_t cA, cB;
-            pred_count_walk(kp, grid + goff, Z, PHI, zi, w, cA, cB);
+            pred_count_walk(kp, grid + goff, Z, PHI, zi, zpos, w, cA, cB, keep);
             emitted = cA < cB ? cA : cB;
             my_slots += cA;
             my_trunc += cB - emitted;
@@ -1483,6 +1518,8 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
                 rec.grid_off = goff;
                 rec.zsec = w.zLowSector[1] | (w.zHighSector[1] << 16);
                 rec.psec = w.phiLowSector | (w.phiHighSector << 16) | (w.wrap << 31);
+#pragma unroll
+                for (int q = 0; q < kPredKeep; ++q) rec.hit[q] = (uint32_t)q < emitted ? keep[q] : 0u;
                 recs[r] = rec;
             }
         }
@@ -1516,6 +1553,12 @@ __global__ void __launch_bounds__(256) k_predict_store(
         const uint32_t pos = tile_prefix[p >> 5] + in_tile[p];
         const uint32_t emitted =
             (p + 1 < n ? tile_prefix[(p + 1) >> 5] + in_tile[p + 1] : *total_ptr) - pos;
+        if (emitted <= (uint32_t)kPredKeep) {
+            /* the count pass kept them: the first window-B accepts in visit order */
+            for (uint32_t q = 0; q < emitted; ++q)
+                if (pos + q < cand_cap) cands[pos + q] = make_uint2(p, rec.hit[q]);
+            continue;
+        }
         const uint32_t *lGrid3 = grid + rec.grid_off;
         const uint32_t zLowSector = rec.zsec & 0xffffu, zHighSector = rec.zsec >> 16;
         const uint32_t phiLowSector = rec.psec & 0xffffu;
