@@ -30,7 +30,6 @@ namespace {
 constexpr int kTimerSlots = 64;
 constexpr int kScanItems = 8;       /* items per thread in k_scan */
 constexpr int kScanThreads = 256;
-constexpr int kFilterItems = 4;
 constexpr int kTileItems = 32;      /* items per fused pair / predict tile (one warp) */
 constexpr uint32_t kDefaultRunWalk = 48;  /* see trax_set_tuning */
 constexpr uint32_t kDefaultIndexMin = 16;
@@ -64,6 +63,7 @@ struct trax_ctx {
     DevBuf prec;  /* prediction store records */
     DevBuf zp;    /* input position of each z-index entry */
     DevBuf ptile; /* prediction tile totals / prefixes */
+    DevBuf fmask; /* filter accept mask words and their positions */
     cudaEvent_t timers[kTimerSlots] = {};
     int blk_pair = 0, blk_pair0 = 0, blk_sector = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
 
@@ -372,16 +372,25 @@ trax_status enqueue_filter(trax_ctx *ctx, const SortedCols &h, const uint2 *pair
 {
     const KParams &kp = ctx->kp;
     trax_status s;
-    const uint32_t ntile = tiles_for(cand_cap, 256 * kFilterItems);
+    const uint32_t words = tiles_for(cand_cap, 32) + 1;
+    const uint32_t ntile = tiles_for(words, kScanItems * kScanThreads);
     if ((s = ensure(ctx, ctx->st2, (size_t)ntile * 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->fmask, (size_t)words * 8)) != TRAX_OK) return s;
+    uint32_t *mask = (uint32_t *)ctx->fmask.p, *wpos = mask + words;
     DevState *st = ctx->d_state;
+    CK(cudaMemsetAsync(trk_offsets, 0, (size_t)(max_groups + 1) * 4, ctx->stream));
+    k_filter_count<<<ctx->blk_filter, 256, 0, ctx->stream>>>(kp, h.x, h.y, h.z, h.layer, pairs,
+                                                             cands, &st->n_cands, cand_cap, mask,
+                                                             wpos, st);
+    if ((s = mark(ctx, "filter")) != TRAX_OK) return s;
     CK(cudaMemsetAsync(&st->tile_ctr[2], 0, 4, ctx->stream));
     CK(cudaMemsetAsync(ctx->st2.p, 0, (size_t)ntile * 8, ctx->stream));
-    CK(cudaMemsetAsync(trk_offsets, 0, (size_t)(max_groups + 1) * 4, ctx->stream));
-    k_filter<<<ctx->blk_filter, 256, 0, ctx->stream>>>(kp, h.x, h.y, h.z, h.layer, pairs, cands,
-                                                       &st->n_cands, cand_cap, t1, t2, t3, trk_cap,
-                                                       (unsigned long long *)ctx->st2.p, st);
-    if ((s = mark(ctx, "filter")) != TRAX_OK) return s;
+    k_scan<kScanItems><<<std::min<uint32_t>(ctx->blk_scan, ntile), kScanThreads, 0, ctx->stream>>>(
+        wpos, wpos, &st->n_ftile, words, &st->n_trk, 2, (unsigned long long *)ctx->st2.p, st);
+    if ((s = mark(ctx, "filter_scan")) != TRAX_OK) return s;
+    k_filter_store<<<ctx->blk_filter, 256, 0, ctx->stream>>>(pairs, cands, mask, wpos, t1, t2, t3,
+                                                             trk_cap, st);
+    if ((s = mark(ctx, "filter_store")) != TRAX_OK) return s;
     k_trk_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(t1, h.event, h.layer, trk_offsets,
                                                            kp.n_lt, trk_cap, st);
     if ((s = mark(ctx, "filter_offsets")) != TRAX_OK) return s;
@@ -631,7 +640,7 @@ trax_status trax_ctx_create(trax_ctx **out, int device)
     ctx->blk_sector = ctx->sm_count * std::max(b, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_predict_count, kFusedThreads, 0);
     ctx->blk_pred = ctx->sm_count * std::max(b, 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_filter, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_filter_count, 256, 0);
     ctx->blk_filter = ctx->sm_count * std::max(b, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_scan<kScanItems>, kScanThreads, 0);
     ctx->blk_scan = ctx->sm_count * std::max(b, 1);
@@ -651,7 +660,8 @@ void trax_ctx_destroy(trax_ctx *ctx)
                       &ctx->cexcl, &ctx->st0, &ctx->st1, &ctx->st2, &ctx->st3, &ctx->zi,
                       &ctx->conn_keys, &ctx->conn_sums, &ctx->grid_buf,
                       &ctx->pairs_buf, &ctx->pair_off, &ctx->cands_buf, &ctx->cand_off, &ctx->trk_off,
-                      &ctx->r_seg, &ctx->ing, &ctx->phys, &ctx->prec, &ctx->zp, &ctx->ptile};
+                      &ctx->r_seg, &ctx->ing, &ctx->phys, &ctx->prec, &ctx->zp, &ctx->ptile,
+                      &ctx->fmask};
     for (DevBuf *b : bufs) if (b->p) cudaFree(b->p);
     for (auto &b : ctx->in_cols) if (b.p) cudaFree(b.p);
     for (auto &b : ctx->srt_cols) if (b.p) cudaFree(b.p);
@@ -1300,7 +1310,8 @@ trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers
     if ((s = ensure(ctx, ctx->st1, (size_t)tiles_for(tiles_for(max_pairs, 32) + 1, kScanItems * kScanThreads) * 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->ptile, (size_t)(tiles_for(max_pairs, 32) + 1) * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->prec, (size_t)(max_candidates ? max_candidates : 1) * sizeof(PredRec))) != TRAX_OK) return s;
-    if ((s = ensure(ctx, ctx->st2, (size_t)tiles_for(max_candidates, 256 * kFilterItems) * 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->st2, (size_t)tiles_for(tiles_for(max_candidates, 32) + 1, kScanItems * kScanThreads) * 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->fmask, (size_t)(tiles_for(max_candidates, 32) + 1) * 8)) != TRAX_OK) return s;
     if ((s = ensure_stage(ctx, (size_t)max_events * max_layers * 2 + 4)) != TRAX_OK) return s;
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->r_events = max_events;

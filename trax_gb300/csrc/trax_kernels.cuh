@@ -68,7 +68,7 @@ struct DevState {
     uint32_t aux_n;          /* element count of a standalone prefix sum */
     uint32_t n_prec;         /* prediction store records */
     uint32_t n_ptile;        /* 32-pair tiles of the prediction count pass */
-    uint32_t pad[1];
+    uint32_t n_ftile;        /* 32-candidate words of the filter's accept mask */
 };
 
 struct SortedCols {
@@ -1698,45 +1698,69 @@ __device__ __forceinline__ bool filter_cut(const KParams &kp, uint32_t lt, const
     return valid;
 }
 
-__global__ void __launch_bounds__(256) k_filter(KParams kp, const float *X, const float *Y,
-                                                const float *Z, const uint32_t *LAYER,
-                                                const uint2 *pairs, const uint2 *cands,
-                                                const uint32_t *n_cands_ptr, uint32_t cand_cap,
-                                                uint32_t *t1, uint32_t *t2, uint32_t *t3,
-                                                uint32_t trk_cap, unsigned long long *status,
-                                                DevState *st)
+/*
+ * The filter as the reference structures it (filterCount's accept bitmap,
+ * filterPopCount, scan, filterStore; TripletThetaPhiFilter.h:50-252), without
+ * any wait between warps: k_filter_count evaluates the cuts one candidate per
+ * thread and writes each 32-candidate word of the accept mask and its
+ * popcount; k_scan turns the popcounts into positions; k_filter_store writes
+ * the accepted candidates' hits at those positions in candidate order.
+ */
+__global__ void __launch_bounds__(256) k_filter_count(KParams kp, const float *X, const float *Y,
+                                                      const float *Z, const uint32_t *LAYER,
+                                                      const uint2 *pairs, const uint2 *cands,
+                                                      const uint32_t *n_cands_ptr,
+                                                      uint32_t cand_cap, uint32_t *mask,
+                                                      uint32_t *word_count, DevState *st)
 {
+    const uint32_t lane = threadIdx.x & 31;
     uint32_t n = *n_cands_ptr;
     if (n > cand_cap) n = cand_cap;
-    if (n == 0) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) st->n_trk = 0;
-        return;
-    }
-    lookback_scan<4>(
-        n, &st->tile_ctr[2], status, st,
-        [&](uint32_t i) -> uint32_t {
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->n_ftile = (n + 31) / 32;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; i0 < n; i0 += stride) {
+        const uint32_t i = i0 + lane;
+        bool ok = false;
+        if (i < n) {
             const uint2 c = cands[i];
             const uint2 pr = pairs[c.x];
             const uint32_t lt = LAYER[pr.x] - 1;
-            if (lt >= kp.n_lt) {
+            if (lt >= kp.n_lt)
                 set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_BAD_TRIPLET_INDEX);
-                return 0u;
-            }
-            return filter_cut(kp, lt, X, Y, Z, pr.x, pr.y, c.y) ? 1u : 0u;
-        },
-        [&](uint32_t i, uint32_t pos, uint32_t v) {
-            if (v && pos < trk_cap) {
-                const uint2 c = cands[i];
-                const uint2 pr = pairs[c.x];
-                t1[pos] = pr.x;
-                t2[pos] = pr.y;
-                t3[pos] = c.y;
-            }
-        },
-        [&](uint32_t total) {
-            st->n_trk = total;
-            if (total > trk_cap) set_fault(st, TRAX_ERR_CAPACITY, TRAX_DETAIL_TRACKLET_CAPACITY);
-        });
+            else
+                ok = filter_cut(kp, lt, X, Y, Z, pr.x, pr.y, c.y);
+        }
+        const uint32_t m = __ballot_sync(kFull, ok);
+        if (lane == 0) {
+            mask[i0 >> 5] = m;
+            word_count[i0 >> 5] = __popc(m);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_filter_store(const uint2 *pairs, const uint2 *cands,
+                                                      const uint32_t *mask,
+                                                      const uint32_t *word_pos, uint32_t *t1,
+                                                      uint32_t *t2, uint32_t *t3,
+                                                      uint32_t trk_cap, DevState *st)
+{
+    const uint32_t words = st->n_ftile;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && st->n_trk > trk_cap)
+        set_fault(st, TRAX_ERR_CAPACITY, TRAX_DETAIL_TRACKLET_CAPACITY);
+    /* one mask word per thread (most words have no or one accept) */
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < words; t += gridDim.x * blockDim.x) {
+        uint32_t m = mask[t];
+        if (!m) continue;
+        uint32_t pos = word_pos[t];
+        for (; m; m &= m - 1, ++pos) {
+            if (pos >= trk_cap) break;
+            const uint2 c = cands[t * 32 + (__ffs(m) - 1)];
+            const uint2 pr = pairs[c.x];
+            t1[pos] = pr.x;
+            t2[pos] = pr.y;
+            t3[pos] = c.y;
+        }
+    }
 }
 
 /* filterOffsetStore (TripletThetaPhiFilter.h:270-292): the last tracklet of
