@@ -1341,16 +1341,24 @@ __device__ __forceinline__ PredWindow pred_window(const KParams &kp, uint32_t lt
  *                     position (tile prefix + in-tile prefix).
  * Only pairs with candidates are walked twice, and no window is recomputed.
  */
-constexpr int kPredKeep = 8;  /* window-B accepts a store record carries */
+constexpr int kPredKeep = 7;  /* window-B accepts a store record carries */
 
+/* 32-byte store record of a pair that emits.  A pair emitting at most
+ * kPredKeep candidates carries them; any other carries its store window.
+ * The store pass tells the two apart by the pair's emitted count. */
 struct PredRec {
-    float zLow, zHigh, phiLow, phiHigh;  /* window B */
     uint32_t pair;
-    uint32_t grid_off;                   /* layer-3 grid of the pair's event */
-    uint32_t zsec;                       /* zLowSector | zHighSector << 16 */
-    uint32_t psec;                       /* phiLowSector | phiHighSector << 16 | wrap << 31 */
-    uint32_t hit[kPredKeep];             /* the first window-B accepts in visit order */
+    union {
+        uint32_t hit[kPredKeep];  /* the first window-B accepts in visit order */
+        struct {
+            uint32_t grid_off;    /* layer-3 grid of the pair's event */
+            uint32_t zsec;        /* zLowSector | zHighSector << 16 */
+            uint32_t psec;        /* phiLowSector | phiHighSector << 16 | wrap << 31 */
+            float zLow, zHigh, phiLow, phiHigh;  /* window B */
+        } win;
+    };
 };
+static_assert(sizeof(PredRec) == 32, "a store record is one 32-byte sector");
 
 /* Adds window-B accept j (the n-th found) to keep[], the first kPredKeep
  * accepts in visit order: position order within a cell, whose accepts begin
@@ -1510,16 +1518,19 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
             const uint32_t r = base + __popc(want & lt_mask);
             if (r < rec_cap) {
                 PredRec rec;
-                rec.zLow = w.zLow[1];
-                rec.zHigh = w.zHigh[1];
-                rec.phiLow = w.phiLow;
-                rec.phiHigh = w.phiHigh;
                 rec.pair = p;
-                rec.grid_off = goff;
-                rec.zsec = w.zLowSector[1] | (w.zHighSector[1] << 16);
-                rec.psec = w.phiLowSector | (w.phiHighSector << 16) | (w.wrap << 31);
+                if (emitted <= (uint32_t)kPredKeep) {
 #pragma unroll
-                for (int q = 0; q < kPredKeep; ++q) rec.hit[q] = (uint32_t)q < emitted ? keep[q] : 0u;
+                    for (int q = 0; q < kPredKeep; ++q) rec.hit[q] = (uint32_t)q < emitted ? keep[q] : 0u;
+                } else {
+                    rec.win.grid_off = goff;
+                    rec.win.zsec = w.zLowSector[1] | (w.zHighSector[1] << 16);
+                    rec.win.psec = w.phiLowSector | (w.phiHighSector << 16) | (w.wrap << 31);
+                    rec.win.zLow = w.zLow[1];
+                    rec.win.zHigh = w.zHigh[1];
+                    rec.win.phiLow = w.phiLow;
+                    rec.win.phiHigh = w.phiHigh;
+                }
                 recs[r] = rec;
             }
         }
@@ -1547,8 +1558,8 @@ __global__ void __launch_bounds__(256) k_predict_store(
     if (n > pair_cap) n = pair_cap;
     const uint32_t P1 = kp.nphi + 1;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < nrec; r += gridDim.x * blockDim.x) {
-        const PredRec rec = recs[r];
-        const uint32_t p = rec.pair;
+        const PredRec r0 = recs[r];
+        const uint32_t p = r0.pair;
         if (p >= n) continue;
         const uint32_t pos = tile_prefix[p >> 5] + in_tile[p];
         const uint32_t emitted =
@@ -1556,9 +1567,10 @@ __global__ void __launch_bounds__(256) k_predict_store(
         if (emitted <= (uint32_t)kPredKeep) {
             /* the count pass kept them: the first window-B accepts in visit order */
             for (uint32_t q = 0; q < emitted; ++q)
-                if (pos + q < cand_cap) cands[pos + q] = make_uint2(p, rec.hit[q]);
+                if (pos + q < cand_cap) cands[pos + q] = make_uint2(p, r0.hit[q]);
             continue;
         }
+        const auto &rec = r0.win;
         const uint32_t *lGrid3 = grid + rec.grid_off;
         const uint32_t zLowSector = rec.zsec & 0xffffu, zHighSector = rec.zsec >> 16;
         const uint32_t phiLowSector = rec.psec & 0xffffu;
