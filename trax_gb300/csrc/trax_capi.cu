@@ -64,6 +64,7 @@ struct trax_ctx {
     DevBuf zp;    /* input position of each z-index entry */
     DevBuf ptile; /* prediction tile totals / prefixes */
     DevBuf fmask; /* filter accept mask words and their positions */
+    DevBuf zphi;  /* packed (z, phi) of the sorted hits */
     cudaEvent_t timers[kTimerSlots] = {};
     int blk_pair = 0, blk_pair0 = 0, blk_sector = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
 
@@ -295,11 +296,11 @@ trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *gr
             (unsigned long long *)ctx->st0.p, st);
     else if (kp.pair_record)
         k_pair_fused<true><<<ctx->blk_pair, kFusedThreads, 0, ctx->stream>>>(
-            kp, grid, h.x, h.y, h.z, h.phi, slots, slot_cap, pexcl, pairs, pair_cap,
+            kp, grid, h.x, h.y, h.z, h.phi, h.zphi, slots, slot_cap, pexcl, pairs, pair_cap,
             (unsigned long long *)ctx->st0.p, st);
     else
         k_pair_fused<false><<<ctx->blk_pair0, kFusedThreads, 0, ctx->stream>>>(
-            kp, grid, h.x, h.y, h.z, h.phi, slots, slot_cap, pexcl, pairs, pair_cap,
+            kp, grid, h.x, h.y, h.z, h.phi, h.zphi, slots, slot_cap, pexcl, pairs, pair_cap,
             (unsigned long long *)ctx->st0.p, st);
     if ((s = mark(ctx, "pair_gen")) != TRAX_OK) return s;
     k_group_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(g_base, pexcl, pair_offsets, kp.n_lt,
@@ -346,7 +347,7 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
      * from pair_offsets[G] by trax_triplet_predict */
     CK(cudaMemsetAsync(&st->n_prec, 0, 4, ctx->stream));
     k_predict_count<<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
-        kp, grid, h.x, h.y, h.z, h.phi, h.event, h.layer, (const float2 *)ctx->zi.p,
+        kp, grid, h.x, h.y, h.z, h.phi, h.zphi, h.event, h.layer, (const float2 *)ctx->zi.p,
         (const uint32_t *)ctx->zp.p, pairs, &st->n_pairs, pair_cap, cexcl, ptile, recs, rec_cap, st);
     if ((s = mark(ctx, "predict")) != TRAX_OK) return s;
     CK(cudaMemsetAsync(&st->tile_ctr[1], 0, 4, ctx->stream));
@@ -355,7 +356,7 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
         ptile, ptile, &st->n_ptile, ptiles, &st->n_cands, 1, (unsigned long long *)ctx->st1.p, st);
     if ((s = mark(ctx, "predict_scan")) != TRAX_OK) return s;
     k_predict_store<<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
-        kp, grid, h.z, h.phi, (const float2 *)ctx->zi.p, (const uint32_t *)ctx->zp.p, recs,
+        kp, grid, h.zphi, (const float2 *)ctx->zi.p, (const uint32_t *)ctx->zp.p, recs,
         rec_cap, cexcl, ptile, &st->n_pairs, pair_cap, &st->n_cands, cands, cand_cap, st);
     if ((s = mark(ctx, "predict_store")) != TRAX_OK) return s;
     k_cand_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(pair_offsets, cexcl, ptile,
@@ -405,7 +406,23 @@ SortedCols sorted_from(const trax_sorted_hits *o)
     s.x = o->x; s.y = o->y; s.z = o->z; s.phi = o->phi;
     s.layer = o->layer; s.det = o->detector_id; s.hitid = o->hit_id; s.event = o->event;
     s.orig = o->orig;
+    s.zphi = nullptr;
     return s;
+}
+
+/* Stage calls get the caller's sorted columns: pack (z, phi) for the
+ * candidate loops into context scratch first. */
+trax_status with_zphi(trax_ctx *ctx, SortedCols &s, uint32_t n)
+{
+    trax_status st = ensure(ctx, ctx->zphi, (size_t)n * 8 + 8);
+    if (st != TRAX_OK) return st;
+    s.zphi = (float2 *)ctx->zphi.p;
+    if (n) {
+        k_pack_zphi<<<std::min<uint32_t>((n + 255) / 256, ctx->blk_small * 4), 256, 0,
+                      ctx->stream>>>(s.z, s.phi, n, s.zphi);
+        CK(cudaGetLastError());
+    }
+    return TRAX_OK;
 }
 
 trax_status build_segments(trax_ctx *ctx, const trax_layout *lay, uint32_t n_hits,
@@ -661,7 +678,7 @@ void trax_ctx_destroy(trax_ctx *ctx)
                       &ctx->conn_keys, &ctx->conn_sums, &ctx->grid_buf,
                       &ctx->pairs_buf, &ctx->pair_off, &ctx->cands_buf, &ctx->cand_off, &ctx->trk_off,
                       &ctx->r_seg, &ctx->ing, &ctx->phys, &ctx->prec, &ctx->zp, &ctx->ptile,
-                      &ctx->fmask};
+                      &ctx->fmask, &ctx->zphi};
     for (DevBuf *b : bufs) if (b->p) cudaFree(b->p);
     for (auto &b : ctx->in_cols) if (b.p) cudaFree(b.p);
     for (auto &b : ctx->srt_cols) if (b.p) cudaFree(b.p);
@@ -1210,7 +1227,9 @@ static trax_status pair_gen(trax_ctx *ctx, const trax_sorted_hits *hits, const u
     const uint32_t G = grid->n_events * ctx->kp.n_lt;
     const uint64_t slot_cap = (uint64_t)hits->n * ctx->kp.n_lt + 1;
     if (slot_cap > 0xF0000000ull) return fail(ctx, TRAX_ERR_BAD_ARG, "too many hits");
-    return enqueue_pairs(ctx, sorted_from(hits), d_grid, (uint2 *)out->pairs, out->offsets,
+    SortedCols sc = sorted_from(hits);
+    if ((s = with_zphi(ctx, sc, hits->n)) != TRAX_OK) return s;
+    return enqueue_pairs(ctx, sc, d_grid, (uint2 *)out->pairs, out->offsets,
                          out->capacity, (uint32_t)slot_cap, G, generator);
 }
 
@@ -1241,8 +1260,10 @@ trax_status trax_triplet_predict(trax_ctx *ctx, const trax_sorted_hits *hits,
      * kernels read (device to device, stream ordered) */
     CK(cudaMemcpyAsync(&ctx->d_state->n_pairs, pairs->offsets + G, 4, cudaMemcpyDeviceToDevice,
                        ctx->stream));
-    if ((s = enqueue_zindex(ctx, sorted_from(hits), d_grid, hits->n)) != TRAX_OK) return s;
-    return enqueue_predict(ctx, sorted_from(hits), d_grid, (const uint2 *)pairs->pairs,
+    SortedCols sc = sorted_from(hits);
+    if ((s = with_zphi(ctx, sc, hits->n)) != TRAX_OK) return s;
+    if ((s = enqueue_zindex(ctx, sc, d_grid, hits->n)) != TRAX_OK) return s;
+    return enqueue_predict(ctx, sc, d_grid, (const uint2 *)pairs->pairs,
                            pairs->offsets, pairs->capacity, (uint2 *)cands->pairs, cands->offsets,
                            cands->capacity, G);
 }
@@ -1301,6 +1322,7 @@ trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers
     /* scratch at its maximum so the captured graph never reallocates */
     if ((s = ensure(ctx, ctx->zi, (size_t)max_hits * 8 + 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->zp, (size_t)max_hits * 4 + 4)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->zphi, (size_t)max_hits * 8 + 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->g_start, G * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->g_base, (G + 1) * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->slots, slot_cap * 8)) != TRAX_OK) return s;
@@ -1335,6 +1357,7 @@ SortedCols reserved_sorted(trax_ctx *ctx)
     s.layer = (uint32_t *)ctx->srt_cols[4].p; s.det = (uint32_t *)ctx->srt_cols[5].p;
     s.hitid = (uint32_t *)ctx->srt_cols[6].p; s.event = (uint32_t *)ctx->srt_cols[7].p;
     s.orig = (uint32_t *)ctx->srt_cols[8].p;
+    s.zphi = (float2 *)ctx->zphi.p;
     return s;
 }
 

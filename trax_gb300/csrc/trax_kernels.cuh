@@ -74,6 +74,7 @@ struct DevState {
 struct SortedCols {
     float *x, *y, *z, *phi;
     uint32_t *layer, *det, *hitid, *event, *orig;
+    float2 *zphi;  /* (z, phi) packed for the candidate loops; may be null */
 };
 
 struct InCols {
@@ -611,6 +612,7 @@ __global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols o
                         out.x[d] = x; out.y[d] = y; out.z[d] = z; out.phi[d] = phi;
                         out.layer[d] = ly; out.det[d] = in.det[h]; out.hitid[d] = in.hitid[h];
                         out.event[d] = ev; out.orig[d] = h;
+                        if (out.zphi) out.zphi[d] = make_float2(z, phi);
                     }
                 }
             }
@@ -629,11 +631,20 @@ __global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols o
                 out.x[d] = x; out.y[d] = y; out.z[d] = z; out.phi[d] = s_phi[k];
                 out.layer[d] = ly; out.det[d] = dt; out.hitid[d] = hd; out.event[d] = ev;
                 out.orig[d] = h;
+                if (out.zphi) out.zphi[d] = make_float2(z, s_phi[k]);
             }
             if (mismatch) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_LAYER_MISMATCH);
             __syncthreads();
         }
     }
+}
+
+/* (z, phi) of the sorted hits packed for the candidate loops. */
+__global__ void __launch_bounds__(256) k_pack_zphi(const float *Z, const float *PHI, uint32_t n,
+                                                   float2 *zphi)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        zphi[i] = make_float2(Z[i], PHI[i]);
 }
 
 /* ------------------------------------------------------------------------
@@ -773,7 +784,7 @@ __device__ __forceinline__ bool phi_in(float actPhi, float phiLow, float phiHigh
  */
 template <bool STORE>
 __device__ __forceinline__ void pair_visit(const KParams &kp, const uint32_t *lGrid1,
-                                           const float *Z, const float *PHI,
+                                           const float2 *ZP,
                                            const PairWindow &w, uint32_t lane, uint32_t lt_mask,
                                            uint32_t outer, uint32_t &visits, uint32_t &distinct,
                                            uint2 *pairs, uint32_t pos, uint32_t cap)
@@ -799,8 +810,8 @@ __device__ __forceinline__ void pair_visit(const KParams &kp, const uint32_t *lG
                     const uint32_t idx = c + lane;
                     bool acc = false;
                     if (idx < hi) {
-                        const float zz = Z[idx];
-                        acc = w.zLow <= zz && zz <= w.zHigh && phi_in(PHI[idx], w.phiLow, w.phiHigh, w.wrap);
+                        const float2 v = ZP[idx];
+                        acc = w.zLow <= v.x && v.x <= w.zHigh && phi_in(v.y, w.phiLow, w.phiHigh, w.wrap);
                     }
                     const uint32_t b = __ballot_sync(kFull, acc);
                     if (acc) {
@@ -824,7 +835,7 @@ __device__ __forceinline__ void pair_visit(const KParams &kp, const uint32_t *lG
  * (> cap: the record is incomplete and the store sweeps again).
  */
 __device__ __forceinline__ void pair_count_sweep(const KParams &kp, const uint32_t *lGrid1,
-                                                 const float *Z, const float *PHI,
+                                                 const float2 *ZP,
                                                  const PairWindow &w, uint32_t lane,
                                                  uint32_t &visits, uint32_t &distinct,
                                                  uint2 *save, uint32_t &n_save, uint32_t cap)
@@ -848,8 +859,8 @@ __device__ __forceinline__ void pair_count_sweep(const KParams &kp, const uint32
                 const uint32_t idx = c + lane;
                 bool acc = false;
                 if (idx < hi) {
-                    const float zz = Z[idx];
-                    acc = w.zLow <= zz && zz <= w.zHigh && phi_in(PHI[idx], w.phiLow, w.phiHigh, w.wrap);
+                    const float2 v = ZP[idx];
+                    acc = w.zLow <= v.x && v.x <= w.zHigh && phi_in(v.y, w.phiLow, w.phiHigh, w.wrap);
                 }
                 const uint32_t m = __ballot_sync(kFull, acc);
                 const uint32_t nm = __popc(m);
@@ -893,6 +904,7 @@ template <bool RECORD>
 __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *grid,
                                                     const float *X, const float *Y,
                                                     const float *Z, const float *PHI,
+                                                    const float2 *ZP,
                                                     const uint2 *slots, uint32_t slot_cap,
                                                     uint32_t *pexcl, uint2 *pairs,
                                                     uint32_t pair_cap, unsigned long long *status,
@@ -943,7 +955,7 @@ __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *
             const PairWindow wk = shfl_window(w, k);
             const uint32_t lgk = __shfl_sync(kFull, lgoff, k);
             uint32_t visits = 0, distinct = 0, nsave = 0;
-            pair_count_sweep(kp, grid + lgk, Z, PHI, wk, lane, visits, distinct,
+            pair_count_sweep(kp, grid + lgk, ZP, wk, lane, visits, distinct,
                              &s_save[wib][k][0], nsave, RECORD ? kPairSave : 0);
             if (lane == (uint32_t)k) mine = distinct;
             if (lane == 0) {
@@ -980,7 +992,7 @@ __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *
                 const PairWindow wk = shfl_window(w, k);
                 const uint32_t lgk = __shfl_sync(kFull, lgoff, k);
                 uint32_t visits = 0, distinct = 0;
-                pair_visit<true>(kp, grid + lgk, Z, PHI, wk, lane, lt_mask, ok, visits, distinct,
+                pair_visit<true>(kp, grid + lgk, ZP, wk, lane, lt_mask, ok, visits, distinct,
                                  pairs, pk, pair_cap);
             }
         }
@@ -1381,8 +1393,7 @@ __device__ __forceinline__ void pred_keep(uint32_t *keep, uint32_t n, uint32_t c
 /* Count walk of one pair: accepts of window A (cA) and B (cB), and the first
  * kPredKeep window-B accepts in the reference's visit order. */
 __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_t *lGrid3,
-                                                const float *Z, const float *PHI,
-                                                const float2 *zi, const uint32_t *zpos,
+                                                const float2 *ZP, const float2 *zi, const uint32_t *zpos,
                                                 const PredWindow &w, uint32_t &cA,
                                                 uint32_t &cB, uint32_t *keep)
 {
@@ -1410,8 +1421,9 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
             if (rb - ra <= kp.run_walk) {
                 /* a small run: walk its contiguous hits */
                 for (uint32_t j = ra; j < rb; ++j) {
-                    const float zz = Z[j];
-                    const bool ph = phi_in(PHI[j], w.phiLow, w.phiHigh, w.wrap);
+                    const float2 v = ZP[j];
+                    const float zz = v.x;
+                    const bool ph = phi_in(v.y, w.phiLow, w.phiHigh, w.wrap);
                     cA += (inA && ph && w.zLow[0] <= zz && zz <= w.zHigh[0]) ? 1u : 0u;
                     if (inB && ph && w.zLow[1] <= zz && zz <= w.zHigh[1]) {
                         pred_keep(keep, cB, cB, j);
@@ -1424,8 +1436,9 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
                 const uint32_t ca = row[c], cb = row[c + 1];
                 if (cb - ca <= kp.zi_min || cb - ca > kZiMax) {
                     for (uint32_t j = ca; j < cb; ++j) {
-                        const float zz = Z[j];
-                        const bool ph = phi_in(PHI[j], w.phiLow, w.phiHigh, w.wrap);
+                        const float2 v = ZP[j];
+                        const float zz = v.x;
+                        const bool ph = phi_in(v.y, w.phiLow, w.phiHigh, w.wrap);
                         cA += (inA && ph && w.zLow[0] <= zz && zz <= w.zHigh[0]) ? 1u : 0u;
                         if (inB && ph && w.zLow[1] <= zz && zz <= w.zHigh[1]) {
                             pred_keep(keep, cB, cB, j);
@@ -1457,8 +1470,9 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
 
 __global__ void __launch_bounds__(256, 5) k_predict_count(
     KParams kp, const uint32_t *grid, const float *X, const float *Y, const float *Z,
-    const float *PHI, const uint32_t *EVENT, const uint32_t *LAYER, const float2 *zi,
-    const uint32_t *zpos, const uint2 *pairs, const uint32_t *n_pairs_ptr, uint32_t pair_cap,
+    const float *PHI, const float2 *ZP, const uint32_t *EVENT, const uint32_t *LAYER,
+    const float2 *zi, const uint32_t *zpos, const uint2 *pairs, const uint32_t *n_pairs_ptr,
+    uint32_t pair_cap,
     uint32_t *in_tile,
     uint32_t *tile_sum, PredRec *recs, uint32_t rec_cap, DevState *st)
 {
@@ -1497,7 +1511,7 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
         uint32_t keep[kPredKeep];
         if (live) {
             uint32_t cA, cB;
-            pred_count_walk(kp, grid + goff, Z, PHI, zi, zpos, w, cA, cB, keep);
+            pred_count_walk(kp, grid + goff, ZP, zi, zpos, w, cA, cB, keep);
             emitted = cA < cB ? cA : cB;
             my_slots += cA;
             my_trunc += cB - emitted;
@@ -1547,7 +1561,7 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
 }
 
 __global__ void __launch_bounds__(256) k_predict_store(
-    KParams kp, const uint32_t *grid, const float *Z, const float *PHI, const float2 *zi,
+    KParams kp, const uint32_t *grid, const float2 *ZP, const float2 *zi,
     const uint32_t *zpos, const PredRec *recs, uint32_t rec_cap, const uint32_t *in_tile,
     const uint32_t *tile_prefix, const uint32_t *n_pairs_ptr, uint32_t pair_cap,
     const uint32_t *total_ptr, uint2 *cands, uint32_t cand_cap, DevState *st)
@@ -1591,9 +1605,9 @@ __global__ void __launch_bounds__(256) k_predict_store(
                 const uint32_t ra = row[c0], rb = row[c1];
                 if (rb - ra <= kp.run_walk) {
                     for (uint32_t j = ra; j < rb && written < emitted; ++j) {
-                        const float zz = Z[j];
-                        if (rec.zLow <= zz && zz <= rec.zHigh &&
-                            phi_in(PHI[j], rec.phiLow, rec.phiHigh, wrap)) {
+                        const float2 v = ZP[j];
+                        if (rec.zLow <= v.x && v.x <= rec.zHigh &&
+                            phi_in(v.y, rec.phiLow, rec.phiHigh, wrap)) {
                             if (pos + written < cand_cap) cands[pos + written] = make_uint2(p, j);
                             ++written;
                         }
@@ -1630,9 +1644,9 @@ __global__ void __launch_bounds__(256) k_predict_store(
                         continue;
                     }
                     for (uint32_t j = ca; j < cb && written < emitted; ++j) {
-                        const float zz = Z[j];
-                        if (rec.zLow <= zz && zz <= rec.zHigh &&
-                            phi_in(PHI[j], rec.phiLow, rec.phiHigh, wrap)) {
+                        const float2 v = ZP[j];
+                        if (rec.zLow <= v.x && v.x <= rec.zHigh &&
+                            phi_in(v.y, rec.phiLow, rec.phiHigh, wrap)) {
                             if (pos + written < cand_cap) cands[pos + written] = make_uint2(p, j);
                             ++written;
                         }
