@@ -177,7 +177,7 @@ int grid_build_warps(const trax_ctx *ctx, uint32_t C, uint32_t avg_seg, uint32_t
     const size_t budget = std::min<size_t>(ctx->smem_optin, 200 * 1024);
     long w = (long)((budget - 8ull * stage) / (4ull * C)) - 1;
     long want = 1;
-    while (want < 32 && want * 128 < (long)avg_seg) want <<= 1;
+    while (want < 32 && want * 32 * kGridItems < (long)avg_seg) want <<= 1;
     if (w > want) w = want;
     return (int)w;
 }

@@ -774,22 +774,20 @@ __device__ __forceinline__ bool phi_in(float actPhi, float phiLow, float phiHigh
 }
 
 /*
- * Visits one outer hit's inner candidates row by row.  For each row the
- * reference loop walks j in [jlo, end2) and maps j >= rowEnd back by the row
- * length; that is the index range A = [jlo, min(end2, rowEnd)) followed by
- * the wrapped range B = [max(jlo, rowEnd) - len, end2 - len).  The store
- * emits the union in ascending index order (the reference's bitmap order):
- * B first, then the part of A above B.  Counting mode returns the accepted
- * visits (A and B, with repeats) and the distinct accepted indices.
+ * Store sweep of one outer hit's inner candidates, row by row.  For each row
+ * the reference loop walks j in [jlo, end2) and maps j >= rowEnd back by the
+ * row length; that is the index range A = [jlo, min(end2, rowEnd)) followed
+ * by the wrapped range B = [max(jlo, rowEnd) - len, end2 - len).  The pairs
+ * are the union in ascending index order (the reference's bitmap order): B
+ * first, then the part of A above B, written from `pos` on.
  */
-template <bool STORE>
-__device__ __forceinline__ void pair_visit(const KParams &kp, const uint32_t *lGrid1,
-                                           const float2 *ZP,
-                                           const PairWindow &w, uint32_t lane, uint32_t lt_mask,
-                                           uint32_t outer, uint32_t &visits, uint32_t &distinct,
-                                           uint2 *pairs, uint32_t pos, uint32_t cap)
+__device__ __forceinline__ void pair_store_sweep(const KParams &kp, const uint32_t *lGrid1,
+                                                 const float2 *ZP, const PairWindow &w,
+                                                 uint32_t lane, uint32_t lt_mask, uint32_t outer,
+                                                 uint2 *pairs, uint32_t pos, uint32_t cap)
 {
     const uint32_t P1 = kp.nphi + 1;
+    uint32_t distinct = 0;
     for (uint32_t zs = w.zLowSector; zs < w.zHighSector; ++zs) {
         const uint32_t rowStart = lGrid1[zs * P1];
         const uint32_t rowEnd = lGrid1[(zs + 1) * P1 - 1];
@@ -800,26 +798,23 @@ __device__ __forceinline__ void pair_visit(const KParams &kp, const uint32_t *lG
         const uint32_t jb = max(jlo, rowEnd);
         const uint32_t bLo = jb - len;
         const uint32_t bHi = end2 > jb ? end2 - len : bLo;
-        {
-            /* ascending union: B, then A above B */
-            const uint32_t a2 = max(aLo, bHi);
-            for (int part = 0; part < 2; ++part) {
-                const uint32_t lo = part == 0 ? bLo : a2;
-                const uint32_t hi = part == 0 ? bHi : aHi;
-                for (uint32_t c = lo; c < hi; c += 32) {
-                    const uint32_t idx = c + lane;
-                    bool acc = false;
-                    if (idx < hi) {
-                        const float2 v = ZP[idx];
-                        acc = w.zLow <= v.x && v.x <= w.zHigh && phi_in(v.y, w.phiLow, w.phiHigh, w.wrap);
-                    }
-                    const uint32_t b = __ballot_sync(kFull, acc);
-                    if (acc) {
-                        const uint32_t p = pos + distinct + __popc(b & lt_mask);
-                        if (p < cap) pairs[p] = make_uint2(idx, outer);
-                    }
-                    distinct += __popc(b);
+        const uint32_t a2 = max(aLo, bHi);
+        for (int part = 0; part < 2; ++part) {
+            const uint32_t lo = part == 0 ? bLo : a2;
+            const uint32_t hi = part == 0 ? bHi : aHi;
+            for (uint32_t c = lo; c < hi; c += 32) {
+                const uint32_t idx = c + lane;
+                bool acc = false;
+                if (idx < hi) {
+                    const float2 v = ZP[idx];
+                    acc = w.zLow <= v.x && v.x <= w.zHigh && phi_in(v.y, w.phiLow, w.phiHigh, w.wrap);
                 }
+                const uint32_t b = __ballot_sync(kFull, acc);
+                if (acc) {
+                    const uint32_t p = pos + distinct + __popc(b & lt_mask);
+                    if (p < cap) pairs[p] = make_uint2(idx, outer);
+                }
+                distinct += __popc(b);
             }
         }
     }
@@ -881,8 +876,10 @@ __device__ __forceinline__ void pair_count_sweep(const KParams &kp, const uint32
  * each lane computes its own outer hit's window (no redundant math), then
  * the warp sweeps the candidates of its 32 items one item at a time with all
  * lanes (coalesced loads; ballots keep the inner-hit order).  A warp scan
- * plus warp-wide decoupled look-back turns the distinct counts into positions
- * and a second sweep, on L1-resident hits, stores the pairs.
+ * plus warp-wide decoupled look-back turns the distinct counts into positions;
+ * with RECORD the store replays the count sweep's ballots (kept per item in
+ * shared memory), otherwise -- and for an item whose ballots did not fit --
+ * a second sweep on L1-resident hits stores the pairs.
  */
 __device__ __forceinline__ PairWindow shfl_window(const PairWindow &w, int k)
 {
@@ -991,9 +988,7 @@ __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *
             } else {
                 const PairWindow wk = shfl_window(w, k);
                 const uint32_t lgk = __shfl_sync(kFull, lgoff, k);
-                uint32_t visits = 0, distinct = 0;
-                pair_visit<true>(kp, grid + lgk, ZP, wk, lane, lt_mask, ok, visits, distinct,
-                                 pairs, pk, pair_cap);
+                pair_store_sweep(kp, grid + lgk, ZP, wk, lane, lt_mask, ok, pairs, pk, pair_cap);
             }
         }
         __syncwarp();
