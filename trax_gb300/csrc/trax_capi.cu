@@ -65,6 +65,7 @@ struct trax_ctx {
     DevBuf ptile; /* prediction tile totals / prefixes */
     DevBuf fmask; /* filter accept mask words and their positions */
     DevBuf zphi;  /* packed (z, phi) of the sorted hits */
+    DevBuf zh;    /* half-precision z of the sorted hits (candidate screen) */
     cudaEvent_t timers[kTimerSlots] = {};
     int blk_pair = 0, blk_pair0 = 0, blk_sector = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
 
@@ -347,7 +348,7 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
      * from pair_offsets[G] by trax_triplet_predict */
     CK(cudaMemsetAsync(&st->n_prec, 0, 4, ctx->stream));
     k_predict_count<<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
-        kp, grid, h.x, h.y, h.z, h.phi, h.zphi, h.event, h.layer, (const float2 *)ctx->zi.p,
+        kp, grid, h.x, h.y, h.z, h.phi, h.zphi, h.zh, h.event, h.layer, (const float2 *)ctx->zi.p,
         (const uint32_t *)ctx->zp.p, pairs, &st->n_pairs, pair_cap, cexcl, ptile, recs, rec_cap, st);
     if ((s = mark(ctx, "predict")) != TRAX_OK) return s;
     CK(cudaMemsetAsync(&st->tile_ctr[1], 0, 4, ctx->stream));
@@ -356,7 +357,7 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
         ptile, ptile, &st->n_ptile, ptiles, &st->n_cands, 1, (unsigned long long *)ctx->st1.p, st);
     if ((s = mark(ctx, "predict_scan")) != TRAX_OK) return s;
     k_predict_store<<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
-        kp, grid, h.zphi, (const float2 *)ctx->zi.p, (const uint32_t *)ctx->zp.p, recs,
+        kp, grid, h.zphi, h.zh, recs,
         rec_cap, cexcl, ptile, &st->n_pairs, pair_cap, &st->n_cands, cands, cand_cap, st);
     if ((s = mark(ctx, "predict_store")) != TRAX_OK) return s;
     k_cand_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(pair_offsets, cexcl, ptile,
@@ -407,6 +408,7 @@ SortedCols sorted_from(const trax_sorted_hits *o)
     s.layer = o->layer; s.det = o->detector_id; s.hitid = o->hit_id; s.event = o->event;
     s.orig = o->orig;
     s.zphi = nullptr;
+    s.zh = nullptr;
     return s;
 }
 
@@ -416,10 +418,12 @@ trax_status with_zphi(trax_ctx *ctx, SortedCols &s, uint32_t n)
 {
     trax_status st = ensure(ctx, ctx->zphi, (size_t)n * 8 + 8);
     if (st != TRAX_OK) return st;
+    if ((st = ensure(ctx, ctx->zh, (size_t)n * 2 + 32)) != TRAX_OK) return st;
     s.zphi = (float2 *)ctx->zphi.p;
+    s.zh = (uint16_t *)ctx->zh.p;
     if (n) {
         k_pack_zphi<<<std::min<uint32_t>((n + 255) / 256, ctx->blk_small * 4), 256, 0,
-                      ctx->stream>>>(s.z, s.phi, n, s.zphi);
+                      ctx->stream>>>(s.z, s.phi, n, s.zphi, s.zh);
         CK(cudaGetLastError());
     }
     return TRAX_OK;
@@ -678,7 +682,7 @@ void trax_ctx_destroy(trax_ctx *ctx)
                       &ctx->conn_keys, &ctx->conn_sums, &ctx->grid_buf,
                       &ctx->pairs_buf, &ctx->pair_off, &ctx->cands_buf, &ctx->cand_off, &ctx->trk_off,
                       &ctx->r_seg, &ctx->ing, &ctx->phys, &ctx->prec, &ctx->zp, &ctx->ptile,
-                      &ctx->fmask, &ctx->zphi};
+                      &ctx->fmask, &ctx->zphi, &ctx->zh};
     for (DevBuf *b : bufs) if (b->p) cudaFree(b->p);
     for (auto &b : ctx->in_cols) if (b.p) cudaFree(b.p);
     for (auto &b : ctx->srt_cols) if (b.p) cudaFree(b.p);
@@ -1323,6 +1327,7 @@ trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers
     if ((s = ensure(ctx, ctx->zi, (size_t)max_hits * 8 + 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->zp, (size_t)max_hits * 4 + 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->zphi, (size_t)max_hits * 8 + 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->zh, (size_t)max_hits * 2 + 32)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->g_start, G * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->g_base, (G + 1) * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->slots, slot_cap * 8)) != TRAX_OK) return s;
@@ -1358,6 +1363,7 @@ SortedCols reserved_sorted(trax_ctx *ctx)
     s.hitid = (uint32_t *)ctx->srt_cols[6].p; s.event = (uint32_t *)ctx->srt_cols[7].p;
     s.orig = (uint32_t *)ctx->srt_cols[8].p;
     s.zphi = (float2 *)ctx->zphi.p;
+    s.zh = (uint16_t *)ctx->zh.p;
     return s;
 }
 

@@ -19,6 +19,7 @@
  */
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -75,6 +76,8 @@ struct SortedCols {
     float *x, *y, *z, *phi;
     uint32_t *layer, *det, *hitid, *event, *orig;
     float2 *zphi;  /* (z, phi) packed for the candidate loops; may be null */
+    uint16_t *zh;  /* z rounded to half precision (bits), the candidate screen;
+                    * null exactly when zphi is; 8 readable slots past the end */
 };
 
 struct InCols {
@@ -612,7 +615,10 @@ __global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols o
                         out.x[d] = x; out.y[d] = y; out.z[d] = z; out.phi[d] = phi;
                         out.layer[d] = ly; out.det[d] = in.det[h]; out.hitid[d] = in.hitid[h];
                         out.event[d] = ev; out.orig[d] = h;
-                        if (out.zphi) out.zphi[d] = make_float2(z, phi);
+                        if (out.zphi) {
+                            out.zphi[d] = make_float2(z, phi);
+                            out.zh[d] = __half_as_ushort(__float2half_rn(z));
+                        }
                     }
                 }
             }
@@ -631,7 +637,10 @@ __global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols o
                 out.x[d] = x; out.y[d] = y; out.z[d] = z; out.phi[d] = s_phi[k];
                 out.layer[d] = ly; out.det[d] = dt; out.hitid[d] = hd; out.event[d] = ev;
                 out.orig[d] = h;
-                if (out.zphi) out.zphi[d] = make_float2(z, s_phi[k]);
+                if (out.zphi) {
+                    out.zphi[d] = make_float2(z, s_phi[k]);
+                    out.zh[d] = __half_as_ushort(__float2half_rn(z));
+                }
             }
             if (mismatch) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_LAYER_MISMATCH);
             __syncthreads();
@@ -639,12 +648,70 @@ __global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols o
     }
 }
 
-/* (z, phi) of the sorted hits packed for the candidate loops. */
+/* (z, phi) of the sorted hits packed for the candidate loops, and z in
+ * half precision for the candidate screen. */
 __global__ void __launch_bounds__(256) k_pack_zphi(const float *Z, const float *PHI, uint32_t n,
-                                                   float2 *zphi)
+                                                   float2 *zphi, uint16_t *zh)
 {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         zphi[i] = make_float2(Z[i], PHI[i]);
+        zh[i] = __half_as_ushort(__float2half_rn(Z[i]));
+    }
+}
+
+/*
+ * Candidate screen on half-precision z.  Rounding to nearest is monotone, so
+ * a hit with zLow <= z <= zHigh has RD(zLow) <= RN(z) <= RU(zHigh) in half
+ * precision: hits outside that half interval cannot pass the exact test and
+ * are skipped without loading their float columns (NaN fails both).  The
+ * screen reads 8 halves (16 bytes) per step; `visit(j)` runs, in ascending
+ * j, for every hit of [ra, rb) that passes, until it returns false.
+ */
+struct ZScreen {
+    __half2 lo, hi;
+};
+
+/* The screen for the union of the active z windows [lo_v, hi_v]; a window
+ * that accepts nothing (lo > hi, or NaN) is left out. */
+__device__ __forceinline__ ZScreen zscreen_make(bool a, float loA, float hiA, bool b, float loB,
+                                                float hiB)
+{
+    float lo = INFINITY, hi = -INFINITY;
+    if (a && loA <= hiA) { lo = loA; hi = hiA; }
+    if (b && loB <= hiB) { lo = loB < lo ? loB : lo; hi = hiB > hi ? hiB : hi; }
+    ZScreen zs;
+    zs.lo = __half2half2(__float2half_rd(lo));
+    zs.hi = __half2half2(__float2half_ru(hi));
+    return zs;
+}
+
+__device__ __forceinline__ uint32_t zscreen_word(uint32_t w, const ZScreen &zs)
+{
+    const __half2 h = *reinterpret_cast<const __half2 *>(&w);
+    return __hge2_mask(h, zs.lo) & __hle2_mask(h, zs.hi);
+}
+
+template <class Visit>
+__device__ __forceinline__ void zscreen_walk(const uint16_t *ZH, uint32_t ra, uint32_t rb,
+                                             const ZScreen &zs, Visit &&visit)
+{
+    for (uint32_t j8 = ra & ~7u; j8 < rb; j8 += 8) {
+        const uint4 q = *reinterpret_cast<const uint4 *>(ZH + j8);
+        const uint32_t m0 = zscreen_word(q.x, zs), m1 = zscreen_word(q.y, zs);
+        const uint32_t m2 = zscreen_word(q.z, zs), m3 = zscreen_word(q.w, zs);
+        if ((m0 | m1 | m2 | m3) == 0u) continue;
+        uint32_t bits = (m0 & 1u) | ((m0 >> 15) & 2u) | ((m1 & 1u) << 2) | ((m1 >> 13) & 8u) |
+                        ((m2 & 1u) << 4) | ((m2 >> 11) & 0x20u) | ((m3 & 1u) << 6) |
+                        ((m3 >> 9) & 0x80u);
+        const uint32_t lo_off = ra > j8 ? ra - j8 : 0u;
+        const uint32_t hi_off = rb - j8 < 8u ? rb - j8 : 8u;
+        bits &= ((1u << hi_off) - 1u) & ~((1u << lo_off) - 1u);
+        while (bits) {
+            const uint32_t b = __ffs(bits) - 1;
+            bits &= bits - 1;
+            if (!visit(j8 + b)) return;
+        }
+    }
 }
 
 /* ------------------------------------------------------------------------
@@ -1388,7 +1455,8 @@ __device__ __forceinline__ void pred_keep(uint32_t *keep, uint32_t n, uint32_t c
 /* Count walk of one pair: accepts of window A (cA) and B (cB), and the first
  * kPredKeep window-B accepts in the reference's visit order. */
 __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_t *lGrid3,
-                                                const float2 *ZP, const float2 *zi, const uint32_t *zpos,
+                                                const float2 *ZP, const uint16_t *ZH,
+                                                const float2 *zi, const uint32_t *zpos,
                                                 const PredWindow &w, uint32_t &cA,
                                                 uint32_t &cB, uint32_t *keep)
 {
@@ -1405,6 +1473,19 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
         const uint32_t keyLo = min(inA ? kA0 : 0xffffffffu, inB ? kB0 : 0xffffffffu);
         const uint32_t keyHi = max(inA ? kA1 : 0u, inB ? kB1 : 0u);
         const uint32_t *row = lGrid3 + zs * P1;
+        const ZScreen scr = zscreen_make(inA, w.zLow[0], w.zHigh[0], inB, w.zLow[1], w.zHigh[1]);
+        /* the exact test of a hit that passed the screen (walks visit in
+         * position order, so accepts append) */
+        auto exact = [&](uint32_t j) {
+            const float2 v = ZP[j];
+            const bool ph = phi_in(v.y, w.phiLow, w.phiHigh, w.wrap);
+            cA += (inA && ph && w.zLow[0] <= v.x && v.x <= w.zHigh[0]) ? 1u : 0u;
+            if (inB && ph && w.zLow[1] <= v.x && v.x <= w.zHigh[1]) {
+                pred_keep(keep, cB, cB, j);
+                ++cB;
+            }
+            return true;
+        };
         /* the reference's visits, as runs of whole cells: columns
          * pLow..pHigh-1, or with wrap-around pLow..P then 0..pHigh-1 */
         for (int run = 0; run < 2; ++run) {
@@ -1415,31 +1496,13 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
             const uint32_t ra = row[c0], rb = row[c1];
             if (rb - ra <= kp.run_walk) {
                 /* a small run: walk its contiguous hits */
-                for (uint32_t j = ra; j < rb; ++j) {
-                    const float2 v = ZP[j];
-                    const float zz = v.x;
-                    const bool ph = phi_in(v.y, w.phiLow, w.phiHigh, w.wrap);
-                    cA += (inA && ph && w.zLow[0] <= zz && zz <= w.zHigh[0]) ? 1u : 0u;
-                    if (inB && ph && w.zLow[1] <= zz && zz <= w.zHigh[1]) {
-                        pred_keep(keep, cB, cB, j);
-                        ++cB;
-                    }
-                }
+                zscreen_walk(ZH, ra, rb, scr, exact);
                 continue;
             }
             for (uint32_t c = c0; c < c1; ++c) {
                 const uint32_t ca = row[c], cb = row[c + 1];
                 if (cb - ca <= kp.zi_min || cb - ca > kZiMax) {
-                    for (uint32_t j = ca; j < cb; ++j) {
-                        const float2 v = ZP[j];
-                        const float zz = v.x;
-                        const bool ph = phi_in(v.y, w.phiLow, w.phiHigh, w.wrap);
-                        cA += (inA && ph && w.zLow[0] <= zz && zz <= w.zHigh[0]) ? 1u : 0u;
-                        if (inB && ph && w.zLow[1] <= zz && zz <= w.zHigh[1]) {
-                            pred_keep(keep, cB, cB, j);
-                            ++cB;
-                        }
-                    }
+                    zscreen_walk(ZH, ca, cb, scr, exact);
                     continue;
                 }
                 uint32_t lo = ca, hi = cb;
@@ -1465,8 +1528,9 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
 
 __global__ void __launch_bounds__(256, 5) k_predict_count(
     KParams kp, const uint32_t *grid, const float *X, const float *Y, const float *Z,
-    const float *PHI, const float2 *ZP, const uint32_t *EVENT, const uint32_t *LAYER,
-    const float2 *zi, const uint32_t *zpos, const uint2 *pairs, const uint32_t *n_pairs_ptr,
+    const float *PHI, const float2 *ZP, const uint16_t *ZH, const uint32_t *EVENT,
+    const uint32_t *LAYER, const float2 *zi, const uint32_t *zpos, const uint2 *pairs,
+    const uint32_t *n_pairs_ptr,
     uint32_t pair_cap,
     uint32_t *in_tile,
     uint32_t *tile_sum, PredRec *recs, uint32_t rec_cap, DevState *st)
@@ -1506,7 +1570,7 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
         uint32_t keep[kPredKeep];
         if (live) {
             uint32_t cA, cB;
-            pred_count_walk(kp, grid + goff, ZP, zi, zpos, w, cA, cB, keep);
+            pred_count_walk(kp, grid + goff, ZP, ZH, zi, zpos, w, cA, cB, keep);
             emitted = cA < cB ? cA : cB;
             my_slots += cA;
             my_trunc += cB - emitted;
@@ -1556,8 +1620,8 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
 }
 
 __global__ void __launch_bounds__(256) k_predict_store(
-    KParams kp, const uint32_t *grid, const float2 *ZP, const float2 *zi,
-    const uint32_t *zpos, const PredRec *recs, uint32_t rec_cap, const uint32_t *in_tile,
+    KParams kp, const uint32_t *grid, const float2 *ZP, const uint16_t *ZH,
+    const PredRec *recs, uint32_t rec_cap, const uint32_t *in_tile,
     const uint32_t *tile_prefix, const uint32_t *n_pairs_ptr, uint32_t pair_cap,
     const uint32_t *total_ptr, uint2 *cands, uint32_t cand_cap, DevState *st)
 {
@@ -1585,68 +1649,28 @@ __global__ void __launch_bounds__(256) k_predict_store(
         const uint32_t phiLowSector = rec.psec & 0xffffu;
         const uint32_t phiHighSector = (rec.psec >> 16) & 0x7fffu;
         const uint32_t wrap = rec.psec >> 31;
-        const uint32_t kB0 = zkey(rec.zLow), kB1 = zkey(rec.zHigh);
+        const ZScreen scr = zscreen_make(false, 0.f, 0.f, true, rec.zLow, rec.zHigh);
         /* the first `emitted` accepts of window B in the reference's visit
-         * order: cells in run order, hits of a cell by position.  An indexed
-         * cell yields its accepts from the z range of the index, smallest
-         * position first (selection over the few hits in that range). */
+         * order: cells in run order, hits of a cell by position -- runs of
+         * whole cells walked in position order through the z screen (no
+         * z index: its accepts would come in z order) */
         uint32_t written = 0;
+        /* a hit of a walk that passed the screen: the exact test */
+        auto store = [&](uint32_t j) {
+            const float2 v = ZP[j];
+            if (rec.zLow <= v.x && v.x <= rec.zHigh && phi_in(v.y, rec.phiLow, rec.phiHigh, wrap)) {
+                if (pos + written < cand_cap) cands[pos + written] = make_uint2(p, j);
+                ++written;
+            }
+            return written < emitted;
+        };
         for (uint32_t zs = zLowSector; zs < zHighSector && written < emitted; ++zs) {
             const uint32_t *row = lGrid3 + zs * P1;
             for (int run = 0; run < 2 && written < emitted; ++run) {
                 const uint32_t c0 = run == 0 ? phiLowSector : 0u;
                 const uint32_t c1 = run == 0 ? (wrap ? P1 : phiHighSector) : (wrap ? phiHighSector : 0u);
                 if (c1 <= c0) continue;
-                const uint32_t ra = row[c0], rb = row[c1];
-                if (rb - ra <= kp.run_walk) {
-                    for (uint32_t j = ra; j < rb && written < emitted; ++j) {
-                        const float2 v = ZP[j];
-                        if (rec.zLow <= v.x && v.x <= rec.zHigh &&
-                            phi_in(v.y, rec.phiLow, rec.phiHigh, wrap)) {
-                            if (pos + written < cand_cap) cands[pos + written] = make_uint2(p, j);
-                            ++written;
-                        }
-                    }
-                    continue;
-                }
-                for (uint32_t c = c0; c < c1 && written < emitted; ++c) {
-                    const uint32_t ca = row[c], cb = row[c + 1];
-                    if (cb - ca > kp.zi_min && cb - ca <= kZiMax) {
-                        uint32_t lo = ca, hi = cb;
-                        while (lo < hi) {
-                            const uint32_t m = (lo + hi) >> 1;
-                            if (zkey(zi[m].x) < kB0) lo = m + 1; else hi = m;
-                        }
-                        uint32_t last = 0;
-                        bool first = true;
-                        while (written < emitted) {
-                            uint32_t best = 0xffffffffu;
-                            for (uint32_t q = lo; q < cb; ++q) {
-                                const float2 v = zi[q];
-                                if (zkey(v.x) > kB1) break;
-                                if (rec.zLow <= v.x && v.x <= rec.zHigh &&
-                                    phi_in(v.y, rec.phiLow, rec.phiHigh, wrap)) {
-                                    const uint32_t j = zpos[q];
-                                    if ((first || j > last) && j < best) best = j;
-                                }
-                            }
-                            if (best == 0xffffffffu) break;
-                            if (pos + written < cand_cap) cands[pos + written] = make_uint2(p, best);
-                            ++written;
-                            last = best;
-                            first = false;
-                        }
-                        continue;
-                    }
-                    for (uint32_t j = ca; j < cb && written < emitted; ++j) {
-                        const float2 v = ZP[j];
-                        if (rec.zLow <= v.x && v.x <= rec.zHigh &&
-                            phi_in(v.y, rec.phiLow, rec.phiHigh, wrap)) {
-                            if (pos + written < cand_cap) cands[pos + written] = make_uint2(p, j);
-                            ++written;
-                        }
-                    }
-                }
+                zscreen_walk(ZH, row[c0], row[c1], scr, store);
             }
         }
     }
