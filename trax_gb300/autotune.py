@@ -42,17 +42,19 @@ def time_staged(ctx: Context, p: Pipeline, reps: int) -> float:
 
 def tune_walk(ctx: Context, p: Pipeline, batch: gen.EventBatch, reps=5,
               candidates=WALK_CANDIDATES):
-    """Stages `batch`, times each (run_walk, index_min) with the pair stage
-    replaying its ballots, then the best of them with the pair stage sweeping
-    twice, and installs the fastest (run_walk, index_min, pair_record)."""
+    """Stages `batch`, times each (run_walk, index_min) with the pair stage's
+    one-outer-hit-per-lane kernel, then the best of them with the warp-swept
+    pair kernel (replaying its ballots, then sweeping twice), and installs the
+    fastest (run_walk, index_min, pair_record)."""
     p.stage(batch)
     timings = {}
     for cand in candidates:
-        ctx.set_tuning(*cand, 1)
-        timings[(*cand, 1)] = time_staged(ctx, p, reps)
+        ctx.set_tuning(*cand, 2)
+        timings[(*cand, 2)] = time_staged(ctx, p, reps)
     best = min(timings, key=timings.get)
-    ctx.set_tuning(best[0], best[1], 0)
-    timings[(best[0], best[1], 0)] = time_staged(ctx, p, reps)
+    for rec in (1, 0):
+        ctx.set_tuning(best[0], best[1], rec)
+        timings[(best[0], best[1], rec)] = time_staged(ctx, p, reps)
     best = min(timings, key=timings.get)
     ctx.set_tuning(*best)
     return best, timings

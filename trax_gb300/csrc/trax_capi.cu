@@ -67,7 +67,7 @@ struct trax_ctx {
     DevBuf zphi;  /* packed (z, phi) of the sorted hits */
     DevBuf zh;    /* half-precision z of the sorted hits (candidate screen) */
     cudaEvent_t timers[kTimerSlots] = {};
-    int blk_pair = 0, blk_pair0 = 0, blk_sector = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
+    int blk_pair = 0, blk_pair0 = 0, blk_pair_lane = 0, blk_sector = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
 
     /* batched pipeline */
     bool reserved = false;
@@ -294,6 +294,10 @@ trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *gr
     if (sector)
         k_pair_sector<<<ctx->blk_sector, kFusedThreads, 0, ctx->stream>>>(
             kp, grid, h.z, h.phi, slots, slot_cap, pexcl, pairs, pair_cap,
+            (unsigned long long *)ctx->st0.p, st);
+    else if (kp.pair_record == 2)
+        k_pair_lane<<<ctx->blk_pair_lane, kFusedThreads, 0, ctx->stream>>>(
+            kp, grid, h.x, h.y, h.z, h.phi, h.zphi, h.zh, slots, slot_cap, pexcl, pairs, pair_cap,
             (unsigned long long *)ctx->st0.p, st);
     else if (kp.pair_record)
         k_pair_fused<true><<<ctx->blk_pair, kFusedThreads, 0, ctx->stream>>>(
@@ -657,6 +661,8 @@ trax_status trax_ctx_create(trax_ctx **out, int device)
     ctx->blk_pair = ctx->sm_count * std::max(b, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_fused<false>, kFusedThreads, 0);
     ctx->blk_pair0 = ctx->sm_count * std::max(b, 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_lane, kFusedThreads, 0);
+    ctx->blk_pair_lane = ctx->sm_count * std::max(b, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_sector, kFusedThreads, 0);
     ctx->blk_sector = ctx->sm_count * std::max(b, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_predict_count, kFusedThreads, 0);
@@ -757,7 +763,7 @@ trax_status trax_configure(trax_ctx *ctx, const trax_config *cfg)
     if (kp.run_walk == 0 && kp.zi_min == 0) {
         kp.run_walk = kDefaultRunWalk;
         kp.zi_min = kDefaultIndexMin;
-        kp.pair_record = 1;
+        kp.pair_record = 2;
     }
     ctx->configured = true;
     if (ctx->graph) {
@@ -771,10 +777,11 @@ trax_status trax_set_tuning(trax_ctx *ctx, const trax_tuning *t)
 {
     if (!ctx || !t) return TRAX_ERR_BAD_ARG;
     if (t->index_min > 256) return fail(ctx, TRAX_ERR_BAD_ARG, "index_min must be <= 256");
+    if (t->pair_record > 2) return fail(ctx, TRAX_ERR_BAD_ARG, "pair_record must be 0, 1 or 2");
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->kp.run_walk = t->run_walk;
     ctx->kp.zi_min = t->index_min;
-    ctx->kp.pair_record = t->pair_record ? 1u : 0u;
+    ctx->kp.pair_record = t->pair_record;
     if (ctx->graph) {
         cudaGraphExecDestroy(ctx->graph);
         ctx->graph = nullptr;

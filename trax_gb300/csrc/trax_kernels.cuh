@@ -1063,6 +1063,126 @@ __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *
     if (lane == 0 && my_visits) atomicAdd(&st->pair_slots, my_visits);
 }
 
+/*
+ * Pair stage with one outer hit per lane.  The lane walks its own window's
+ * candidates in the reference's bitmap order (per row: B, then the part of A
+ * above B), screening them on half-precision z, so a warp handles 32 outer
+ * hits at once instead of one.  The count walk keeps the first kPairKeep
+ * accepts; a warp scan plus warp-wide decoupled look-back gives every lane
+ * its position, and the lane writes the kept accepts or, when it had more,
+ * walks again.
+ */
+constexpr int kPairKeep = 16;
+
+/* The walk of one outer hit; visit(j, both) gets every accepted inner hit in
+ * ascending order (both: a B accept that also lies in A, which the
+ * reference's visit count sees twice) and returns false to stop. */
+template <class Visit>
+__device__ __forceinline__ void pair_lane_walk(const KParams &kp, const uint32_t *lGrid1,
+                                               const float2 *ZP, const uint16_t *ZH,
+                                               const PairWindow &w, Visit &&visit)
+{
+    const uint32_t P1 = kp.nphi + 1;
+    const ZScreen scr = zscreen_make(true, w.zLow, w.zHigh, false, 0.f, 0.f);
+    bool go = true;
+    for (uint32_t zs = w.zLowSector; zs < w.zHighSector && go; ++zs) {
+        const uint32_t rowStart = lGrid1[zs * P1];
+        const uint32_t rowEnd = lGrid1[(zs + 1) * P1 - 1];
+        const uint32_t len = rowEnd - rowStart;
+        const uint32_t jlo = lGrid1[zs * P1 + w.phiLowSector];
+        const uint32_t end2 = w.wrap * rowEnd + lGrid1[zs * P1 + w.phiHighSector] - w.wrap * rowStart;
+        const uint32_t aLo = jlo, aHi = min(end2, rowEnd);
+        const uint32_t jb = max(jlo, rowEnd);
+        const uint32_t bLo = jb - len;
+        const uint32_t bHi = end2 > jb ? end2 - len : bLo;
+        const uint32_t a2 = max(aLo, bHi);
+        auto test = [&](uint32_t j, bool inB) {
+            const float2 v = ZP[j];
+            if (w.zLow <= v.x && v.x <= w.zHigh && phi_in(v.y, w.phiLow, w.phiHigh, w.wrap))
+                go = visit(j, inB && j >= aLo && j < aHi);
+            return go;
+        };
+        if (bLo < bHi) zscreen_walk(ZH, bLo, bHi, scr, [&](uint32_t j) { return test(j, true); });
+        if (go && a2 < aHi) zscreen_walk(ZH, a2, aHi, scr, [&](uint32_t j) { return test(j, false); });
+    }
+}
+
+__global__ void __launch_bounds__(256) k_pair_lane(KParams kp, const uint32_t *grid,
+                                                   const float *X, const float *Y,
+                                                   const float *Z, const float *PHI,
+                                                   const float2 *ZP, const uint16_t *ZH,
+                                                   const uint2 *slots, uint32_t slot_cap,
+                                                   uint32_t *pexcl, uint2 *pairs,
+                                                   uint32_t pair_cap, unsigned long long *status,
+                                                   DevState *st)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t n = st->n_outer;
+    if (n > slot_cap) n = slot_cap;
+    if (n == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            pexcl[0] = 0;
+            st->n_pairs = 0;
+        }
+        return;
+    }
+    const uint32_t ntiles = (n + 31) / 32;
+    unsigned long long my_visits = 0;
+    for (;;) {
+        uint32_t tile = 0;
+        if (lane == 0) tile = atomicAdd(&st->tile_ctr[0], 1u);
+        tile = __shfl_sync(kFull, tile, 0);
+        if (tile >= ntiles) break;
+        const uint32_t s = tile * 32 + lane;
+        bool live = s < n;
+        PairWindow w{};
+        uint32_t outer = 0;
+        const uint32_t *lGrid1 = grid;
+        if (live) {
+            const uint2 sl = slots[s];
+            outer = sl.x;
+            const uint32_t e = sl.y / kp.n_lt, lt = sl.y % kp.n_lt;
+            lGrid1 = grid + (size_t)(e * kp.n_layers + (kp.l1[lt] - 1)) * kp.C;
+            w = pair_window(kp, lt, X[outer], Y[outer], Z[outer], PHI[outer]);
+            if (!w.ok) {
+                set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_WINDOW_OUTSIDE_GRID);
+                live = false;
+            }
+        }
+        uint32_t mine = 0;
+        uint32_t keep[kPairKeep];
+        if (live) {
+            pair_lane_walk(kp, lGrid1, ZP, ZH, w, [&](uint32_t j, bool both) {
+                my_visits += both ? 2u : 1u;
+                if (mine < (uint32_t)kPairKeep) keep[mine] = j;
+                ++mine;
+                return true;
+            });
+        }
+        uint32_t tile_end;
+        const uint32_t pos = warp_tile_position(mine, tile, status, st, &tile_end);
+        if (s < n) pexcl[s] = pos;
+        if (tile == ntiles - 1 && lane == 0) {
+            pexcl[n] = tile_end;
+            st->n_pairs = tile_end;
+        }
+        if (mine == 0) continue;
+        if (mine <= (uint32_t)kPairKeep) {
+            for (uint32_t q = 0; q < mine; ++q)
+                if (pos + q < pair_cap) pairs[pos + q] = make_uint2(keep[q], outer);
+        } else {
+            uint32_t q = pos;
+            pair_lane_walk(kp, lGrid1, ZP, ZH, w, [&](uint32_t j, bool) {
+                if (q < pair_cap) pairs[q] = make_uint2(j, outer);
+                ++q;
+                return true;
+            });
+        }
+    }
+    for (int d = 16; d; d >>= 1) my_visits += __shfl_down_sync(kFull, my_visits, d);
+    if (lane == 0 && my_visits) atomicAdd(&st->pair_slots, my_visits);
+}
+
 /* ------------------------------------------------------------------------
  * Stage 2, sector variant (PairGeneratorSector.h:43-230).  No cut: every
  * layer-2 hit in the block of pairSpreadZ rows and pairSpreadPhi columns on

@@ -263,7 +263,7 @@ class Context:
         self.config = cfg
         return self
 
-    def set_tuning(self, run_walk: int, index_min: int, pair_record: int = 1):
+    def set_tuning(self, run_walk: int, index_min: int, pair_record: int = 2):
         self._check(self.lib.trax_set_tuning(
             self.h, C.byref(A.TraxTuning(run_walk, index_min, pair_record))))
 
