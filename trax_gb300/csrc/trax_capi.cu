@@ -297,7 +297,7 @@ trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *gr
             (unsigned long long *)ctx->st0.p, st);
     else if (kp.pair_record == 2)
         k_pair_lane<<<ctx->blk_pair_lane, kFusedThreads, 0, ctx->stream>>>(
-            kp, grid, h.x, h.y, h.z, h.phi, h.zphi, h.zh, slots, slot_cap, pexcl, pairs, pair_cap,
+            kp, grid, h.x, h.y, h.z, h.phi, h.zphi, slots, slot_cap, pexcl, pairs, pair_cap,
             (unsigned long long *)ctx->st0.p, st);
     else if (kp.pair_record)
         k_pair_fused<true><<<ctx->blk_pair, kFusedThreads, 0, ctx->stream>>>(

@@ -1066,24 +1066,25 @@ __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *
 /*
  * Pair stage with one outer hit per lane.  The lane walks its own window's
  * candidates in the reference's bitmap order (per row: B, then the part of A
- * above B), screening them on half-precision z, so a warp handles 32 outer
- * hits at once instead of one.  The count walk keeps the first kPairKeep
- * accepts; a warp scan plus warp-wide decoupled look-back gives every lane
- * its position, and the lane writes the kept accepts or, when it had more,
- * walks again.
+ * above B), so a warp handles 32 outer hits at once instead of one; the walk
+ * loads kPairUnroll candidates before testing them, so that their loads are
+ * in flight together.  The count walk keeps the first kPairKeep accepts; a
+ * warp scan plus warp-wide decoupled look-back gives every lane its
+ * position, and the lane writes the kept accepts or, when it had more, walks
+ * again.
  */
 constexpr int kPairKeep = 16;
+constexpr int kPairUnroll = 4;
 
 /* The walk of one outer hit; visit(j, both) gets every accepted inner hit in
  * ascending order (both: a B accept that also lies in A, which the
  * reference's visit count sees twice) and returns false to stop. */
 template <class Visit>
 __device__ __forceinline__ void pair_lane_walk(const KParams &kp, const uint32_t *lGrid1,
-                                               const float2 *ZP, const uint16_t *ZH,
-                                               const PairWindow &w, Visit &&visit)
+                                               const float2 *ZP, const PairWindow &w,
+                                               Visit &&visit)
 {
     const uint32_t P1 = kp.nphi + 1;
-    const ZScreen scr = zscreen_make(true, w.zLow, w.zHigh, false, 0.f, 0.f);
     bool go = true;
     for (uint32_t zs = w.zLowSector; zs < w.zHighSector && go; ++zs) {
         const uint32_t rowStart = lGrid1[zs * P1];
@@ -1096,21 +1097,28 @@ __device__ __forceinline__ void pair_lane_walk(const KParams &kp, const uint32_t
         const uint32_t bLo = jb - len;
         const uint32_t bHi = end2 > jb ? end2 - len : bLo;
         const uint32_t a2 = max(aLo, bHi);
-        auto test = [&](uint32_t j, bool inB) {
-            const float2 v = ZP[j];
-            if (w.zLow <= v.x && v.x <= w.zHigh && phi_in(v.y, w.phiLow, w.phiHigh, w.wrap))
-                go = visit(j, inB && j >= aLo && j < aHi);
-            return go;
+        auto range = [&](uint32_t lo, uint32_t hi, bool inB) {
+            for (uint32_t j = lo; j < hi && go; j += kPairUnroll) {
+                float2 v[kPairUnroll];
+#pragma unroll
+                for (int u = 0; u < kPairUnroll; ++u)
+                    v[u] = j + u < hi ? ZP[j + u] : make_float2(NAN, NAN);  /* NaN fails */
+#pragma unroll
+                for (int u = 0; u < kPairUnroll; ++u)
+                    if (go && w.zLow <= v[u].x && v[u].x <= w.zHigh &&
+                        phi_in(v[u].y, w.phiLow, w.phiHigh, w.wrap))
+                        go = visit(j + u, inB && j + u >= aLo && j + u < aHi);
+            }
         };
-        if (bLo < bHi) zscreen_walk(ZH, bLo, bHi, scr, [&](uint32_t j) { return test(j, true); });
-        if (go && a2 < aHi) zscreen_walk(ZH, a2, aHi, scr, [&](uint32_t j) { return test(j, false); });
+        range(bLo, bHi, true);
+        if (go) range(a2, aHi, false);
     }
 }
 
 __global__ void __launch_bounds__(256) k_pair_lane(KParams kp, const uint32_t *grid,
                                                    const float *X, const float *Y,
                                                    const float *Z, const float *PHI,
-                                                   const float2 *ZP, const uint16_t *ZH,
+                                                   const float2 *ZP,
                                                    const uint2 *slots, uint32_t slot_cap,
                                                    uint32_t *pexcl, uint2 *pairs,
                                                    uint32_t pair_cap, unsigned long long *status,
@@ -1152,7 +1160,7 @@ __global__ void __launch_bounds__(256) k_pair_lane(KParams kp, const uint32_t *g
         uint32_t mine = 0;
         uint32_t keep[kPairKeep];
         if (live) {
-            pair_lane_walk(kp, lGrid1, ZP, ZH, w, [&](uint32_t j, bool both) {
+            pair_lane_walk(kp, lGrid1, ZP, w, [&](uint32_t j, bool both) {
                 my_visits += both ? 2u : 1u;
                 if (mine < (uint32_t)kPairKeep) keep[mine] = j;
                 ++mine;
@@ -1172,7 +1180,7 @@ __global__ void __launch_bounds__(256) k_pair_lane(KParams kp, const uint32_t *g
                 if (pos + q < pair_cap) pairs[pos + q] = make_uint2(keep[q], outer);
         } else {
             uint32_t q = pos;
-            pair_lane_walk(kp, lGrid1, ZP, ZH, w, [&](uint32_t j, bool) {
+            pair_lane_walk(kp, lGrid1, ZP, w, [&](uint32_t j, bool) {
                 if (q < pair_cap) pairs[q] = make_uint2(j, outer);
                 ++q;
                 return true;
