@@ -66,6 +66,7 @@ struct trax_ctx {
     DevBuf fmask; /* filter accept mask words and their positions */
     DevBuf zphi;  /* packed (z, phi) of the sorted hits */
     DevBuf zh;    /* half-precision z of the sorted hits (candidate screen) */
+    DevBuf xyzp;  /* packed (x, y, z, phi) of the sorted hits */
     cudaEvent_t timers[kTimerSlots] = {};
     int blk_pair = 0, blk_pair0 = 0, blk_pair_lane = 0, blk_sector = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
 
@@ -267,13 +268,23 @@ trax_status enqueue_grid(trax_ctx *ctx, const InCols &in, const SortedCols &out,
 /* Pair stage with either generator: TRAX_PAIRS_BEAMSPOT (items are the
  * outer hits, k_pair_fused) or TRAX_PAIRS_SECTOR (items are the inner hits,
  * k_pair_sector).  Both write pairs (inner, outer) and per-group offsets. */
+/* The candidate kernels read the packed columns; a stage call without them
+ * is a bug of this library, reported instead of faulting on the device. */
+trax_status need_packed(trax_ctx *ctx, const SortedCols &h)
+{
+    if (!h.zphi || !h.zh || !h.xyzp)
+        return fail(ctx, TRAX_ERR_BAD_ARG, "packed hit columns missing");
+    return TRAX_OK;
+}
+
 trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *grid, uint2 *pairs,
                           uint32_t *pair_offsets, uint32_t pair_cap, uint32_t slot_cap,
                           uint32_t max_groups, int generator)
 {
     const bool sector = generator == TRAX_PAIRS_SECTOR;
     const KParams &kp = ctx->kp;
-    trax_status s;
+    trax_status s = need_packed(ctx, h);
+    if (s != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->g_start, (size_t)max_groups * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->g_base, (size_t)(max_groups + 1) * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->slots, (size_t)slot_cap * 8)) != TRAX_OK) return s;
@@ -297,7 +308,7 @@ trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *gr
             (unsigned long long *)ctx->st0.p, st);
     else if (kp.pair_record == 2)
         k_pair_lane<<<ctx->blk_pair_lane, kFusedThreads, 0, ctx->stream>>>(
-            kp, grid, h.x, h.y, h.z, h.phi, h.zphi, slots, slot_cap, pexcl, pairs, pair_cap,
+            kp, grid, h.xyzp, h.zphi, slots, slot_cap, pexcl, pairs, pair_cap,
             (unsigned long long *)ctx->st0.p, st);
     else if (kp.pair_record)
         k_pair_fused<true><<<ctx->blk_pair, kFusedThreads, 0, ctx->stream>>>(
@@ -336,7 +347,8 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
                             uint32_t max_groups)
 {
     const KParams &kp = ctx->kp;
-    trax_status s;
+    trax_status s = need_packed(ctx, h);
+    if (s != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->cexcl, (size_t)(pair_cap + 1) * 4)) != TRAX_OK) return s;
     const uint32_t ptiles = tiles_for(pair_cap, 32) + 1;
     const uint32_t ntile = tiles_for(ptiles, kScanItems * kScanThreads);
@@ -352,7 +364,7 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
      * from pair_offsets[G] by trax_triplet_predict */
     CK(cudaMemsetAsync(&st->n_prec, 0, 4, ctx->stream));
     k_predict_count<<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
-        kp, grid, h.x, h.y, h.z, h.phi, h.zphi, h.zh, h.event, h.layer, (const float2 *)ctx->zi.p,
+        kp, grid, h.xyzp, h.zphi, h.zh, h.event, h.layer, (const float2 *)ctx->zi.p,
         (const uint32_t *)ctx->zp.p, pairs, &st->n_pairs, pair_cap, cexcl, ptile, recs, rec_cap, st);
     if ((s = mark(ctx, "predict")) != TRAX_OK) return s;
     CK(cudaMemsetAsync(&st->tile_ctr[1], 0, 4, ctx->stream));
@@ -377,7 +389,8 @@ trax_status enqueue_filter(trax_ctx *ctx, const SortedCols &h, const uint2 *pair
                            uint32_t max_groups)
 {
     const KParams &kp = ctx->kp;
-    trax_status s;
+    trax_status s = need_packed(ctx, h);
+    if (s != TRAX_OK) return s;
     const uint32_t words = tiles_for(cand_cap, 32) + 1;
     const uint32_t ntile = tiles_for(words, kScanItems * kScanThreads);
     if ((s = ensure(ctx, ctx->st2, (size_t)ntile * 8)) != TRAX_OK) return s;
@@ -385,7 +398,7 @@ trax_status enqueue_filter(trax_ctx *ctx, const SortedCols &h, const uint2 *pair
     uint32_t *mask = (uint32_t *)ctx->fmask.p, *wpos = mask + words;
     DevState *st = ctx->d_state;
     CK(cudaMemsetAsync(trk_offsets, 0, (size_t)(max_groups + 1) * 4, ctx->stream));
-    k_filter_count<<<ctx->blk_filter, 256, 0, ctx->stream>>>(kp, h.x, h.y, h.z, h.layer, pairs,
+    k_filter_count<<<ctx->blk_filter, 256, 0, ctx->stream>>>(kp, h.xyzp, h.layer, pairs,
                                                              cands, &st->n_cands, cand_cap, mask,
                                                              wpos, st);
     if ((s = mark(ctx, "filter")) != TRAX_OK) return s;
@@ -413,6 +426,7 @@ SortedCols sorted_from(const trax_sorted_hits *o)
     s.orig = o->orig;
     s.zphi = nullptr;
     s.zh = nullptr;
+    s.xyzp = nullptr;
     return s;
 }
 
@@ -423,11 +437,13 @@ trax_status with_zphi(trax_ctx *ctx, SortedCols &s, uint32_t n)
     trax_status st = ensure(ctx, ctx->zphi, (size_t)n * 8 + 8);
     if (st != TRAX_OK) return st;
     if ((st = ensure(ctx, ctx->zh, (size_t)n * 2 + 32)) != TRAX_OK) return st;
+    if ((st = ensure(ctx, ctx->xyzp, (size_t)n * 16 + 16)) != TRAX_OK) return st;
     s.zphi = (float2 *)ctx->zphi.p;
     s.zh = (uint16_t *)ctx->zh.p;
+    s.xyzp = (float4 *)ctx->xyzp.p;
     if (n) {
         k_pack_zphi<<<std::min<uint32_t>((n + 255) / 256, ctx->blk_small * 4), 256, 0,
-                      ctx->stream>>>(s.z, s.phi, n, s.zphi, s.zh);
+                      ctx->stream>>>(s.x, s.y, s.z, s.phi, n, s.zphi, s.zh, s.xyzp);
         CK(cudaGetLastError());
     }
     return TRAX_OK;
@@ -688,7 +704,7 @@ void trax_ctx_destroy(trax_ctx *ctx)
                       &ctx->conn_keys, &ctx->conn_sums, &ctx->grid_buf,
                       &ctx->pairs_buf, &ctx->pair_off, &ctx->cands_buf, &ctx->cand_off, &ctx->trk_off,
                       &ctx->r_seg, &ctx->ing, &ctx->phys, &ctx->prec, &ctx->zp, &ctx->ptile,
-                      &ctx->fmask, &ctx->zphi, &ctx->zh};
+                      &ctx->fmask, &ctx->zphi, &ctx->zh, &ctx->xyzp};
     for (DevBuf *b : bufs) if (b->p) cudaFree(b->p);
     for (auto &b : ctx->in_cols) if (b.p) cudaFree(b.p);
     for (auto &b : ctx->srt_cols) if (b.p) cudaFree(b.p);
@@ -1290,7 +1306,9 @@ trax_status trax_triplet_filter(trax_ctx *ctx, const trax_sorted_hits *hits,
     const uint32_t G = grid->n_events * ctx->kp.n_lt;
     CK(cudaMemcpyAsync(&ctx->d_state->n_cands, cands->offsets + G, 4, cudaMemcpyDeviceToDevice,
                        ctx->stream));
-    return enqueue_filter(ctx, sorted_from(hits), (const uint2 *)pairs->pairs,
+    SortedCols sc = sorted_from(hits);
+    if ((s = with_zphi(ctx, sc, hits->n)) != TRAX_OK) return s;
+    return enqueue_filter(ctx, sc, (const uint2 *)pairs->pairs,
                           (const uint2 *)cands->pairs, cands->capacity, out->hit1, out->hit2,
                           out->hit3, out->offsets, out->capacity, G);
 }
@@ -1335,6 +1353,7 @@ trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers
     if ((s = ensure(ctx, ctx->zp, (size_t)max_hits * 4 + 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->zphi, (size_t)max_hits * 8 + 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->zh, (size_t)max_hits * 2 + 32)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->xyzp, (size_t)max_hits * 16 + 16)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->g_start, G * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->g_base, (G + 1) * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->slots, slot_cap * 8)) != TRAX_OK) return s;
@@ -1371,6 +1390,7 @@ SortedCols reserved_sorted(trax_ctx *ctx)
     s.orig = (uint32_t *)ctx->srt_cols[8].p;
     s.zphi = (float2 *)ctx->zphi.p;
     s.zh = (uint16_t *)ctx->zh.p;
+    s.xyzp = (float4 *)ctx->xyzp.p;
     return s;
 }
 

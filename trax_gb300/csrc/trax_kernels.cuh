@@ -78,6 +78,8 @@ struct SortedCols {
     float2 *zphi;  /* (z, phi) packed for the candidate loops; may be null */
     uint16_t *zh;  /* z rounded to half precision (bits), the candidate screen;
                     * null exactly when zphi is; 8 readable slots past the end */
+    float4 *xyzp;  /* (x, y, z, phi) of each hit, one load for the window and
+                    * cut arithmetic; null exactly when zphi is */
 };
 
 struct InCols {
@@ -618,6 +620,7 @@ __global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols o
                         if (out.zphi) {
                             out.zphi[d] = make_float2(z, phi);
                             out.zh[d] = __half_as_ushort(__float2half_rn(z));
+                            out.xyzp[d] = make_float4(x, y, z, phi);
                         }
                     }
                 }
@@ -640,6 +643,7 @@ __global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols o
                 if (out.zphi) {
                     out.zphi[d] = make_float2(z, s_phi[k]);
                     out.zh[d] = __half_as_ushort(__float2half_rn(z));
+                    out.xyzp[d] = make_float4(x, y, z, s_phi[k]);
                 }
             }
             if (mismatch) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_LAYER_MISMATCH);
@@ -648,14 +652,17 @@ __global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols o
     }
 }
 
-/* (z, phi) of the sorted hits packed for the candidate loops, and z in
- * half precision for the candidate screen. */
-__global__ void __launch_bounds__(256) k_pack_zphi(const float *Z, const float *PHI, uint32_t n,
-                                                   float2 *zphi, uint16_t *zh)
+/* (z, phi) of the sorted hits packed for the candidate loops, z in half
+ * precision for the candidate screen, and (x, y, z, phi) packed. */
+__global__ void __launch_bounds__(256) k_pack_zphi(const float *X, const float *Y, const float *Z,
+                                                   const float *PHI, uint32_t n, float2 *zphi,
+                                                   uint16_t *zh, float4 *xyzp)
 {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        zphi[i] = make_float2(Z[i], PHI[i]);
-        zh[i] = __half_as_ushort(__float2half_rn(Z[i]));
+        const float z = Z[i], phi = PHI[i];
+        zphi[i] = make_float2(z, phi);
+        zh[i] = __half_as_ushort(__float2half_rn(z));
+        xyzp[i] = make_float4(X[i], Y[i], z, phi);
     }
 }
 
@@ -1116,9 +1123,7 @@ __device__ __forceinline__ void pair_lane_walk(const KParams &kp, const uint32_t
 }
 
 __global__ void __launch_bounds__(256) k_pair_lane(KParams kp, const uint32_t *grid,
-                                                   const float *X, const float *Y,
-                                                   const float *Z, const float *PHI,
-                                                   const float2 *ZP,
+                                                   const float4 *XYZP, const float2 *ZP,
                                                    const uint2 *slots, uint32_t slot_cap,
                                                    uint32_t *pexcl, uint2 *pairs,
                                                    uint32_t pair_cap, unsigned long long *status,
@@ -1151,7 +1156,8 @@ __global__ void __launch_bounds__(256) k_pair_lane(KParams kp, const uint32_t *g
             outer = sl.x;
             const uint32_t e = sl.y / kp.n_lt, lt = sl.y % kp.n_lt;
             lGrid1 = grid + (size_t)(e * kp.n_layers + (kp.l1[lt] - 1)) * kp.C;
-            w = pair_window(kp, lt, X[outer], Y[outer], Z[outer], PHI[outer]);
+            const float4 o = XYZP[outer];
+            w = pair_window(kp, lt, o.x, o.y, o.z, o.w);
             if (!w.ok) {
                 set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_WINDOW_OUTSIDE_GRID);
                 live = false;
@@ -1655,8 +1661,8 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
 }
 
 __global__ void __launch_bounds__(256, 5) k_predict_count(
-    KParams kp, const uint32_t *grid, const float *X, const float *Y, const float *Z,
-    const float *PHI, const float2 *ZP, const uint16_t *ZH, const uint32_t *EVENT,
+    KParams kp, const uint32_t *grid, const float4 *XYZP, const float2 *ZP,
+    const uint16_t *ZH, const uint32_t *EVENT,
     const uint32_t *LAYER, const float2 *zi, const uint32_t *zpos, const uint2 *pairs,
     const uint32_t *n_pairs_ptr,
     uint32_t pair_cap,
@@ -1686,8 +1692,8 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
                 live = false;
             } else {
                 goff = (event * kp.n_layers + (kp.l3[lt] - 1)) * kp.C;
-                w = pred_window(kp, lt, X[h1], Y[h1], Z[h1], X[h2], Y[h2], Z[h2], PHI[h1],
-                                PHI[h2]);
+                const float4 a = XYZP[h1], b = XYZP[h2];
+                w = pred_window(kp, lt, a.x, a.y, a.z, b.x, b.y, b.z, a.w, b.w);
                 if (!w.ok) {
                     set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_WINDOW_OUTSIDE_GRID);
                     live = false;
@@ -1825,17 +1831,18 @@ __global__ void k_cand_offsets(const uint32_t *pair_offsets, const uint32_t *in_
 /* ------------------------------------------------------------------------
  * Stage 4: triplet filter + stable compaction in one pass.
  * ---------------------------------------------------------------------- */
-__device__ __forceinline__ bool filter_cut(const KParams &kp, uint32_t lt, const float *X,
-                                           const float *Y, const float *Z, uint32_t firstHit,
-                                           uint32_t secondHit, uint32_t thirdHit)
+__device__ __forceinline__ bool filter_cut(const KParams &kp, uint32_t lt, const float4 *XYZP,
+                                           uint32_t firstHit, uint32_t secondHit,
+                                           uint32_t thirdHit)
 {
     const float dThetaCut = kp.dtheta[lt];
     const float dPhiCut = kp.dphi[lt];
     const float tipCut = kp.tip[lt];
     const float minRadius = kp.rmin_curv;
-    const float x1 = X[firstHit], y1 = Y[firstHit], z1 = Z[firstHit];
-    const float x2 = X[secondHit], y2 = Y[secondHit], z2 = Z[secondHit];
-    const float x3 = X[thirdHit], y3 = Y[thirdHit], z3 = Z[thirdHit];
+    const float4 h1 = XYZP[firstHit], h2 = XYZP[secondHit], h3 = XYZP[thirdHit];
+    const float x1 = h1.x, y1 = h1.y, z1 = h1.z;
+    const float x2 = h2.x, y2 = h2.y, z2 = h2.z;
+    const float x3 = h3.x, y3 = h3.y, z3 = h3.z;
     bool valid = true;
     float angle1 = trax_atan2f(sqrtf((x2 - x1) * (x2 - x1) + (y2 - y1) * (y2 - y1)), (z2 - z1));
     float angle2 = trax_atan2f(sqrtf((x3 - x2) * (x3 - x2) + (y3 - y2) * (y3 - y2)), (z3 - z2));
@@ -1879,8 +1886,8 @@ __device__ __forceinline__ bool filter_cut(const KParams &kp, uint32_t lt, const
  * popcount; k_scan turns the popcounts into positions; k_filter_store writes
  * the accepted candidates' hits at those positions in candidate order.
  */
-__global__ void __launch_bounds__(256) k_filter_count(KParams kp, const float *X, const float *Y,
-                                                      const float *Z, const uint32_t *LAYER,
+__global__ void __launch_bounds__(256) k_filter_count(KParams kp, const float4 *XYZP,
+                                                      const uint32_t *LAYER,
                                                       const uint2 *pairs, const uint2 *cands,
                                                       const uint32_t *n_cands_ptr,
                                                       uint32_t cand_cap, uint32_t *mask,
@@ -1901,7 +1908,7 @@ __global__ void __launch_bounds__(256) k_filter_count(KParams kp, const float *X
             if (lt >= kp.n_lt)
                 set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_BAD_TRIPLET_INDEX);
             else
-                ok = filter_cut(kp, lt, X, Y, Z, pr.x, pr.y, c.y);
+                ok = filter_cut(kp, lt, XYZP, pr.x, pr.y, c.y);
         }
         const uint32_t m = __ballot_sync(kFull, ok);
         if (lane == 0) {
@@ -1920,19 +1927,21 @@ __global__ void __launch_bounds__(256) k_filter_store(const uint2 *pairs, const 
     const uint32_t words = st->n_ftile;
     if (blockIdx.x == 0 && threadIdx.x == 0 && st->n_trk > trk_cap)
         set_fault(st, TRAX_ERR_CAPACITY, TRAX_DETAIL_TRACKLET_CAPACITY);
-    /* one mask word per thread (most words have no or one accept) */
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < words; t += gridDim.x * blockDim.x) {
-        uint32_t m = mask[t];
-        if (!m) continue;
-        uint32_t pos = word_pos[t];
-        for (; m; m &= m - 1, ++pos) {
-            if (pos >= trk_cap) break;
-            const uint2 c = cands[t * 32 + (__ffs(m) - 1)];
-            const uint2 pr = pairs[c.x];
-            t1[pos] = pr.x;
-            t2[pos] = pr.y;
-            t3[pos] = c.y;
-        }
+    /* one mask word per warp: lane b stores candidate 32 t + b if accepted,
+     * so the candidate reads and the tracklet writes are coalesced */
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lt_mask = lanemask_lt();
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < words; t += nw) {
+        const uint32_t m = mask[t];
+        if (!((m >> lane) & 1u)) continue;
+        const uint32_t pos = word_pos[t] + __popc(m & lt_mask);
+        if (pos >= trk_cap) continue;
+        const uint2 c = cands[t * 32 + lane];
+        const uint2 pr = pairs[c.x];
+        t1[pos] = pr.x;
+        t2[pos] = pr.y;
+        t3[pos] = c.y;
     }
 }
 
