@@ -501,6 +501,21 @@ trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers
  * CUDA graph and downloads the tracklets.  Synchronous. */
 trax_status trax_seed_batch(trax_ctx *ctx, const trax_event_batch *in, trax_batch_result *out);
 
+/* Streaming form of trax_seed_batch (the reference's per-group loop in
+ * TripletBuilder.cpp:183-285, with the next group's upload overlapping this
+ * group's chain).  trax_submit_batch queues one batch -- its upload on the
+ * context's copy stream, the chain's graph, the results written by the
+ * device straight into the output buffers -- and returns at once with a
+ * ticket; trax_wait_batch waits for that batch and fills n_tracklets and
+ * counts (status and capacity errors as trax_seed_batch).  Two batches may be
+ * in flight; a third submit before a wait returns TRAX_ERR_BAD_ARG.  The
+ * output buffers (hit1..3, offsets) must be pinned host memory
+ * (trax_host_alloc_pinned or cudaHostAlloc); the input arrays must stay
+ * unchanged until the wait returns. */
+trax_status trax_submit_batch(trax_ctx *ctx, const trax_event_batch *in,
+                              const trax_batch_result *out, uint32_t *ticket);
+trax_status trax_wait_batch(trax_ctx *ctx, uint32_t ticket, trax_batch_result *out);
+
 /* Device-resident variant for throughput measurement: the batch was uploaded
  * by trax_stage_batch; runs the graph only (asynchronous). */
 trax_status trax_stage_batch(trax_ctx *ctx, const trax_event_batch *in);

@@ -39,6 +39,19 @@ struct DevBuf {
     size_t bytes = 0;
 };
 
+/* One of the two batches a context can have in flight
+ * (trax_submit_batch / trax_wait_batch): its own inputs, upload staging,
+ * graph and result counts. */
+struct AsyncSlot {
+    DevBuf in_cols[7], seg;
+    uint32_t *h_meta = nullptr;   /* pinned: segment starts, counts, (events, hits) */
+    DevState *h_snap = nullptr;   /* pinned: the run's counts, written by the device */
+    cudaEvent_t h2d_done = nullptr, done = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    bool busy = false;
+    uint32_t ticket = 0, capacity = 0;
+};
+
 }  // namespace
 
 struct trax_ctx {
@@ -81,6 +94,10 @@ struct trax_ctx {
     uint32_t gb_stage = 0;                /* k_grid_build staged-segment capacity */
     cudaGraphExec_t graph = nullptr;
     uint32_t staged_events = 0, staged_hits = 0;
+    /* streaming submission: two slots, uploads on their own stream */
+    AsyncSlot aslot[2];
+    cudaStream_t copy_stream = nullptr;
+    uint32_t next_ticket = 0;
     /* per-kernel timing marks (events recorded between launches) */
     bool profiling = false;
     int n_marks = 0;
@@ -96,6 +113,43 @@ trax_status fail(trax_ctx *c, trax_status s, const std::string &msg)
     return s;
 }
 
+/* Executable graphs hold the reserved buffers' addresses; any change of the
+ * captured parameters or buffers drops them all (they are re-captured on
+ * their next launch). */
+bool has_graph(const trax_ctx *ctx)
+{
+    return ctx->graph || ctx->aslot[0].graph || ctx->aslot[1].graph;
+}
+
+void drop_graphs(trax_ctx *ctx)
+{
+    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+    ctx->graph = nullptr;
+    for (auto &a : ctx->aslot) {
+        if (a.graph) cudaGraphExecDestroy(a.graph);
+        a.graph = nullptr;
+    }
+}
+
+/* Frees the streaming slots (after their work is done); trax_submit_batch
+ * creates them again at the reservation's sizes. */
+void free_async(trax_ctx *ctx)
+{
+    for (auto &a : ctx->aslot) {
+        if (a.done) cudaEventSynchronize(a.done);
+        if (a.graph) cudaGraphExecDestroy(a.graph);
+        for (auto &b : a.in_cols) if (b.p) cudaFree(b.p);
+        if (a.seg.p) cudaFree(a.seg.p);
+        if (a.h_meta) cudaFreeHost(a.h_meta);
+        if (a.h_snap) cudaFreeHost(a.h_snap);
+        if (a.h2d_done) cudaEventDestroy(a.h2d_done);
+        if (a.done) cudaEventDestroy(a.done);
+        a = AsyncSlot{};
+    }
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    ctx->copy_stream = nullptr;
+}
+
 #define CK(call)                                                                          \
     do {                                                                                  \
         cudaError_t e_ = (call);                                                          \
@@ -107,7 +161,7 @@ trax_status ensure(trax_ctx *ctx, DevBuf &b, size_t bytes)
 {
     if (bytes == 0) bytes = 16;
     if (b.bytes >= bytes) return TRAX_OK;
-    if (ctx->reserved && ctx->graph) {
+    if (ctx->reserved && has_graph(ctx)) {
         /* buffers captured in the graph must not move */
         return fail(ctx, TRAX_ERR_OOM, "scratch beyond the reserved size");
     }
@@ -698,6 +752,7 @@ void trax_ctx_destroy(trax_ctx *ctx)
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_async(ctx);
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
     DevBuf *bufs[] = {&ctx->seg, &ctx->g_start, &ctx->g_base, &ctx->slots, &ctx->pexcl,
                       &ctx->cexcl, &ctx->st0, &ctx->st1, &ctx->st2, &ctx->st3, &ctx->zi,
@@ -724,10 +779,7 @@ trax_status trax_ctx_set_stream(trax_ctx *ctx, void *stream)
     if (!ctx) return TRAX_ERR_BAD_ARG;
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
-    if (ctx->graph) {
-        cudaGraphExecDestroy(ctx->graph);
-        ctx->graph = nullptr;
-    }
+    drop_graphs(ctx);
     return TRAX_OK;
 }
 
@@ -782,10 +834,7 @@ trax_status trax_configure(trax_ctx *ctx, const trax_config *cfg)
         kp.pair_record = 2;
     }
     ctx->configured = true;
-    if (ctx->graph) {
-        cudaGraphExecDestroy(ctx->graph);
-        ctx->graph = nullptr;
-    }
+    drop_graphs(ctx);
     return TRAX_OK;
 }
 
@@ -798,10 +847,7 @@ trax_status trax_set_tuning(trax_ctx *ctx, const trax_tuning *t)
     ctx->kp.run_walk = t->run_walk;
     ctx->kp.zi_min = t->index_min;
     ctx->kp.pair_record = t->pair_record;
-    if (ctx->graph) {
-        cudaGraphExecDestroy(ctx->graph);
-        ctx->graph = nullptr;
-    }
+    drop_graphs(ctx);
     return TRAX_OK;
 }
 
@@ -812,10 +858,7 @@ trax_status trax_set_pair_generator(trax_ctx *ctx, int generator)
         return fail(ctx, TRAX_ERR_BAD_ARG, "unknown pair generator");
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->pair_generator = generator;
-    if (ctx->graph) {
-        cudaGraphExecDestroy(ctx->graph);
-        ctx->graph = nullptr;
-    }
+    drop_graphs(ctx);
     return TRAX_OK;
 }
 
@@ -1326,10 +1369,9 @@ trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers
     g.n_layers = max_layers;
     trax_status s = check_grid(ctx, &g);
     if (s != TRAX_OK) return s;
-    if (ctx->graph) {
-        cudaGraphExecDestroy(ctx->graph);
-        ctx->graph = nullptr;
-    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    drop_graphs(ctx);
+    free_async(ctx);
     ctx->reserved = false;
     const uint32_t T = ctx->kp.n_lt;
     const uint64_t C = (uint64_t)(g.n_sectors_z + 1) * (g.n_sectors_phi + 1);
@@ -1394,19 +1436,22 @@ SortedCols reserved_sorted(trax_ctx *ctx)
     return s;
 }
 
-/* The whole chain on reserved buffers; sizes come from DevState. */
-trax_status enqueue_pipeline(trax_ctx *ctx)
+InCols in_cols_of(const DevBuf *c)
+{
+    return InCols{(const float *)c[0].p, (const float *)c[1].p, (const float *)c[2].p,
+                  (const uint32_t *)c[3].p, (const uint32_t *)c[4].p, (const uint32_t *)c[5].p,
+                  (const uint32_t *)c[6].p};
+}
+
+/* The whole chain on reserved buffers, reading the inputs `ic` and the
+ * segment table `seg`; sizes come from DevState. */
+trax_status enqueue_pipeline(trax_ctx *ctx, const InCols &ic, const uint32_t *seg)
 {
     const uint32_t T = ctx->kp.n_lt;
     const uint32_t G = ctx->r_events * T;
     const uint32_t nseg = ctx->r_events * ctx->r_layers;
-    InCols ic{(const float *)ctx->in_cols[0].p, (const float *)ctx->in_cols[1].p,
-              (const float *)ctx->in_cols[2].p, (const uint32_t *)ctx->in_cols[3].p,
-              (const uint32_t *)ctx->in_cols[4].p, (const uint32_t *)ctx->in_cols[5].p,
-              (const uint32_t *)ctx->in_cols[6].p};
     const SortedCols sc = reserved_sorted(ctx);
     uint32_t *grid = (uint32_t *)ctx->grid_buf.p;
-    const uint32_t *seg = (const uint32_t *)ctx->r_seg.p;
     trax_status s = begin_marks(ctx);
     if (s != TRAX_OK) return s;
     CK(cudaMemsetAsync(&ctx->d_state->n_outer, 0, sizeof(DevState) - 8, ctx->stream));
@@ -1429,6 +1474,31 @@ trax_status enqueue_pipeline(trax_ctx *ctx)
                           G);
 }
 
+/* Writes a finished batch's results into host memory (the caller's pinned
+ * output buffers, addressed from the device) and the run's counts into the
+ * slot's pinned snapshot; tracklets only when they fit the capacity. */
+__global__ void k_emit(const DevState *st, DevState *snap, const uint32_t *orig,
+                       const uint32_t *t1, const uint32_t *t2, const uint32_t *t3, uint32_t r_trk,
+                       uint32_t *o1, uint32_t *o2, uint32_t *o3, uint32_t cap,
+                       const uint32_t *off, uint32_t *o_off, uint32_t n_off)
+{
+    uint32_t n = st->n_trk;
+    if (n > r_trk) n = r_trk;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    if (n <= cap) {
+        for (uint32_t i = tid; i < n; i += stride) {
+            const uint32_t a = t1[i], b = t2[i], c = t3[i];
+            if (o1) o1[i] = orig ? orig[a] : a;
+            if (o2) o2[i] = orig ? orig[b] : b;
+            if (o3) o3[i] = orig ? orig[c] : c;
+        }
+    }
+    if (o_off)
+        for (uint32_t g = tid; g < n_off; g += stride) o_off[g] = off[g];
+    if (tid == 0) *snap = *st;
+}
+
 __global__ void k_map_orig(const uint32_t *orig, const uint32_t *t1, const uint32_t *t2,
                            const uint32_t *t3, uint32_t *m1, uint32_t *m2, uint32_t *m3,
                            uint32_t cap, const DevState *st)
@@ -1444,6 +1514,26 @@ __global__ void k_map_orig(const uint32_t *orig, const uint32_t *t1, const uint3
 
 }  // namespace
 
+/* Segment table of a batch at the reservation's stride: starts in
+ * hs[0, nseg_r), counts in hs[nseg_r, 2 nseg_r), then (events, hits). */
+static trax_status fill_meta(trax_ctx *ctx, const trax_event_batch *in, uint32_t *hs,
+                             size_t nseg_r)
+{
+    const uint32_t E = in->n_events, L = in->n_layers;
+    uint32_t *hn = hs + nseg_r;
+    uint64_t run = 0;
+    for (uint32_t e = 0; e < E; ++e)
+        for (uint32_t l = 0; l < L; ++l) {
+            hs[(size_t)e * L + l] = (uint32_t)run;
+            hn[(size_t)e * L + l] = in->layer_nhits[(size_t)e * L + l];
+            run += in->layer_nhits[(size_t)e * L + l];
+        }
+    if (run != in->n_hits) return fail(ctx, TRAX_ERR_BAD_INPUT, "layer_nhits do not sum to n_hits");
+    hs[2 * nseg_r] = E;
+    hs[2 * nseg_r + 1] = in->n_hits;
+    return TRAX_OK;
+}
+
 trax_status trax_stage_batch(trax_ctx *ctx, const trax_event_batch *in)
 {
     if (!ctx || !in) return TRAX_ERR_BAD_ARG;
@@ -1456,16 +1546,7 @@ trax_status trax_stage_batch(trax_ctx *ctx, const trax_event_batch *in)
     trax_status s = ensure_stage(ctx, 2 * nseg_r + 4);
     if (s != TRAX_OK) return s;
     uint32_t *hs = ctx->h_stage, *hn = ctx->h_stage + nseg_r;
-    uint64_t run = 0;
-    for (uint32_t e = 0; e < E; ++e)
-        for (uint32_t l = 0; l < L; ++l) {
-            hs[(size_t)e * L + l] = (uint32_t)run;
-            hn[(size_t)e * L + l] = in->layer_nhits[(size_t)e * L + l];
-            run += in->layer_nhits[(size_t)e * L + l];
-        }
-    if (run != in->n_hits) return fail(ctx, TRAX_ERR_BAD_INPUT, "layer_nhits do not sum to n_hits");
-    hs[2 * nseg_r] = E;
-    hs[2 * nseg_r + 1] = in->n_hits;
+    if ((s = fill_meta(ctx, in, hs, nseg_r)) != TRAX_OK) return s;
     const size_t nseg = (size_t)E * L;
     CK(cudaMemcpyAsync(ctx->r_seg.p, hs, nseg * 4, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync((uint32_t *)ctx->r_seg.p + nseg_r, hn, nseg * 4, cudaMemcpyHostToDevice, ctx->stream));
@@ -1480,29 +1561,39 @@ trax_status trax_stage_batch(trax_ctx *ctx, const trax_event_batch *in)
     return TRAX_OK;
 }
 
+/* Captures the chain over the inputs `ic` / `seg` into *exec. */
+trax_status capture_pipeline(trax_ctx *ctx, const InCols &ic, const uint32_t *seg,
+                             cudaGraphExec_t *exec)
+{
+    const uint32_t nseg = ctx->r_events * ctx->r_layers;
+    trax_status s0 = grid_plan(ctx, ctx->kp.C, nseg ? ctx->r_hits / nseg : 0);
+    if (s0 != TRAX_OK) return s0;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    trax_status s = enqueue_pipeline(ctx, ic, seg);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (s != TRAX_OK) {
+        if (g) cudaGraphDestroy(g);
+        return s;
+    }
+    if (e != cudaSuccess) return fail(ctx, TRAX_ERR_DEVICE, cudaGetErrorString(e));
+    e = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        *exec = nullptr;
+        return fail(ctx, TRAX_ERR_DEVICE, cudaGetErrorString(e));
+    }
+    return TRAX_OK;
+}
+
 trax_status trax_run_staged(trax_ctx *ctx)
 {
     if (!ctx || !ctx->reserved) return TRAX_ERR_BAD_ARG;
     fill_grid_params(ctx->kp, &ctx->r_grid);
     if (!ctx->graph) {
-        const uint32_t nseg = ctx->r_events * ctx->r_layers;
-        trax_status s0 = grid_plan(ctx, ctx->kp.C, nseg ? ctx->r_hits / nseg : 0);
-        if (s0 != TRAX_OK) return s0;
-        cudaGraph_t g = nullptr;
-        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        trax_status s = enqueue_pipeline(ctx);
-        cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
-        if (s != TRAX_OK) {
-            if (g) cudaGraphDestroy(g);
-            return s;
-        }
-        if (e != cudaSuccess) return fail(ctx, TRAX_ERR_DEVICE, cudaGetErrorString(e));
-        e = cudaGraphInstantiate(&ctx->graph, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) {
-            ctx->graph = nullptr;
-            return fail(ctx, TRAX_ERR_DEVICE, cudaGetErrorString(e));
-        }
+        trax_status s = capture_pipeline(ctx, in_cols_of(ctx->in_cols),
+                                         (const uint32_t *)ctx->r_seg.p, &ctx->graph);
+        if (s != TRAX_OK) return s;
     }
     CK(cudaGraphLaunch(ctx->graph, ctx->stream));
     return TRAX_OK;
@@ -1512,16 +1603,15 @@ trax_status trax_run_staged_eager(trax_ctx *ctx)
 {
     if (!ctx || !ctx->reserved) return TRAX_ERR_BAD_ARG;
     fill_grid_params(ctx->kp, &ctx->r_grid);
-    return enqueue_pipeline(ctx);
+    return enqueue_pipeline(ctx, in_cols_of(ctx->in_cols), (const uint32_t *)ctx->r_seg.p);
 }
 
 trax_status trax_set_profiling(trax_ctx *ctx, int on)
 {
     if (!ctx) return TRAX_ERR_BAD_ARG;
-    if ((bool)on != ctx->profiling && ctx->graph) {
+    if ((bool)on != ctx->profiling && has_graph(ctx)) {
         CK(cudaStreamSynchronize(ctx->stream));
-        cudaGraphExecDestroy(ctx->graph);
-        ctx->graph = nullptr;
+        drop_graphs(ctx);
     }
     ctx->profiling = on != 0;
     return TRAX_OK;
@@ -1582,6 +1672,124 @@ trax_status trax_seed_batch(trax_ctx *ctx, const trax_event_batch *in, trax_batc
         return fail(ctx, (trax_status)out->counts.status, buf);
     }
     if (!fits) return fail(ctx, TRAX_ERR_CAPACITY, "result larger than the output capacity");
+    return TRAX_OK;
+}
+
+/* Creates a streaming slot's buffers at the reservation's sizes. */
+static trax_status ensure_slot(trax_ctx *ctx, AsyncSlot &a)
+{
+    if (!ctx->copy_stream) CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    if (a.h_meta) return TRAX_OK;
+    const size_t nseg_r = (size_t)ctx->r_events * ctx->r_layers;
+    /* plain allocations: the slot's graph is captured after them */
+    for (auto &b : a.in_cols) {
+        b.bytes = std::max<size_t>((size_t)ctx->r_hits * 4, 16);
+        CK(cudaMalloc(&b.p, b.bytes));
+    }
+    a.seg.bytes = (2 * nseg_r + 2) * 4;
+    CK(cudaMalloc(&a.seg.p, a.seg.bytes));
+    CK(cudaMallocHost(&a.h_meta, (2 * nseg_r + 2) * 4));
+    CK(cudaMallocHost(&a.h_snap, sizeof(DevState)));
+    CK(cudaEventCreateWithFlags(&a.h2d_done, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&a.done, cudaEventDisableTiming));
+    return TRAX_OK;
+}
+
+/* Device address of a pinned host buffer (null stays null). */
+static trax_status device_alias(trax_ctx *ctx, void *host, uint32_t **dev)
+{
+    *dev = nullptr;
+    if (!host) return TRAX_OK;
+    void *d = nullptr;
+    if (cudaHostGetDevicePointer(&d, host, 0) != cudaSuccess || !d) {
+        cudaGetLastError();
+        return fail(ctx, TRAX_ERR_BAD_ARG,
+                    "trax_submit_batch: output buffers must be pinned host memory");
+    }
+    *dev = (uint32_t *)d;
+    return TRAX_OK;
+}
+
+trax_status trax_submit_batch(trax_ctx *ctx, const trax_event_batch *in,
+                              const trax_batch_result *out, uint32_t *ticket)
+{
+    if (!ctx || !in || !out || !ticket) return TRAX_ERR_BAD_ARG;
+    if (!ctx->reserved) return fail(ctx, TRAX_ERR_BAD_ARG, "trax_reserve not called");
+    if (in->n_events > ctx->r_events || in->n_layers != ctx->r_layers || in->n_hits > ctx->r_hits)
+        return fail(ctx, TRAX_ERR_CAPACITY, "batch larger than the reservation");
+    AsyncSlot &a = ctx->aslot[ctx->next_ticket & 1];
+    if (a.busy) return fail(ctx, TRAX_ERR_BAD_ARG, "two batches in flight: wait for the older one first");
+    trax_status s = ensure_slot(ctx, a);
+    if (s != TRAX_OK) return s;
+    uint32_t *o[4];
+    void *hosts[4] = {out->hit1, out->hit2, out->hit3, out->offsets};
+    for (int i = 0; i < 4; ++i)
+        if ((s = device_alias(ctx, hosts[i], &o[i])) != TRAX_OK) return s;
+    const size_t nseg_r = (size_t)ctx->r_events * ctx->r_layers;
+    const size_t nseg = (size_t)in->n_events * in->n_layers;
+    if ((s = fill_meta(ctx, in, a.h_meta, nseg_r)) != TRAX_OK) return s;
+    /* uploads: the slot's previous batch was waited for, so nothing reads
+     * its inputs any more */
+    uint32_t *seg = (uint32_t *)a.seg.p;
+    CK(cudaMemcpyAsync(seg, a.h_meta, nseg * 4, cudaMemcpyHostToDevice, ctx->copy_stream));
+    CK(cudaMemcpyAsync(seg + nseg_r, a.h_meta + nseg_r, nseg * 4, cudaMemcpyHostToDevice,
+                       ctx->copy_stream));
+    CK(cudaMemcpyAsync(seg + 2 * nseg_r, a.h_meta + 2 * nseg_r, 8, cudaMemcpyHostToDevice,
+                       ctx->copy_stream));
+    const void *src[7] = {in->x, in->y, in->z, in->layer, in->detector_id, in->hit_id, in->event};
+    for (int i = 0; i < 7; ++i)
+        if (in->n_hits)
+            CK(cudaMemcpyAsync(a.in_cols[i].p, src[i], (size_t)in->n_hits * 4,
+                               cudaMemcpyHostToDevice, ctx->copy_stream));
+    CK(cudaEventRecord(a.h2d_done, ctx->copy_stream));
+    /* the chain on the context stream once the upload is in */
+    fill_grid_params(ctx->kp, &ctx->r_grid);
+    if (!a.graph) {
+        if ((s = capture_pipeline(ctx, in_cols_of(a.in_cols), seg, &a.graph)) != TRAX_OK) return s;
+    }
+    CK(cudaStreamWaitEvent(ctx->stream, a.h2d_done, 0));
+    CK(cudaMemcpyAsync(ctx->d_state, seg + 2 * nseg_r, 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaGraphLaunch(a.graph, ctx->stream));
+    const uint32_t n_off = in->n_events * ctx->kp.n_lt + 1;
+    k_emit<<<ctx->blk_small, 256, 0, ctx->stream>>>(
+        ctx->d_state, a.h_snap, out->input_indices ? (const uint32_t *)ctx->srt_cols[8].p : nullptr,
+        (const uint32_t *)ctx->trk_cols[0].p, (const uint32_t *)ctx->trk_cols[1].p,
+        (const uint32_t *)ctx->trk_cols[2].p, ctx->r_trk, o[0], o[1], o[2], out->capacity,
+        (const uint32_t *)ctx->trk_off.p, o[3], n_off);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(a.done, ctx->stream));
+    a.busy = true;
+    a.ticket = ctx->next_ticket++;
+    a.capacity = out->capacity;
+    *ticket = a.ticket;
+    return TRAX_OK;
+}
+
+trax_status trax_wait_batch(trax_ctx *ctx, uint32_t ticket, trax_batch_result *out)
+{
+    if (!ctx || !out) return TRAX_ERR_BAD_ARG;
+    AsyncSlot &a = ctx->aslot[ticket & 1];
+    if (!a.busy || a.ticket != ticket) return fail(ctx, TRAX_ERR_BAD_ARG, "no batch in flight with this ticket");
+    a.busy = false;
+    CK(cudaEventSynchronize(a.done));
+    const DevState &st = *a.h_snap;
+    out->counts.n_hits = st.n_hits;
+    out->counts.n_pairs = st.n_pairs;
+    out->counts.pair_slots = st.pair_slots;
+    out->counts.n_candidates = st.n_cands;
+    out->counts.cand_slots = st.cand_slots;
+    out->counts.cand_truncated = st.cand_truncated;
+    out->counts.n_tracklets = st.n_trk;
+    out->counts.status = st.status;
+    out->counts.error_detail = st.detail;
+    out->n_tracklets = st.n_trk;
+    if (st.status != TRAX_OK) {
+        char buf[96];
+        snprintf(buf, sizeof buf, "device status %u detail %u", st.status, st.detail);
+        return fail(ctx, (trax_status)st.status, buf);
+    }
+    if (st.n_trk > ctx->r_trk || st.n_trk > a.capacity)
+        return fail(ctx, TRAX_ERR_CAPACITY, "result larger than the output capacity");
     return TRAX_OK;
 }
 

@@ -360,7 +360,11 @@ class Pipeline:
         # pinned result buffers, reused by every seed() call
         cap = self.max_tracklets
         self._out = [PinnedBuffer(ctx, 4 * cap, U32) for _ in range(3)]
-        self._off = PinnedBuffer(ctx, 4 * (int(max_events) * self.n_triplets + 1), U32)
+        self._off_len = int(max_events) * self.n_triplets + 1
+        self._off = PinnedBuffer(ctx, 4 * self._off_len, U32)
+        # streaming (submit / wait): two slots, result buffers made on first use
+        self._stream_out = [None, None]
+        self._inflight = {}
 
     def _batch_struct(self, b: EventBatch):
         cols = [np.ascontiguousarray(c) for c in b.columns()]
@@ -384,6 +388,48 @@ class Pipeline:
         if not copy:
             return [x[:n] for x in h], off, r.counts.as_dict()
         return np.stack([x[:n] for x in h], axis=1), off.copy(), r.counts.as_dict()
+
+    def submit(self, b: EventBatch, input_indices=False):
+        """Streaming form (trax_submit_batch): queues `b` and returns a ticket
+        at once; two batches may be in flight, each with its own pinned
+        result buffers.  `b`'s arrays must stay unchanged until wait()."""
+        busy = {v[3] for v in self._inflight.values()}
+        free = [k for k in (0, 1) if k not in busy]
+        if not free:
+            raise RuntimeError("two batches in flight: wait for the older one first")
+        k = free[0]
+        if self._stream_out[k] is None:
+            cap = self.max_tracklets
+            self._stream_out[k] = ([PinnedBuffer(self.ctx, 4 * cap, U32) for _ in range(3)],
+                                   PinnedBuffer(self.ctx, 4 * self._off_len, U32))
+        outs, off = self._stream_out[k]
+        cols = [np.ascontiguousarray(c) for c in b.columns()]
+        ln = np.ascontiguousarray(b.layer_nhits.reshape(-1), dtype=U32)
+        bs = A.TraxEventBatch(b.n_events, b.n_layers, b.n_hits, *[c.ctypes.data for c in cols],
+                              ln.ctypes.data)
+        r = A.TraxBatchResult(outs[0].ptr, outs[1].ptr, outs[2].ptr, off.ptr, self.max_tracklets,
+                              1 if input_indices else 0, 0, A.TraxCounts())
+        t = C.c_uint32()
+        self.ctx._check(self.ctx.lib.trax_submit_batch(self.ctx.h, C.byref(bs), C.byref(r),
+                                                       C.byref(t)))
+        self._inflight[t.value] = (r, cols + [ln], b.n_events, k)
+        return t.value
+
+    def wait(self, ticket, copy=True):
+        """Waits for a submitted batch; returns (tracklets, offsets, counts)
+        like seed() (copy=False: views of the batch's pinned buffers, valid
+        until the next submit)."""
+        if ticket not in self._inflight:
+            raise RuntimeError(f"no batch in flight with ticket {ticket}")
+        r, _, n_events, k = self._inflight.pop(ticket)
+        self.ctx._check(self.ctx.lib.trax_wait_batch(self.ctx.h, ticket, C.byref(r)))
+        outs, off = self._stream_out[k]
+        n = r.n_tracklets
+        h = [o.array[:n] for o in outs]
+        o = off.array[: n_events * self.n_triplets + 1]
+        if not copy:
+            return h, o, r.counts.as_dict()
+        return np.stack(h, axis=1), o.copy(), r.counts.as_dict()
 
     def stage(self, b: EventBatch):
         bs = self._batch_struct(b)

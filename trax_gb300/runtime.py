@@ -103,6 +103,9 @@ _SIGS = {
     "trax_seed_batch": (C.c_int, [C.c_void_p, C.POINTER(A.TraxEventBatch),
                                   C.POINTER(A.TraxBatchResult)]),
     "trax_stage_batch": (C.c_int, [C.c_void_p, C.POINTER(A.TraxEventBatch)]),
+    "trax_submit_batch": (C.c_int, [C.c_void_p, C.POINTER(A.TraxEventBatch),
+                                    C.POINTER(A.TraxBatchResult), C.POINTER(C.c_uint32)]),
+    "trax_wait_batch": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(A.TraxBatchResult)]),
     "trax_run_staged": (C.c_int, [C.c_void_p]),
     "trax_run_staged_eager": (C.c_int, [C.c_void_p]),
     "trax_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
