@@ -1602,10 +1602,6 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
     for (uint32_t zs = zlo; zs < zhi; ++zs) {
         const bool inA = zs >= w.zLowSector[0] && zs < w.zHighSector[0];
         const bool inB = zs >= w.zLowSector[1] && zs < w.zHighSector[1];
-        const uint32_t kA0 = zkey(w.zLow[0]), kA1 = zkey(w.zHigh[0]);
-        const uint32_t kB0 = zkey(w.zLow[1]), kB1 = zkey(w.zHigh[1]);
-        const uint32_t keyLo = min(inA ? kA0 : 0xffffffffu, inB ? kB0 : 0xffffffffu);
-        const uint32_t keyHi = max(inA ? kA1 : 0u, inB ? kB1 : 0u);
         const uint32_t *row = lGrid3 + zs * P1;
         const ZScreen scr = zscreen_make(inA, w.zLow[0], w.zHigh[0], inB, w.zLow[1], w.zHigh[1]);
         /* the exact test of a hit that passed the screen (walks visit in
@@ -1639,6 +1635,9 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
                     zscreen_walk(ZH, ca, cb, scr, exact);
                     continue;
                 }
+                const uint32_t keyLo = min(inA ? zkey(w.zLow[0]) : 0xffffffffu,
+                                           inB ? zkey(w.zLow[1]) : 0xffffffffu);
+                const uint32_t keyHi = max(inA ? zkey(w.zHigh[0]) : 0u, inB ? zkey(w.zHigh[1]) : 0u);
                 uint32_t lo = ca, hi = cb;
                 while (lo < hi) {
                     const uint32_t m = (lo + hi) >> 1;
