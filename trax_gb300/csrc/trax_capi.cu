@@ -437,10 +437,14 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
     return mark(ctx, "predict_offsets");
 }
 
+/* cand_offsets: the chain's own candidate offsets (the batched pipeline),
+ * which let the tracklet offsets come from the accept mask; null (a stage
+ * call with the caller's candidates) derives them from the tracklets' hits
+ * as the reference does. */
 trax_status enqueue_filter(trax_ctx *ctx, const SortedCols &h, const uint2 *pairs,
                            const uint2 *cands, uint32_t cand_cap, uint32_t *t1, uint32_t *t2,
                            uint32_t *t3, uint32_t *trk_offsets, uint32_t trk_cap,
-                           uint32_t max_groups)
+                           uint32_t max_groups, const uint32_t *cand_offsets)
 {
     const KParams &kp = ctx->kp;
     trax_status s = need_packed(ctx, h);
@@ -464,6 +468,14 @@ trax_status enqueue_filter(trax_ctx *ctx, const SortedCols &h, const uint2 *pair
     k_filter_store<<<ctx->blk_filter, 256, 0, ctx->stream>>>(pairs, cands, mask, wpos, t1, t2, t3,
                                                              trk_cap, st);
     if ((s = mark(ctx, "filter_store")) != TRAX_OK) return s;
+    bool by_mask = cand_offsets != nullptr;
+    for (uint32_t lt = 0; lt < kp.n_lt; ++lt) by_mask = by_mask && kp.l1[lt] == lt + 1;
+    if (by_mask) {
+        k_trk_offsets_mask<<<ctx->blk_small, 256, 0, ctx->stream>>>(
+            cand_offsets, mask, wpos, trk_offsets, kp.n_lt, cand_cap, trk_cap, st);
+        CK(cudaGetLastError());
+        return mark(ctx, "filter_offsets");
+    }
     k_trk_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(t1, h.event, h.layer, trk_offsets,
                                                            kp.n_lt, trk_cap, st);
     if ((s = mark(ctx, "filter_offsets")) != TRAX_OK) return s;
@@ -1353,7 +1365,7 @@ trax_status trax_triplet_filter(trax_ctx *ctx, const trax_sorted_hits *hits,
     if ((s = with_zphi(ctx, sc, hits->n)) != TRAX_OK) return s;
     return enqueue_filter(ctx, sc, (const uint2 *)pairs->pairs,
                           (const uint2 *)cands->pairs, cands->capacity, out->hit1, out->hit2,
-                          out->hit3, out->offsets, out->capacity, G);
+                          out->hit3, out->offsets, out->capacity, G, nullptr);
 }
 
 /* ---------------------------------------------------------------------- */
@@ -1471,7 +1483,7 @@ trax_status enqueue_pipeline(trax_ctx *ctx, const InCols &ic, const uint32_t *se
                           (const uint2 *)ctx->cands_buf.p, ctx->r_cands,
                           (uint32_t *)ctx->trk_cols[0].p, (uint32_t *)ctx->trk_cols[1].p,
                           (uint32_t *)ctx->trk_cols[2].p, (uint32_t *)ctx->trk_off.p, ctx->r_trk,
-                          G);
+                          G, (const uint32_t *)ctx->cand_off.p);
 }
 
 /* Writes a finished batch's results into host memory (the caller's pinned

@@ -1964,6 +1964,33 @@ __global__ void k_trk_offsets(const uint32_t *t1, const uint32_t *EVENT, const u
     }
 }
 
+/* The same offsets when every candidate group is its tracklets' group (the
+ * chain's own candidates, with each layer triplet starting on layer lt + 1):
+ * the tracklets before group g are the accepted candidates before the
+ * group's first candidate, read from the accept mask and its scanned word
+ * counts -- one thread per group instead of one per tracklet plus the
+ * running maximum. */
+__global__ void k_trk_offsets_mask(const uint32_t *cand_offsets, const uint32_t *mask,
+                                   const uint32_t *word_pos, uint32_t *offsets, uint32_t n_lt,
+                                   uint32_t cand_cap, uint32_t trk_cap, DevState *st)
+{
+    const uint32_t G = st->n_events * n_lt;
+    uint32_t n = st->n_cands;
+    if (n > cand_cap) n = cand_cap;
+    const uint32_t total = st->n_trk;
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g <= G; g += gridDim.x * blockDim.x) {
+        uint32_t q = cand_offsets[g];
+        uint32_t v;
+        if (q >= n) {
+            v = total;
+        } else {
+            const uint32_t b = q & 31u;
+            v = word_pos[q >> 5] + (b ? __popc(mask[q >> 5] & ((1u << b) - 1u)) : 0u);
+        }
+        offsets[g] = v < trk_cap ? v : trk_cap;
+    }
+}
+
 /* filterOffsetMonotonizeStore with sequential semantics: a zero entry takes
  * the previous value, i.e. a running maximum.  One CTA. */
 __global__ void __launch_bounds__(1024) k_monotonize(uint32_t *offsets, uint32_t n_lt, DevState *st)
