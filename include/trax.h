@@ -506,14 +506,15 @@ trax_status trax_seed_batch(trax_ctx *ctx, const trax_event_batch *in, trax_batc
 /* Streaming form of trax_seed_batch (the reference's per-group loop in
  * TripletBuilder.cpp:183-285, with the next group's upload overlapping this
  * group's chain).  trax_submit_batch queues one batch -- its upload on the
- * context's copy stream, the chain's graph, the results written by the
- * device straight into the output buffers -- and returns at once with a
- * ticket; trax_wait_batch waits for that batch and fills n_tracklets and
- * counts (status and capacity errors as trax_seed_batch).  Two batches may be
- * in flight; a third submit before a wait returns TRAX_ERR_BAD_ARG.  The
- * output buffers (hit1..3, offsets) must be pinned host memory
- * (trax_host_alloc_pinned or cudaHostAlloc); the input arrays must stay
- * unchanged until the wait returns. */
+ * context's copy stream, then the chain's graph and a copy of the results
+ * into the batch's own device buffers -- and returns at once with a ticket;
+ * trax_wait_batch waits for that batch, downloads its tracklets and offsets
+ * into the output buffers given at submit (on a third stream, while the next
+ * batch computes) and fills n_tracklets and counts (status and capacity
+ * errors as trax_seed_batch).  Two batches may be in flight; a third submit
+ * before a wait returns TRAX_ERR_BAD_ARG.  Pinned host buffers
+ * (trax_host_alloc_pinned or cudaHostAlloc) make the copies asynchronous;
+ * inputs and outputs must stay in place until the wait returns. */
 trax_status trax_submit_batch(trax_ctx *ctx, const trax_event_batch *in,
                               const trax_batch_result *out, uint32_t *ticket);
 trax_status trax_wait_batch(trax_ctx *ctx, uint32_t ticket, trax_batch_result *out);

@@ -44,12 +44,14 @@ struct DevBuf {
  * graph and result counts. */
 struct AsyncSlot {
     DevBuf in_cols[7], seg;
+    DevBuf res[3], res_off;       /* the batch's tracklets and offsets, kept until read */
     uint32_t *h_meta = nullptr;   /* pinned: segment starts, counts, (events, hits) */
     DevState *h_snap = nullptr;   /* pinned: the run's counts, written by the device */
     cudaEvent_t h2d_done = nullptr, done = nullptr;
     cudaGraphExec_t graph = nullptr;
     bool busy = false;
-    uint32_t ticket = 0, capacity = 0;
+    uint32_t ticket = 0, capacity = 0, n_off = 0;
+    uint32_t *out[4] = {};        /* the caller's host outputs: hit1..3, offsets */
 };
 
 }  // namespace
@@ -96,7 +98,8 @@ struct trax_ctx {
     uint32_t staged_events = 0, staged_hits = 0;
     /* streaming submission: two slots, uploads on their own stream */
     AsyncSlot aslot[2];
-    cudaStream_t copy_stream = nullptr;
+    cudaStream_t copy_stream = nullptr;   /* uploads */
+    cudaStream_t d2h_stream = nullptr;    /* result downloads */
     uint32_t next_ticket = 0;
     /* per-kernel timing marks (events recorded between launches) */
     bool profiling = false;
@@ -139,6 +142,8 @@ void free_async(trax_ctx *ctx)
         if (a.done) cudaEventSynchronize(a.done);
         if (a.graph) cudaGraphExecDestroy(a.graph);
         for (auto &b : a.in_cols) if (b.p) cudaFree(b.p);
+        for (auto &b : a.res) if (b.p) cudaFree(b.p);
+        if (a.res_off.p) cudaFree(a.res_off.p);
         if (a.seg.p) cudaFree(a.seg.p);
         if (a.h_meta) cudaFreeHost(a.h_meta);
         if (a.h_snap) cudaFreeHost(a.h_snap);
@@ -147,7 +152,8 @@ void free_async(trax_ctx *ctx)
         a = AsyncSlot{};
     }
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
-    ctx->copy_stream = nullptr;
+    if (ctx->d2h_stream) cudaStreamDestroy(ctx->d2h_stream);
+    ctx->copy_stream = ctx->d2h_stream = nullptr;
 }
 
 #define CK(call)                                                                          \
@@ -1486,9 +1492,10 @@ trax_status enqueue_pipeline(trax_ctx *ctx, const InCols &ic, const uint32_t *se
                           G, (const uint32_t *)ctx->cand_off.p);
 }
 
-/* Writes a finished batch's results into host memory (the caller's pinned
- * output buffers, addressed from the device) and the run's counts into the
- * slot's pinned snapshot; tracklets only when they fit the capacity. */
+/* Copies a finished batch's results into the slot's own device buffers (the
+ * next batch overwrites the chain's), mapping to input positions on
+ * request, and the run's counts into the slot's pinned snapshot; tracklets
+ * only when they fit the capacity. */
 __global__ void k_emit(const DevState *st, DevState *snap, const uint32_t *orig,
                        const uint32_t *t1, const uint32_t *t2, const uint32_t *t3, uint32_t r_trk,
                        uint32_t *o1, uint32_t *o2, uint32_t *o3, uint32_t cap,
@@ -1691,6 +1698,7 @@ trax_status trax_seed_batch(trax_ctx *ctx, const trax_event_batch *in, trax_batc
 static trax_status ensure_slot(trax_ctx *ctx, AsyncSlot &a)
 {
     if (!ctx->copy_stream) CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    if (!ctx->d2h_stream) CK(cudaStreamCreateWithFlags(&ctx->d2h_stream, cudaStreamNonBlocking));
     if (a.h_meta) return TRAX_OK;
     const size_t nseg_r = (size_t)ctx->r_events * ctx->r_layers;
     /* plain allocations: the slot's graph is captured after them */
@@ -1700,25 +1708,16 @@ static trax_status ensure_slot(trax_ctx *ctx, AsyncSlot &a)
     }
     a.seg.bytes = (2 * nseg_r + 2) * 4;
     CK(cudaMalloc(&a.seg.p, a.seg.bytes));
+    for (auto &b : a.res) {
+        b.bytes = std::max<size_t>((size_t)ctx->r_trk * 4, 16);
+        CK(cudaMalloc(&b.p, b.bytes));
+    }
+    a.res_off.bytes = ((size_t)ctx->r_events * ctx->kp.n_lt + 1) * 4;
+    CK(cudaMalloc(&a.res_off.p, a.res_off.bytes));
     CK(cudaMallocHost(&a.h_meta, (2 * nseg_r + 2) * 4));
     CK(cudaMallocHost(&a.h_snap, sizeof(DevState)));
     CK(cudaEventCreateWithFlags(&a.h2d_done, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&a.done, cudaEventDisableTiming));
-    return TRAX_OK;
-}
-
-/* Device address of a pinned host buffer (null stays null). */
-static trax_status device_alias(trax_ctx *ctx, void *host, uint32_t **dev)
-{
-    *dev = nullptr;
-    if (!host) return TRAX_OK;
-    void *d = nullptr;
-    if (cudaHostGetDevicePointer(&d, host, 0) != cudaSuccess || !d) {
-        cudaGetLastError();
-        return fail(ctx, TRAX_ERR_BAD_ARG,
-                    "trax_submit_batch: output buffers must be pinned host memory");
-    }
-    *dev = (uint32_t *)d;
     return TRAX_OK;
 }
 
@@ -1733,10 +1732,6 @@ trax_status trax_submit_batch(trax_ctx *ctx, const trax_event_batch *in,
     if (a.busy) return fail(ctx, TRAX_ERR_BAD_ARG, "two batches in flight: wait for the older one first");
     trax_status s = ensure_slot(ctx, a);
     if (s != TRAX_OK) return s;
-    uint32_t *o[4];
-    void *hosts[4] = {out->hit1, out->hit2, out->hit3, out->offsets};
-    for (int i = 0; i < 4; ++i)
-        if ((s = device_alias(ctx, hosts[i], &o[i])) != TRAX_OK) return s;
     const size_t nseg_r = (size_t)ctx->r_events * ctx->r_layers;
     const size_t nseg = (size_t)in->n_events * in->n_layers;
     if ((s = fill_meta(ctx, in, a.h_meta, nseg_r)) != TRAX_OK) return s;
@@ -1766,13 +1761,19 @@ trax_status trax_submit_batch(trax_ctx *ctx, const trax_event_batch *in,
     k_emit<<<ctx->blk_small, 256, 0, ctx->stream>>>(
         ctx->d_state, a.h_snap, out->input_indices ? (const uint32_t *)ctx->srt_cols[8].p : nullptr,
         (const uint32_t *)ctx->trk_cols[0].p, (const uint32_t *)ctx->trk_cols[1].p,
-        (const uint32_t *)ctx->trk_cols[2].p, ctx->r_trk, o[0], o[1], o[2], out->capacity,
-        (const uint32_t *)ctx->trk_off.p, o[3], n_off);
+        (const uint32_t *)ctx->trk_cols[2].p, ctx->r_trk, (uint32_t *)a.res[0].p,
+        (uint32_t *)a.res[1].p, (uint32_t *)a.res[2].p, out->capacity,
+        (const uint32_t *)ctx->trk_off.p, (uint32_t *)a.res_off.p, n_off);
     CK(cudaGetLastError());
     CK(cudaEventRecord(a.done, ctx->stream));
     a.busy = true;
     a.ticket = ctx->next_ticket++;
     a.capacity = out->capacity;
+    a.n_off = n_off;
+    a.out[0] = out->hit1;
+    a.out[1] = out->hit2;
+    a.out[2] = out->hit3;
+    a.out[3] = out->offsets;
     *ticket = a.ticket;
     return TRAX_OK;
 }
@@ -1802,6 +1803,15 @@ trax_status trax_wait_batch(trax_ctx *ctx, uint32_t ticket, trax_batch_result *o
     }
     if (st.n_trk > ctx->r_trk || st.n_trk > a.capacity)
         return fail(ctx, TRAX_ERR_CAPACITY, "result larger than the output capacity");
+    /* the download, on its own stream: it overlaps the next batch's chain */
+    for (int i = 0; i < 3; ++i)
+        if (a.out[i] && st.n_trk)
+            CK(cudaMemcpyAsync(a.out[i], a.res[i].p, (size_t)st.n_trk * 4, cudaMemcpyDeviceToHost,
+                               ctx->d2h_stream));
+    if (a.out[3])
+        CK(cudaMemcpyAsync(a.out[3], a.res_off.p, (size_t)a.n_off * 4, cudaMemcpyDeviceToHost,
+                           ctx->d2h_stream));
+    CK(cudaStreamSynchronize(ctx->d2h_stream));
     return TRAX_OK;
 }
 
