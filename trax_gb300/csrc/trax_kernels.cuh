@@ -1081,7 +1081,7 @@ __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *
  * again.
  */
 constexpr int kPairKeep = 16;
-constexpr int kPairUnroll = 4;
+constexpr int kPairUnroll = 8;
 
 /* The walk of one outer hit; visit(j, both) gets every accepted inner hit in
  * ascending order (both: a B accept that also lies in A, which the
@@ -1110,11 +1110,17 @@ __device__ __forceinline__ void pair_lane_walk(const KParams &kp, const uint32_t
 #pragma unroll
                 for (int u = 0; u < kPairUnroll; ++u)
                     v[u] = j + u < hi ? ZP[j + u] : make_float2(NAN, NAN);  /* NaN fails */
+                /* the tests without branches, then the (few) accepts */
+                uint32_t m = 0;
 #pragma unroll
                 for (int u = 0; u < kPairUnroll; ++u)
-                    if (go && w.zLow <= v[u].x && v[u].x <= w.zHigh &&
-                        phi_in(v[u].y, w.phiLow, w.phiHigh, w.wrap))
-                        go = visit(j + u, inB && j + u >= aLo && j + u < aHi);
+                    m |= (w.zLow <= v[u].x && v[u].x <= w.zHigh &&
+                          phi_in(v[u].y, w.phiLow, w.phiHigh, w.wrap)) ? 1u << u : 0u;
+                while (m && go) {
+                    const uint32_t jj = j + __ffs(m) - 1;
+                    m &= m - 1;
+                    go = visit(jj, inB && jj >= aLo && jj < aHi);
+                }
             }
         };
         range(bLo, bHi, true);
