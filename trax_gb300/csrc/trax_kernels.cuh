@@ -1605,11 +1605,13 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
     cB = 0;
     const uint32_t zlo = min(w.zLowSector[0], w.zLowSector[1]);
     const uint32_t zhi = max(w.zHighSector[0], w.zHighSector[1]);
+    /* one screen for the pair: the union of the two z windows (a row in
+     * only one of them screens a little wider; the exact test decides) */
+    const ZScreen scr = zscreen_make(true, w.zLow[0], w.zHigh[0], true, w.zLow[1], w.zHigh[1]);
     for (uint32_t zs = zlo; zs < zhi; ++zs) {
         const bool inA = zs >= w.zLowSector[0] && zs < w.zHighSector[0];
         const bool inB = zs >= w.zLowSector[1] && zs < w.zHighSector[1];
         const uint32_t *row = lGrid3 + zs * P1;
-        const ZScreen scr = zscreen_make(inA, w.zLow[0], w.zHigh[0], inB, w.zLow[1], w.zHigh[1]);
         /* the exact test of a hit that passed the screen (walks visit in
          * position order, so accepts append) */
         auto exact = [&](uint32_t j) {
@@ -1623,17 +1625,13 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
             return true;
         };
         /* the reference's visits, as runs of whole cells: columns
-         * pLow..pHigh-1, or with wrap-around pLow..P then 0..pHigh-1 */
-        for (int run = 0; run < 2; ++run) {
-            const uint32_t c0 = run == 0 ? w.phiLowSector : 0u;
-            const uint32_t c1 = run == 0 ? (w.wrap ? P1 : w.phiHighSector)
-                                         : (w.wrap ? w.phiHighSector : 0u);
-            if (c1 <= c0) continue;
+         * c0..c1-1 (with wrap-around pLow..P, then 0..pHigh-1) */
+        auto run = [&](uint32_t c0, uint32_t c1) {
             const uint32_t ra = row[c0], rb = row[c1];
             if (rb - ra <= kp.run_walk) {
                 /* a small run: walk its contiguous hits */
                 zscreen_walk(ZH, ra, rb, scr, exact);
-                continue;
+                return;
             }
             for (uint32_t c = c0; c < c1; ++c) {
                 const uint32_t ca = row[c], cb = row[c + 1];
@@ -1661,7 +1659,10 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
                     }
                 }
             }
-        }
+        };
+        const uint32_t c1 = w.wrap ? P1 : w.phiHighSector;
+        if (w.phiLowSector < c1) run(w.phiLowSector, c1);
+        if (w.wrap && w.phiHighSector > 0) run(0, w.phiHighSector);
     }
 }
 
