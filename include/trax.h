@@ -198,12 +198,13 @@ float trax_min_radius_curvature(float min_pt, float bz);
  * never depend on it, only speed: a run of neighbouring cells with at most
  * run_walk hits is walked hit by hit; in larger runs, every cell with more
  * than index_min (<= 256) hits is searched through a per-cell z index.
- * pair_record selects the pair kernel: 2 walks one outer hit per lane; 1 and
- * 0 sweep each outer hit's candidates with the whole warp, replaying the
- * count sweep's ballots for the store (1) or sweeping twice (0).  Sparse
- * events favour walking and pair_record 2, dense (pile-up) events the index
- * and the double sweep.  trax_configure installs run_walk 48, index_min 16,
- * pair_record 2. */
+ * pair_record selects the pair kernels: 3 walks one outer hit per lane in a
+ * count pass, scans the counts and copies the kept accepts in a store pass;
+ * 2 walks one outer hit per lane with a look-back in one kernel; 1 and 0
+ * sweep each outer hit's candidates with the whole warp, replaying the count
+ * sweep's ballots for the store (1) or sweeping twice (0).  Sparse events
+ * favour walking and pair_record 3, dense (pile-up) events the index.
+ * trax_configure installs run_walk 48, index_min 16, pair_record 3. */
 typedef struct trax_tuning {
     uint32_t run_walk;
     uint32_t index_min;

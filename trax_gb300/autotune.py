@@ -42,17 +42,18 @@ def time_staged(ctx: Context, p: Pipeline, reps: int) -> float:
 
 def tune_walk(ctx: Context, p: Pipeline, batch: gen.EventBatch, reps=5,
               candidates=WALK_CANDIDATES):
-    """Stages `batch`, times each (run_walk, index_min) with the pair stage's
-    one-outer-hit-per-lane kernel, then the best of them with the warp-swept
-    pair kernel (replaying its ballots, then sweeping twice), and installs the
-    fastest (run_walk, index_min, pair_record)."""
+    """Stages `batch`, times each (run_walk, index_min) with the split
+    one-outer-hit-per-lane pair stage, then the best of them with the other
+    pair kernels (one outer hit per lane with look-back, the warp sweep
+    replaying its ballots, the warp sweep twice), and installs the fastest
+    (run_walk, index_min, pair_record)."""
     p.stage(batch)
     timings = {}
     for cand in candidates:
-        ctx.set_tuning(*cand, 2)
-        timings[(*cand, 2)] = time_staged(ctx, p, reps)
+        ctx.set_tuning(*cand, 3)
+        timings[(*cand, 3)] = time_staged(ctx, p, reps)
     best = min(timings, key=timings.get)
-    for rec in (1, 0):
+    for rec in (2, 1, 0):
         ctx.set_tuning(best[0], best[1], rec)
         timings[(best[0], best[1], rec)] = time_staged(ctx, p, reps)
     best = min(timings, key=timings.get)

@@ -31,6 +31,9 @@ constexpr int kTimerSlots = 64;
 constexpr int kScanItems = 8;       /* items per thread in k_scan */
 constexpr int kScanThreads = 256;
 constexpr int kTileItems = 32;      /* items per fused pair / predict tile (one warp) */
+/* pair accepts an outer hit keeps for the split store: more than 32 is rare
+ * below pile-up (an outer hit with more walks again in the store) */
+constexpr uint32_t kPairKeepSplit = 32;
 constexpr uint32_t kDefaultRunWalk = 48;  /* see trax_set_tuning */
 constexpr uint32_t kDefaultIndexMin = 16;
 
@@ -81,9 +84,10 @@ struct trax_ctx {
     DevBuf fmask; /* filter accept mask words and their positions */
     DevBuf zphi;  /* packed (z, phi) of the sorted hits */
     DevBuf zh;    /* half-precision z of the sorted hits (candidate screen) */
+    DevBuf pkeep; /* per outer hit: its first kept pair accepts (split pair stage) */
     DevBuf xyzp;  /* packed (x, y, z, phi) of the sorted hits */
     cudaEvent_t timers[kTimerSlots] = {};
-    int blk_pair = 0, blk_pair0 = 0, blk_pair_lane = 0, blk_sector = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
+    int blk_pair = 0, blk_pair0 = 0, blk_pair_lane = 0, blk_pair_count = 0, blk_pair_store = 0, blk_sector = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
 
     /* batched pipeline */
     bool reserved = false;
@@ -362,7 +366,25 @@ trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *gr
     if ((s = mark(ctx, "pair_slots")) != TRAX_OK) return s;
     CK(cudaMemsetAsync(&st->tile_ctr[0], 0, 4, ctx->stream));
     CK(cudaMemsetAsync(ctx->st0.p, 0, (size_t)ntile * 8, ctx->stream));
-    if (sector)
+    if (!sector && kp.pair_record == 3) {
+        /* split: count -> scan of the counts -> store (no look-back waits) */
+        if ((s = ensure(ctx, ctx->pkeep, (size_t)slot_cap * kPairKeepSplit * 4)) != TRAX_OK) return s;
+        uint32_t *pkeep = (uint32_t *)ctx->pkeep.p;
+        k_pair_count_lane<<<ctx->blk_pair_count, kFusedThreads, 0, ctx->stream>>>(
+            kp, grid, h.xyzp, h.zphi, slots, slot_cap, pexcl, pkeep, kPairKeepSplit, st);
+        if ((s = mark(ctx, "pair_gen")) != TRAX_OK) return s;
+        const uint32_t stile = tiles_for(slot_cap, kScanItems * kScanThreads);
+        CK(cudaMemsetAsync(&st->tile_ctr[0], 0, 4, ctx->stream));
+        CK(cudaMemsetAsync(ctx->st0.p, 0, (size_t)stile * 8, ctx->stream));
+        k_scan<kScanItems><<<std::min<uint32_t>(ctx->blk_scan, stile), kScanThreads, 0, ctx->stream>>>(
+            pexcl, pexcl, &st->n_outer, slot_cap, &st->n_pairs, 0,
+            (unsigned long long *)ctx->st0.p, st);
+        if ((s = mark(ctx, "pair_scan")) != TRAX_OK) return s;
+        k_pair_store_lane<<<ctx->blk_pair_store, kFusedThreads, 0, ctx->stream>>>(
+            kp, grid, h.xyzp, h.zphi, slots, slot_cap, pexcl, pkeep, kPairKeepSplit, pairs,
+            pair_cap, st);
+        if ((s = mark(ctx, "pair_store")) != TRAX_OK) return s;
+    } else if (sector)
         k_pair_sector<<<ctx->blk_sector, kFusedThreads, 0, ctx->stream>>>(
             kp, grid, h.z, h.phi, slots, slot_cap, pexcl, pairs, pair_cap,
             (unsigned long long *)ctx->st0.p, st);
@@ -378,7 +400,8 @@ trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *gr
         k_pair_fused<false><<<ctx->blk_pair0, kFusedThreads, 0, ctx->stream>>>(
             kp, grid, h.x, h.y, h.z, h.phi, h.zphi, slots, slot_cap, pexcl, pairs, pair_cap,
             (unsigned long long *)ctx->st0.p, st);
-    if ((s = mark(ctx, "pair_gen")) != TRAX_OK) return s;
+    if (sector || kp.pair_record != 3)
+        if ((s = mark(ctx, "pair_gen")) != TRAX_OK) return s;
     k_group_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(g_base, pexcl, pair_offsets, kp.n_lt,
                                                              slot_cap, &st->n_pairs, pair_cap,
                                                              TRAX_DETAIL_PAIR_CAPACITY, st);
@@ -751,6 +774,10 @@ trax_status trax_ctx_create(trax_ctx **out, int device)
     ctx->blk_pair0 = ctx->sm_count * std::max(b, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_lane, kFusedThreads, 0);
     ctx->blk_pair_lane = ctx->sm_count * std::max(b, 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_count_lane, kFusedThreads, 0);
+    ctx->blk_pair_count = ctx->sm_count * std::max(b, 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_store_lane, kFusedThreads, 0);
+    ctx->blk_pair_store = ctx->sm_count * std::max(b, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_sector, kFusedThreads, 0);
     ctx->blk_sector = ctx->sm_count * std::max(b, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_predict_count, kFusedThreads, 0);
@@ -777,7 +804,7 @@ void trax_ctx_destroy(trax_ctx *ctx)
                       &ctx->conn_keys, &ctx->conn_sums, &ctx->grid_buf,
                       &ctx->pairs_buf, &ctx->pair_off, &ctx->cands_buf, &ctx->cand_off, &ctx->trk_off,
                       &ctx->r_seg, &ctx->ing, &ctx->phys, &ctx->prec, &ctx->zp, &ctx->ptile,
-                      &ctx->fmask, &ctx->zphi, &ctx->zh, &ctx->xyzp};
+                      &ctx->fmask, &ctx->zphi, &ctx->zh, &ctx->xyzp, &ctx->pkeep};
     for (DevBuf *b : bufs) if (b->p) cudaFree(b->p);
     for (auto &b : ctx->in_cols) if (b.p) cudaFree(b.p);
     for (auto &b : ctx->srt_cols) if (b.p) cudaFree(b.p);
@@ -849,7 +876,7 @@ trax_status trax_configure(trax_ctx *ctx, const trax_config *cfg)
     if (kp.run_walk == 0 && kp.zi_min == 0) {
         kp.run_walk = kDefaultRunWalk;
         kp.zi_min = kDefaultIndexMin;
-        kp.pair_record = 2;
+        kp.pair_record = 3;
     }
     ctx->configured = true;
     drop_graphs(ctx);
@@ -860,7 +887,7 @@ trax_status trax_set_tuning(trax_ctx *ctx, const trax_tuning *t)
 {
     if (!ctx || !t) return TRAX_ERR_BAD_ARG;
     if (t->index_min > 256) return fail(ctx, TRAX_ERR_BAD_ARG, "index_min must be <= 256");
-    if (t->pair_record > 2) return fail(ctx, TRAX_ERR_BAD_ARG, "pair_record must be 0, 1 or 2");
+    if (t->pair_record > 3) return fail(ctx, TRAX_ERR_BAD_ARG, "pair_record must be 0 to 3");
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->kp.run_walk = t->run_walk;
     ctx->kp.zi_min = t->index_min;
@@ -1419,6 +1446,7 @@ trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers
     if ((s = ensure(ctx, ctx->slots, slot_cap * 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->pexcl, (slot_cap + 1) * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->st0, (size_t)tiles_for((uint32_t)slot_cap, kTileItems) * 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->pkeep, (size_t)slot_cap * kPairKeepSplit * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->cexcl, (size_t)(max_pairs + 1) * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->st1, (size_t)tiles_for(tiles_for(max_pairs, 32) + 1, kScanItems * kScanThreads) * 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->ptile, (size_t)(tiles_for(max_pairs, 32) + 1) * 4)) != TRAX_OK) return s;

@@ -1203,6 +1203,128 @@ __global__ void __launch_bounds__(256) k_pair_lane(KParams kp, const uint32_t *g
     if (lane == 0 && my_visits) atomicAdd(&st->pair_slots, my_visits);
 }
 
+/*
+ * The same walk split at the scan, so that no warp waits for another (the
+ * look-back above cost a third of that kernel on sparse events):
+ *   k_pair_count_lane  one outer hit per lane: its count, and its first
+ *                      `keep` accepts in walk order in a per-item scratch row;
+ *   k_scan             exclusive scan of the counts (the pair total);
+ *   k_pair_store_lane  one outer hit per lane: copies its row to the pairs at
+ *                      its position, or (more accepts than kept) recomputes
+ *                      the window and walks again.
+ */
+__global__ void __launch_bounds__(256) k_pair_count_lane(KParams kp, const uint32_t *grid,
+                                                         const float4 *XYZP, const float2 *ZP,
+                                                         const uint2 *slots, uint32_t slot_cap,
+                                                         uint32_t *count, uint32_t *keep,
+                                                         uint32_t keep_n, DevState *st)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t n = st->n_outer;
+    if (n > slot_cap) n = slot_cap;
+    const uint32_t ntiles = (n + 31) / 32;
+    uint32_t my_visits = 0;
+    for (;;) {
+        uint32_t tile = 0;
+        if (lane == 0) tile = atomicAdd(&st->tile_ctr[0], 1u);
+        tile = __shfl_sync(kFull, tile, 0);
+        if (tile >= ntiles) break;
+        const uint32_t s = tile * 32 + lane;
+        if (s < n) {
+            const uint2 sl = slots[s];
+            const uint32_t outer = sl.x;
+            const uint32_t e = sl.y / kp.n_lt, lt = sl.y % kp.n_lt;
+            const uint32_t *lGrid1 = grid + (size_t)(e * kp.n_layers + (kp.l1[lt] - 1)) * kp.C;
+            const float4 o = XYZP[outer];
+            const PairWindow w = pair_window(kp, lt, o.x, o.y, o.z, o.w);
+            uint32_t mine = 0;
+            if (!w.ok) {
+                set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_WINDOW_OUTSIDE_GRID);
+            } else {
+                /* accept q of outer hit s at keep[q * slot_cap + s]: the
+                 * store pass reads each q across 32 hits in one access */
+                pair_lane_walk(kp, lGrid1, ZP, w, [&](uint32_t j, bool both) {
+                    my_visits += both ? 2u : 1u;
+                    if (mine < keep_n) keep[(size_t)mine * slot_cap + s] = j;
+                    ++mine;
+                    return true;
+                });
+            }
+            count[s] = mine;
+        }
+    }
+    unsigned long long v = my_visits;
+    for (int d = 16; d; d >>= 1) v += __shfl_down_sync(kFull, v, d);
+    if (lane == 0 && v) atomicAdd(&st->pair_slots, v);
+}
+
+/* 256 outer hits per block: their pairs form one contiguous range, staged
+ * in shared memory from the kept accepts and written out coalesced (a range
+ * larger than the stage is written directly); outer hits with more accepts
+ * than kept walk again. */
+constexpr uint32_t kPairStoreStage = 4096;
+
+__global__ void __launch_bounds__(256) k_pair_store_lane(KParams kp, const uint32_t *grid,
+                                                         const float4 *XYZP, const float2 *ZP,
+                                                         const uint2 *slots, uint32_t slot_cap,
+                                                         const uint32_t *excl,
+                                                         const uint32_t *keep, uint32_t keep_n,
+                                                         uint2 *pairs, uint32_t pair_cap,
+                                                         DevState *st)
+{
+    __shared__ uint2 s_buf[kPairStoreStage];
+    __shared__ uint32_t s_lo, s_hi;
+    uint32_t n = st->n_outer;
+    if (n > slot_cap) n = slot_cap;
+    const uint32_t total = st->n_pairs;
+    for (uint32_t b0 = blockIdx.x * blockDim.x; b0 < n; b0 += gridDim.x * blockDim.x) {
+        const uint32_t s = b0 + threadIdx.x;
+        uint32_t pos = 0, cnt = 0, outer = 0;
+        if (s < n) {
+            pos = excl[s];
+            cnt = (s + 1 < n ? excl[s + 1] : total) - pos;
+            if (cnt) outer = slots[s].x;
+        }
+        if (threadIdx.x == 0) s_lo = pos;
+        const uint32_t last = min(n, b0 + blockDim.x) - 1;
+        if (s == last) s_hi = pos + cnt;
+        __syncthreads();
+        const uint32_t lo = s_lo, span = s_hi - s_lo;
+        const bool staged = span <= kPairStoreStage;
+        if (cnt && cnt <= keep_n) {
+            for (uint32_t q = 0; q < cnt; ++q) {
+                const uint2 v = make_uint2(keep[(size_t)q * slot_cap + s], outer);
+                if (staged) s_buf[pos - lo + q] = v;
+                else if (pos + q < pair_cap) pairs[pos + q] = v;
+            }
+        } else if (cnt && staged) {
+            /* this outer hit walks again and writes its own range */
+            for (uint32_t q = 0; q < cnt; ++q) s_buf[pos - lo + q] = make_uint2(0u, 0xffffffffu);
+        }
+        __syncthreads();
+        if (staged)
+            for (uint32_t k = threadIdx.x; k < span; k += blockDim.x) {
+                const uint2 v = s_buf[k];
+                /* entries of outer hits that walk again are written by them */
+                if (lo + k < pair_cap && v.y != 0xffffffffu) pairs[lo + k] = v;
+            }
+        if (cnt > keep_n) {
+            const uint2 sl = slots[s];
+            const uint32_t e = sl.y / kp.n_lt, lt = sl.y % kp.n_lt;
+            const uint32_t *lGrid1 = grid + (size_t)(e * kp.n_layers + (kp.l1[lt] - 1)) * kp.C;
+            const float4 o = XYZP[outer];
+            const PairWindow w = pair_window(kp, lt, o.x, o.y, o.z, o.w);
+            uint32_t q = pos;
+            pair_lane_walk(kp, lGrid1, ZP, w, [&](uint32_t j, bool) {
+                if (q < pair_cap) pairs[q] = make_uint2(j, outer);
+                ++q;
+                return true;
+            });
+        }
+        __syncthreads();
+    }
+}
+
 /* ------------------------------------------------------------------------
  * Stage 2, sector variant (PairGeneratorSector.h:43-230).  No cut: every
  * layer-2 hit in the block of pairSpreadZ rows and pairSpreadPhi columns on

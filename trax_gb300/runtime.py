@@ -266,7 +266,7 @@ class Context:
         self.config = cfg
         return self
 
-    def set_tuning(self, run_walk: int, index_min: int, pair_record: int = 2):
+    def set_tuning(self, run_walk: int, index_min: int, pair_record: int = 3):
         self._check(self.lib.trax_set_tuning(
             self.h, C.byref(A.TraxTuning(run_walk, index_min, pair_record))))
 
