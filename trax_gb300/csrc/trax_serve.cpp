@@ -293,17 +293,21 @@ trax_status trax_server_create(trax_server **out, int device, const trax_config 
     srv->T = cfg->n_layer_triplets;
     srv->L = opts->n_layers;
     /* Split the budget over the slots.  Bytes per hit of a slot: 28 input +
-     * 36 sorted + 12 per triplet of outer-slot scratch, plus capacity for
-     * the pairs (12 B each with their scratch), candidates (8 B) and
-     * tracklets (24 B) allowed per hit. */
+     * 36 sorted + 26 packed copies (z/phi, half z, x/y/z/phi) + 12 per
+     * triplet of outer-slot scratch and 4 per kept pair accept (32) and
+     * triplet, plus capacity for the pairs (12 B each with their scratch),
+     * candidates (8 B) and tracklets (24 B) allowed per hit. */
     const uint64_t kp = opts->pairs_per_hit ? opts->pairs_per_hit : 24;
     const uint64_t kc = opts->candidates_per_hit ? opts->candidates_per_hit : 12;
     const uint64_t kt = opts->tracklets_per_hit ? opts->tracklets_per_hit : 4;
-    const uint64_t per_hit = 28 + 36 + 12ull * srv->T + kp * 12 + kc * 8 + kt * 24;
     const uint64_t cells = (uint64_t)(opts->n_sectors_z + 1) * (opts->n_sectors_phi + 1);
     const uint64_t fixed = (uint64_t)opts->max_batch_events * opts->n_layers * cells * 4 +
                            (uint64_t)opts->max_batch_events * srv->T * 40;
     const uint64_t per_slot = opts->memory_budget_bytes / opts->slots;
+    auto per_hit_for = [&](uint64_t keep) {
+        return 28 + 36 + 26 + 12ull * srv->T + 4ull * keep * srv->T + kp * 12 + kc * 8 + kt * 24;
+    };
+    const uint64_t per_hit = per_hit_for(32);
     if (per_slot <= fixed + per_hit * 1024) {
         delete srv;
         return TRAX_ERR_OOM;
