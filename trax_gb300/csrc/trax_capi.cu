@@ -386,7 +386,7 @@ trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *gr
         if ((s = mark(ctx, "pair_store")) != TRAX_OK) return s;
     } else if (sector)
         k_pair_sector<<<ctx->blk_sector, kFusedThreads, 0, ctx->stream>>>(
-            kp, grid, h.z, h.phi, slots, slot_cap, pexcl, pairs, pair_cap,
+            kp, grid, h.zphi, slots, slot_cap, pexcl, pairs, pair_cap,
             (unsigned long long *)ctx->st0.p, st);
     else if (kp.pair_record == 2)
         k_pair_lane<<<ctx->blk_pair_lane, kFusedThreads, 0, ctx->stream>>>(
@@ -394,11 +394,11 @@ trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *gr
             (unsigned long long *)ctx->st0.p, st);
     else if (kp.pair_record)
         k_pair_fused<true><<<ctx->blk_pair, kFusedThreads, 0, ctx->stream>>>(
-            kp, grid, h.x, h.y, h.z, h.phi, h.zphi, slots, slot_cap, pexcl, pairs, pair_cap,
+            kp, grid, h.xyzp, h.zphi, slots, slot_cap, pexcl, pairs, pair_cap,
             (unsigned long long *)ctx->st0.p, st);
     else
         k_pair_fused<false><<<ctx->blk_pair0, kFusedThreads, 0, ctx->stream>>>(
-            kp, grid, h.x, h.y, h.z, h.phi, h.zphi, slots, slot_cap, pexcl, pairs, pair_cap,
+            kp, grid, h.xyzp, h.zphi, slots, slot_cap, pexcl, pairs, pair_cap,
             (unsigned long long *)ctx->st0.p, st);
     if (sector || kp.pair_record != 3)
         if ((s = mark(ctx, "pair_gen")) != TRAX_OK) return s;
@@ -418,7 +418,7 @@ trax_status enqueue_zindex(trax_ctx *ctx, const SortedCols &h, const uint32_t *g
     if (s != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->zp, (size_t)max_hits * 4 + 4)) != TRAX_OK) return s;
     k_zindex<<<ctx->blk_small * 4, 256, 0, ctx->stream>>>(
-        grid, ctx->kp.n_layers * ctx->kp.C, ctx->kp.zi_min, h.z, h.phi, (float2 *)ctx->zi.p,
+        grid, ctx->kp.n_layers * ctx->kp.C, ctx->kp.zi_min, h.zphi, (float2 *)ctx->zi.p,
         (uint32_t *)ctx->zp.p, ctx->d_state);
     CK(cudaGetLastError());
     return mark(ctx, "zindex");
@@ -1425,7 +1425,9 @@ trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers
     if (slot_cap > 0xF0000000ull || (uint64_t)max_events * max_layers * C > 0xF0000000ull)
         return fail(ctx, TRAX_ERR_BAD_ARG, "reservation too large");
     for (int i = 0; i < 7; ++i) if ((s = ensure(ctx, ctx->in_cols[i], (size_t)max_hits * 4)) != TRAX_OK) return s;
-    for (int i = 0; i < 9; ++i) if ((s = ensure(ctx, ctx->srt_cols[i], (size_t)max_hits * 4)) != TRAX_OK) return s;
+    /* the chain keeps only layer, event and input position of the sorted
+     * hits (plus the packed columns below) */
+    for (int i : {4, 7, 8}) if ((s = ensure(ctx, ctx->srt_cols[i], (size_t)max_hits * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->grid_buf, (size_t)(max_events * max_layers * C) * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->r_seg, (size_t)max_events * max_layers * 8 + 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->pairs_buf, (size_t)max_pairs * 8)) != TRAX_OK) return s;
@@ -1471,10 +1473,10 @@ namespace {
 SortedCols reserved_sorted(trax_ctx *ctx)
 {
     SortedCols s;
-    s.x = (float *)ctx->srt_cols[0].p; s.y = (float *)ctx->srt_cols[1].p;
-    s.z = (float *)ctx->srt_cols[2].p; s.phi = (float *)ctx->srt_cols[3].p;
-    s.layer = (uint32_t *)ctx->srt_cols[4].p; s.det = (uint32_t *)ctx->srt_cols[5].p;
-    s.hitid = (uint32_t *)ctx->srt_cols[6].p; s.event = (uint32_t *)ctx->srt_cols[7].p;
+    s.x = s.y = s.z = s.phi = nullptr;  /* not kept by the chain */
+    s.det = s.hitid = nullptr;
+    s.layer = (uint32_t *)ctx->srt_cols[4].p;
+    s.event = (uint32_t *)ctx->srt_cols[7].p;
     s.orig = (uint32_t *)ctx->srt_cols[8].p;
     s.zphi = (float2 *)ctx->zphi.p;
     s.zh = (uint16_t *)ctx->zh.p;

@@ -73,6 +73,8 @@ struct DevState {
 };
 
 struct SortedCols {
+    /* x, y, z, phi, det and hitid are null in the batched chain, which reads
+     * the packed columns and never returns the sorted hits */
     float *x, *y, *z, *phi;
     uint32_t *layer, *det, *hitid, *event, *orig;
     float2 *zphi;  /* (z, phi) packed for the candidate loops; may be null */
@@ -614,9 +616,11 @@ __global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols o
                         const uint32_t ly = in.layer[h], ev = in.event[h];
                         if (ly != l + 1 || ev != e) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_LAYER_MISMATCH);
                         const uint32_t d = start + pos;
-                        out.x[d] = x; out.y[d] = y; out.z[d] = z; out.phi[d] = phi;
-                        out.layer[d] = ly; out.det[d] = in.det[h]; out.hitid[d] = in.hitid[h];
-                        out.event[d] = ev; out.orig[d] = h;
+                        if (out.x) {
+                            out.x[d] = x; out.y[d] = y; out.z[d] = z; out.phi[d] = phi;
+                            out.det[d] = in.det[h]; out.hitid[d] = in.hitid[h];
+                        }
+                        out.layer[d] = ly; out.event[d] = ev; out.orig[d] = h;
                         if (out.zphi) {
                             out.zphi[d] = make_float2(z, phi);
                             out.zh[d] = __half_as_ushort(__float2half_rn(z));
@@ -634,11 +638,14 @@ __global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols o
             for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
                 const uint32_t h = start + s_src[k];
                 const float x = in.x[h], y = in.y[h], z = in.z[h];
-                const uint32_t ly = in.layer[h], dt = in.det[h], hd = in.hitid[h], ev = in.event[h];
+                const uint32_t ly = in.layer[h], ev = in.event[h];
                 mismatch |= ly != l + 1 || ev != e;
                 const uint32_t d = start + k;
-                out.x[d] = x; out.y[d] = y; out.z[d] = z; out.phi[d] = s_phi[k];
-                out.layer[d] = ly; out.det[d] = dt; out.hitid[d] = hd; out.event[d] = ev;
+                if (out.x) {
+                    out.x[d] = x; out.y[d] = y; out.z[d] = z; out.phi[d] = s_phi[k];
+                    out.det[d] = in.det[h]; out.hitid[d] = in.hitid[h];
+                }
+                out.layer[d] = ly; out.event[d] = ev;
                 out.orig[d] = h;
                 if (out.zphi) {
                     out.zphi[d] = make_float2(z, s_phi[k]);
@@ -973,9 +980,7 @@ __device__ __forceinline__ PairWindow shfl_window(const PairWindow &w, int k)
 
 template <bool RECORD>
 __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *grid,
-                                                    const float *X, const float *Y,
-                                                    const float *Z, const float *PHI,
-                                                    const float2 *ZP,
+                                                    const float4 *XYZP, const float2 *ZP,
                                                     const uint2 *slots, uint32_t slot_cap,
                                                     uint32_t *pexcl, uint2 *pairs,
                                                     uint32_t pair_cap, unsigned long long *status,
@@ -1012,7 +1017,8 @@ __global__ void __launch_bounds__(256) k_pair_fused(KParams kp, const uint32_t *
             outer = sl.x;
             const uint32_t e = sl.y / kp.n_lt, lt = sl.y % kp.n_lt;
             lgoff = (e * kp.n_layers + (kp.l1[lt] - 1)) * kp.C;
-            w = pair_window(kp, lt, X[outer], Y[outer], Z[outer], PHI[outer]);
+            const float4 o = XYZP[outer];
+            w = pair_window(kp, lt, o.x, o.y, o.z, o.w);
             if (!w.ok) {
                 set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_WINDOW_OUTSIDE_GRID);
                 live = false;
@@ -1393,7 +1399,7 @@ __device__ __forceinline__ RowSpans sector_row(const uint32_t *lGrid2, uint32_t 
  * writes each item's pairs with all lanes (coalesced 8-byte stores) in
  * ascending outer-hit order -- the order of the reference's bitmap walk. */
 __global__ void __launch_bounds__(256) k_pair_sector(KParams kp, const uint32_t *grid,
-                                                     const float *Z, const float *PHI,
+                                                     const float2 *ZP,
                                                      const uint2 *slots, uint32_t slot_cap,
                                                      uint32_t *pexcl, uint2 *pairs,
                                                      uint32_t pair_cap, unsigned long long *status,
@@ -1426,7 +1432,8 @@ __global__ void __launch_bounds__(256) k_pair_sector(KParams kp, const uint32_t 
             inner = sl.x;
             const uint32_t e = sl.y / kp.n_lt, lt = sl.y % kp.n_lt;
             lgoff = (e * kp.n_layers + (kp.l2[lt] - 1)) * kp.C;
-            w = sector_window(kp, lt, Z[inner], PHI[inner]);
+            const float2 zp = ZP[inner];
+            w = sector_window(kp, lt, zp.x, zp.y);
             if (!w.ok) {
                 set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_WINDOW_OUTSIDE_GRID);
                 live = false;
@@ -1522,7 +1529,7 @@ __device__ __forceinline__ uint32_t zkey(float z)
 /* Each lane probes one cell of a 32-cell group; the warp then ranks the
  * hits of every indexable cell of the group together and scatters them. */
 __global__ void __launch_bounds__(256) k_zindex(const uint32_t *grid, uint32_t cells_per_event,
-                                                uint32_t zi_min, const float *Z, const float *PHI,
+                                                uint32_t zi_min, const float2 *ZP,
                                                 float2 *zi, uint32_t *zpos, DevState *st)
 {
     const uint32_t lane = threadIdx.x & 31;
@@ -1553,8 +1560,9 @@ __global__ void __launch_bounds__(256) k_zindex(const uint32_t *grid, uint32_t c
             zz[k] = 0.f;
             pp[k] = 0.f;
             if (i < cnt) {
-                zz[k] = Z[a + i];
-                pp[k] = PHI[a + i];
+                const float2 v = ZP[a + i];
+                zz[k] = v.x;
+                pp[k] = v.y;
                 key[k] = zkey(zz[k]);
             }
         }

@@ -293,7 +293,8 @@ trax_status trax_server_create(trax_server **out, int device, const trax_config 
     srv->T = cfg->n_layer_triplets;
     srv->L = opts->n_layers;
     /* Split the budget over the slots.  Bytes per hit of a slot: 28 input +
-     * 36 sorted + 26 packed copies (z/phi, half z, x/y/z/phi) + 12 per
+     * 12 sorted (layer, event, input position) + 26 packed copies (z/phi,
+     * half z, x/y/z/phi) + 12 per
      * triplet of outer-slot scratch and 4 per kept pair accept (32) and
      * triplet, plus capacity for the pairs (12 B each with their scratch),
      * candidates (8 B) and tracklets (24 B) allowed per hit. */
@@ -305,7 +306,7 @@ trax_status trax_server_create(trax_server **out, int device, const trax_config 
                            (uint64_t)opts->max_batch_events * srv->T * 40;
     const uint64_t per_slot = opts->memory_budget_bytes / opts->slots;
     auto per_hit_for = [&](uint64_t keep) {
-        return 28 + 36 + 26 + 12ull * srv->T + 4ull * keep * srv->T + kp * 12 + kc * 8 + kt * 24;
+        return 28 + 12 + 26 + 12ull * srv->T + 4ull * keep * srv->T + kp * 12 + kc * 8 + kt * 24;
     };
     const uint64_t per_hit = per_hit_for(32);
     if (per_slot <= fixed + per_hit * 1024) {
