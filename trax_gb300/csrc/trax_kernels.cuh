@@ -1967,28 +1967,39 @@ __global__ void k_cand_offsets(const uint32_t *pair_offsets, const uint32_t *in_
 /* ------------------------------------------------------------------------
  * Stage 4: triplet filter + stable compaction in one pass.
  * ---------------------------------------------------------------------- */
-__device__ __forceinline__ bool filter_cut(const KParams &kp, uint32_t lt, const float4 *XYZP,
-                                           uint32_t firstHit, uint32_t secondHit,
-                                           uint32_t thirdHit)
+/* The filter's cuts (TripletThetaPhiFilter.h:86-147) in two parts with
+ * the reference's arithmetic: the dphi cut, then the dtheta cut and the
+ * circle fit (impact parameter, minimum radius).  A candidate passes when
+ * both do -- the reference's conjunction, evaluated in another order. */
+__device__ __forceinline__ bool filter_phi_cut(const KParams &kp, uint32_t lt, const float4 h1,
+                                               const float4 h2, const float4 h3)
+{
+    const float dPhiCut = kp.dphi[lt];
+    const float x1 = h1.x, y1 = h1.y;
+    const float x2 = h2.x, y2 = h2.y;
+    const float x3 = h3.x, y3 = h3.y;
+    const float angle1 = trax_atan2f((y2 - y1), (x2 - x1));
+    const float angle2 = trax_atan2f((y3 - y2), (x3 - x2));
+    float delta = angle2 - angle1;
+    delta += (delta > TRAX_PI_F) ? -2 * TRAX_PI_F : (delta < -TRAX_PI_F) ? 2 * TRAX_PI_F : 0;
+    return fabsf(delta) <= dPhiCut;
+}
+
+__device__ __forceinline__ bool filter_theta_fit_cut(const KParams &kp, uint32_t lt,
+                                                     const float4 h1, const float4 h2,
+                                                     const float4 h3)
 {
     const float dThetaCut = kp.dtheta[lt];
-    const float dPhiCut = kp.dphi[lt];
     const float tipCut = kp.tip[lt];
     const float minRadius = kp.rmin_curv;
-    const float4 h1 = XYZP[firstHit], h2 = XYZP[secondHit], h3 = XYZP[thirdHit];
     const float x1 = h1.x, y1 = h1.y, z1 = h1.z;
     const float x2 = h2.x, y2 = h2.y, z2 = h2.z;
     const float x3 = h3.x, y3 = h3.y, z3 = h3.z;
     bool valid = true;
-    float angle1 = trax_atan2f(sqrtf((x2 - x1) * (x2 - x1) + (y2 - y1) * (y2 - y1)), (z2 - z1));
-    float angle2 = trax_atan2f(sqrtf((x3 - x2) * (x3 - x2) + (y3 - y2) * (y3 - y2)), (z3 - z2));
-    float delta = fabsf(angle2 / angle1);
+    const float angle1 = trax_atan2f(sqrtf((x2 - x1) * (x2 - x1) + (y2 - y1) * (y2 - y1)), (z2 - z1));
+    const float angle2 = trax_atan2f(sqrtf((x3 - x2) * (x3 - x2) + (y3 - y2) * (y3 - y2)), (z3 - z2));
+    const float delta = fabsf(angle2 / angle1);
     valid = valid && (1 - dThetaCut <= delta && delta <= 1 + dThetaCut);
-    angle1 = trax_atan2f((y2 - y1), (x2 - x1));
-    angle2 = trax_atan2f((y3 - y2), (x3 - x2));
-    delta = angle2 - angle1;
-    delta += (delta > TRAX_PI_F) ? -2 * TRAX_PI_F : (delta < -TRAX_PI_F) ? 2 * TRAX_PI_F : 0;
-    valid = valid && (fabsf(delta) <= dPhiCut);
     const float p1z = x1 * x1 + y1 * y1;
     const float p2z = x2 * x2 + y2 * y2;
     const float p3z = x3 * x3 + y3 * y3;
@@ -2022,6 +2033,11 @@ __device__ __forceinline__ bool filter_cut(const KParams &kp, uint32_t lt, const
  * popcount; k_scan turns the popcounts into positions; k_filter_store writes
  * the accepted candidates' hits at those positions in candidate order.
  */
+/* Two phases per warp and 64 candidates: the dphi cut for all of them
+ * (most candidates fail it), then the dtheta cut and the circle fit for the
+ * survivors only, gathered onto consecutive lanes through shared memory so
+ * that the expensive part runs on full warps.  Accept bits land in the two
+ * mask words by shared-memory atomics. */
 __global__ void __launch_bounds__(256) k_filter_count(KParams kp, const float4 *XYZP,
                                                       const uint32_t *LAYER,
                                                       const uint2 *pairs, const uint2 *cands,
@@ -2029,28 +2045,55 @@ __global__ void __launch_bounds__(256) k_filter_count(KParams kp, const float4 *
                                                       uint32_t cand_cap, uint32_t *mask,
                                                       uint32_t *word_count, DevState *st)
 {
+    __shared__ uint4 s_q[kFusedThreads / 32][64];
+    __shared__ uint32_t s_w[kFusedThreads / 32][2];
     const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lt_mask = lanemask_lt();
+    const uint32_t wib = threadIdx.x >> 5;
     uint32_t n = *n_cands_ptr;
     if (n > cand_cap) n = cand_cap;
     if (blockIdx.x == 0 && threadIdx.x == 0) st->n_ftile = (n + 31) / 32;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; i0 < n; i0 += stride) {
-        const uint32_t i = i0 + lane;
-        bool ok = false;
-        if (i < n) {
-            const uint2 c = cands[i];
-            const uint2 pr = pairs[c.x];
-            const uint32_t lt = LAYER[pr.x] - 1;
-            if (lt >= kp.n_lt)
-                set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_BAD_TRIPLET_INDEX);
-            else
-                ok = filter_cut(kp, lt, XYZP, pr.x, pr.y, c.y);
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i0 = gw * 64; i0 < n; i0 += nw * 64) {
+        if (lane < 2) s_w[wib][lane] = 0;
+        uint32_t nsurv = 0;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const uint32_t i = i0 + half * 32 + lane;
+            bool pass = false;
+            uint4 e = make_uint4(0, 0, 0, 0);
+            if (i < n) {
+                const uint2 c = cands[i];
+                const uint2 pr = pairs[c.x];
+                const uint32_t lt = LAYER[pr.x] - 1;
+                if (lt >= kp.n_lt) {
+                    set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_BAD_TRIPLET_INDEX);
+                } else {
+                    pass = filter_phi_cut(kp, lt, XYZP[pr.x], XYZP[pr.y], XYZP[c.y]);
+                    e = make_uint4(pr.x, pr.y, c.y, lt | ((uint32_t)(half * 32) + lane) << 8);
+                }
+            }
+            const uint32_t b = __ballot_sync(kFull, pass);
+            if (pass) s_q[wib][nsurv + __popc(b & lt_mask)] = e;
+            nsurv += __popc(b);
         }
-        const uint32_t m = __ballot_sync(kFull, ok);
-        if (lane == 0) {
-            mask[i0 >> 5] = m;
-            word_count[i0 >> 5] = __popc(m);
+        __syncwarp();
+        for (uint32_t r = 0; r < nsurv; r += 32) {
+            if (r + lane < nsurv) {
+                const uint4 e = s_q[wib][r + lane];
+                const uint32_t lt = e.w & 0xffu, slot = e.w >> 8;
+                if (filter_theta_fit_cut(kp, lt, XYZP[e.x], XYZP[e.y], XYZP[e.z]))
+                    atomicOr(&s_w[wib][slot >> 5], 1u << (slot & 31));
+            }
         }
+        __syncwarp();
+        if (lane < 2 && i0 + lane * 32 < n) {
+            const uint32_t m = s_w[wib][lane];
+            mask[(i0 >> 5) + lane] = m;
+            word_count[(i0 >> 5) + lane] = __popc(m);
+        }
+        __syncwarp();
     }
 }
 
