@@ -438,17 +438,20 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
     if ((s = ensure(ctx, ctx->st1, (size_t)ntile * 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->ptile, (size_t)ptiles * 4)) != TRAX_OK) return s;
     const uint32_t rec_cap = cand_cap ? cand_cap : 1;
-    if ((s = ensure(ctx, ctx->prec, (size_t)rec_cap * sizeof(PredRec))) != TRAX_OK) return s;
+    /* a walking record stands for more than kPredKeep candidates */
+    const uint32_t walk_cap = rec_cap / (kPredKeep + 1) + 1;
+    if ((s = ensure(ctx, ctx->prec, ((size_t)rec_cap + walk_cap) * sizeof(PredRec))) != TRAX_OK) return s;
     uint32_t *cexcl = (uint32_t *)ctx->cexcl.p;
     uint32_t *ptile = (uint32_t *)ctx->ptile.p;
     PredRec *recs = (PredRec *)ctx->prec.p;
     DevState *st = ctx->d_state;
     /* the pair total is st->n_pairs: written by the pair stage, or copied
      * from pair_offsets[G] by trax_triplet_predict */
-    CK(cudaMemsetAsync(&st->n_prec, 0, 4, ctx->stream));
+    CK(cudaMemsetAsync(&st->n_prec, 0, 8, ctx->stream));  /* n_prec, n_pwalk */
     k_predict_count<<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
         kp, grid, h.xyzp, h.zphi, h.zh, h.event, h.layer, (const float2 *)ctx->zi.p,
-        (const uint32_t *)ctx->zp.p, pairs, &st->n_pairs, pair_cap, cexcl, ptile, recs, rec_cap, st);
+        (const uint32_t *)ctx->zp.p, pairs, &st->n_pairs, pair_cap, cexcl, ptile, recs, rec_cap,
+        walk_cap, st);
     if ((s = mark(ctx, "predict")) != TRAX_OK) return s;
     CK(cudaMemsetAsync(&st->tile_ctr[1], 0, 4, ctx->stream));
     CK(cudaMemsetAsync(ctx->st1.p, 0, (size_t)ntile * 8, ctx->stream));
@@ -457,7 +460,7 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
     if ((s = mark(ctx, "predict_scan")) != TRAX_OK) return s;
     k_predict_store<<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
         kp, grid, h.zphi, h.zh, recs,
-        rec_cap, cexcl, ptile, &st->n_pairs, pair_cap, &st->n_cands, cands, cand_cap, st);
+        rec_cap, walk_cap, cexcl, ptile, &st->n_pairs, pair_cap, &st->n_cands, cands, cand_cap, st);
     if ((s = mark(ctx, "predict_store")) != TRAX_OK) return s;
     k_cand_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(pair_offsets, cexcl, ptile,
                                                             cand_offsets, kp.n_lt, pair_cap,
@@ -1452,7 +1455,10 @@ trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers
     if ((s = ensure(ctx, ctx->cexcl, (size_t)(max_pairs + 1) * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->st1, (size_t)tiles_for(tiles_for(max_pairs, 32) + 1, kScanItems * kScanThreads) * 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->ptile, (size_t)(tiles_for(max_pairs, 32) + 1) * 4)) != TRAX_OK) return s;
-    if ((s = ensure(ctx, ctx->prec, (size_t)(max_candidates ? max_candidates : 1) * sizeof(PredRec))) != TRAX_OK) return s;
+    {
+        const size_t rc = max_candidates ? max_candidates : 1;
+        if ((s = ensure(ctx, ctx->prec, (rc + rc / (kPredKeep + 1) + 1) * sizeof(PredRec))) != TRAX_OK) return s;
+    }
     if ((s = ensure(ctx, ctx->st2, (size_t)tiles_for(tiles_for(max_candidates, 32) + 1, kScanItems * kScanThreads) * 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->fmask, (size_t)(tiles_for(max_candidates, 32) + 1) * 8)) != TRAX_OK) return s;
     if ((s = ensure_stage(ctx, (size_t)max_events * max_layers * 2 + 4)) != TRAX_OK) return s;

@@ -67,7 +67,8 @@ struct DevState {
     unsigned long long cand_truncated;
     uint32_t tile_ctr[4];    /* decoupled look-back tile tickets */
     uint32_t aux_n;          /* element count of a standalone prefix sum */
-    uint32_t n_prec;         /* prediction store records */
+    uint32_t n_prec;         /* prediction store records carrying their accepts */
+    uint32_t n_pwalk;        /* prediction store records that walk (after them) */
     uint32_t n_ptile;        /* 32-pair tiles of the prediction count pass */
     uint32_t n_ftile;        /* 32-candidate words of the filter's accept mask */
 };
@@ -1803,7 +1804,7 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
     const uint32_t *n_pairs_ptr,
     uint32_t pair_cap,
     uint32_t *in_tile,
-    uint32_t *tile_sum, PredRec *recs, uint32_t rec_cap, DevState *st)
+    uint32_t *tile_sum, PredRec *recs, uint32_t rec_cap, uint32_t walk_cap, DevState *st)
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt_mask = lanemask_lt();
@@ -1853,28 +1854,39 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
         }
         if (p < n) in_tile[p] = incl - emitted;
         if (lane == 31) tile_sum[p0 >> 5] = incl;
-        const uint32_t want = __ballot_sync(kFull, emitted != 0);
-        uint32_t base = 0;
+        /* records that carry their accepts go to recs[0, rec_cap), records
+         * that walk to recs[rec_cap, rec_cap + walk_cap): the store pass
+         * then runs the (rare) walks on warps of their own */
+        const bool copy = emitted != 0 && emitted <= (uint32_t)kPredKeep;
+        const bool walk = emitted > (uint32_t)kPredKeep;
+        const uint32_t want = __ballot_sync(kFull, copy), wwant = __ballot_sync(kFull, walk);
+        uint32_t base = 0, wbase = 0;
         if (lane == 0 && want) base = atomicAdd(&st->n_prec, (uint32_t)__popc(want));
+        if (lane == 0 && wwant) wbase = atomicAdd(&st->n_pwalk, (uint32_t)__popc(wwant));
         base = __shfl_sync(kFull, base, 0);
-        if (emitted) {
+        wbase = __shfl_sync(kFull, wbase, 0);
+        if (copy) {
             const uint32_t r = base + __popc(want & lt_mask);
             if (r < rec_cap) {
                 PredRec rec;
                 rec.pair = p;
-                if (emitted <= (uint32_t)kPredKeep) {
 #pragma unroll
-                    for (int q = 0; q < kPredKeep; ++q) rec.hit[q] = (uint32_t)q < emitted ? keep[q] : 0u;
-                } else {
-                    rec.win.grid_off = goff;
-                    rec.win.zsec = w.zLowSector[1] | (w.zHighSector[1] << 16);
-                    rec.win.psec = w.phiLowSector | (w.phiHighSector << 16) | (w.wrap << 31);
-                    rec.win.zLow = w.zLow[1];
-                    rec.win.zHigh = w.zHigh[1];
-                    rec.win.phiLow = w.phiLow;
-                    rec.win.phiHigh = w.phiHigh;
-                }
+                for (int q = 0; q < kPredKeep; ++q) rec.hit[q] = (uint32_t)q < emitted ? keep[q] : 0u;
                 recs[r] = rec;
+            }
+        } else if (walk) {
+            const uint32_t r = wbase + __popc(wwant & lt_mask);
+            if (r < walk_cap) {
+                PredRec rec;
+                rec.pair = p;
+                rec.win.grid_off = goff;
+                rec.win.zsec = w.zLowSector[1] | (w.zHighSector[1] << 16);
+                rec.win.psec = w.phiLowSector | (w.phiHighSector << 16) | (w.wrap << 31);
+                rec.win.zLow = w.zLow[1];
+                rec.win.zHigh = w.zHigh[1];
+                rec.win.phiLow = w.phiLow;
+                rec.win.phiHigh = w.phiHigh;
+                recs[rec_cap + r] = rec;
             }
         }
     }
@@ -1891,17 +1903,21 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
 
 __global__ void __launch_bounds__(256) k_predict_store(
     KParams kp, const uint32_t *grid, const float2 *ZP, const uint16_t *ZH,
-    const PredRec *recs, uint32_t rec_cap, const uint32_t *in_tile,
+    const PredRec *recs, uint32_t rec_cap, uint32_t walk_cap, const uint32_t *in_tile,
     const uint32_t *tile_prefix, const uint32_t *n_pairs_ptr, uint32_t pair_cap,
     const uint32_t *total_ptr, uint2 *cands, uint32_t cand_cap, DevState *st)
 {
-    uint32_t nrec = st->n_prec;
-    if (nrec > rec_cap) nrec = rec_cap;
+    uint32_t ncopy = st->n_prec, nwalk = st->n_pwalk;
+    if (ncopy > rec_cap) ncopy = rec_cap;
+    if (nwalk > walk_cap) nwalk = walk_cap;
     uint32_t n = *n_pairs_ptr;
     if (n > pair_cap) n = pair_cap;
     const uint32_t P1 = kp.nphi + 1;
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < nrec; r += gridDim.x * blockDim.x) {
-        const PredRec r0 = recs[r];
+    /* the copy records, then the walk records: consecutive threads take
+     * records of one kind, so the walks share their warps only with walks */
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < ncopy + nwalk;
+         r += gridDim.x * blockDim.x) {
+        const PredRec r0 = recs[r < ncopy ? r : rec_cap + (r - ncopy)];
         const uint32_t p = r0.pair;
         if (p >= n) continue;
         const uint32_t pos = tile_prefix[p >> 5] + in_tile[p];
