@@ -501,7 +501,10 @@ trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers
                          uint32_t max_tracklets);
 
 /* Uploads the batch, runs grid build -> pairs -> predict -> filter as one
- * CUDA graph and downloads the tracklets.  Synchronous. */
+ * CUDA graph and downloads the tracklets.  Synchronous.  A batch of a million
+ * hits or more runs as two halves of its events through the streaming
+ * slots below, the second half's upload overlapping the first half's chain;
+ * the result is the same. */
 trax_status trax_seed_batch(trax_ctx *ctx, const trax_event_batch *in, trax_batch_result *out);
 
 /* Streaming form of trax_seed_batch (the reference's per-group loop in

@@ -97,3 +97,26 @@ def test_stream_capacity_error(gpu_ctx):
     assert gpu_ctx.lib.trax_submit_batch(gpu_ctx.h, C.byref(bs), C.byref(r), C.byref(t)) == 0
     assert gpu_ctx.lib.trax_wait_batch(gpu_ctx.h, t.value, C.byref(r)) == 5
     assert r.n_tracklets == n
+
+
+def test_large_seed_batch_pipelines_halves(gpu_ctx):
+    """trax_seed_batch runs batches of a million hits or more as two halves
+    through the streaming slots; the concatenated result is the whole
+    batch's (equal to one slot's run of the whole batch and to the oracle)."""
+    import os
+    w = gen.WORKLOADS["multimuon-1000trk"]
+    b = gen.generate_batch(w, 340)
+    assert b.n_hits >= 1 << 20
+    N = b.n_hits
+    p = Pipeline(gpu_ctx, w.config(), w.grid(b.n_events), b.n_events, N, 80 * N, 80 * N, 8 * N)
+    for input_indices in (False, True):
+        trk, off, counts = p.seed(b, input_indices=input_indices)
+        assert counts["status"] == 0
+        whole = p.wait(p.submit(b, input_indices=input_indices))
+        assert np.array_equal(trk, whole[0])
+        assert np.array_equal(off, whole[1])
+        assert counts == whole[2]
+        if not input_indices:
+            ref = oracle.canonical(oracle.run(b, w.config(), w.grid(b.n_events), 4, n_threads=1,
+                                              omp_threads=os.cpu_count() or 1))
+            assert np.array_equal(trk, ref["tracklets"])

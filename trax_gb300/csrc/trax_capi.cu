@@ -31,6 +31,7 @@ constexpr int kTimerSlots = 64;
 constexpr int kScanItems = 8;       /* items per thread in k_scan */
 constexpr int kScanThreads = 256;
 constexpr int kTileItems = 32;      /* items per fused pair / predict tile (one warp) */
+constexpr uint32_t kSplitSeedHits = 1u << 20;  /* trax_seed_batch pipelines two halves from here */
 /* pair accepts an outer hit keeps for the split store: more than 32 is rare
  * below pile-up (an outer hit with more walks again in the store) */
 constexpr uint32_t kPairKeepSplit = 32;
@@ -1535,7 +1536,7 @@ trax_status enqueue_pipeline(trax_ctx *ctx, const InCols &ic, const uint32_t *se
 __global__ void k_emit(const DevState *st, DevState *snap, const uint32_t *orig,
                        const uint32_t *t1, const uint32_t *t2, const uint32_t *t3, uint32_t r_trk,
                        uint32_t *o1, uint32_t *o2, uint32_t *o3, uint32_t cap,
-                       const uint32_t *off, uint32_t *o_off, uint32_t n_off)
+                       const uint32_t *off, uint32_t *o_off, uint32_t n_off, uint32_t index_base)
 {
     uint32_t n = st->n_trk;
     if (n > r_trk) n = r_trk;
@@ -1544,14 +1545,21 @@ __global__ void k_emit(const DevState *st, DevState *snap, const uint32_t *orig,
     if (n <= cap) {
         for (uint32_t i = tid; i < n; i += stride) {
             const uint32_t a = t1[i], b = t2[i], c = t3[i];
-            if (o1) o1[i] = orig ? orig[a] : a;
-            if (o2) o2[i] = orig ? orig[b] : b;
-            if (o3) o3[i] = orig ? orig[c] : c;
+            if (o1) o1[i] = (orig ? orig[a] : a) + index_base;
+            if (o2) o2[i] = (orig ? orig[b] : b) + index_base;
+            if (o3) o3[i] = (orig ? orig[c] : c) + index_base;
         }
     }
     if (o_off)
         for (uint32_t g = tid; g < n_off; g += stride) o_off[g] = off[g];
     if (tid == 0) *snap = *st;
+}
+
+/* Event numbers of a batch's second half, counted from its first event. */
+__global__ void k_rebase_events(uint32_t *event, uint32_t n, uint32_t base)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        event[i] -= base;
 }
 
 __global__ void k_map_orig(const uint32_t *orig, const uint32_t *t1, const uint32_t *t2,
@@ -1690,9 +1698,9 @@ trax_status trax_kernel_times(trax_ctx *ctx, float *ms, const char **names, int 
     return TRAX_OK;
 }
 
-trax_status trax_seed_batch(trax_ctx *ctx, const trax_event_batch *in, trax_batch_result *out)
+/* trax_seed_batch in one piece: upload, graph, download in turn. */
+static trax_status seed_whole(trax_ctx *ctx, const trax_event_batch *in, trax_batch_result *out)
 {
-    if (!ctx || !in || !out) return TRAX_ERR_BAD_ARG;
     trax_status s = trax_stage_batch(ctx, in);
     if (s != TRAX_OK) return s;
     if ((s = trax_run_staged(ctx)) != TRAX_OK) return s;
@@ -1730,6 +1738,74 @@ trax_status trax_seed_batch(trax_ctx *ctx, const trax_event_batch *in, trax_batc
     return TRAX_OK;
 }
 
+static trax_status submit_slot(trax_ctx *ctx, const trax_event_batch *in,
+                               const trax_batch_result *out, uint32_t event_base,
+                               uint32_t index_base, uint32_t *ticket);
+static trax_status wait_slot(trax_ctx *ctx, uint32_t ticket, trax_batch_result *out,
+                             uint32_t trk_shift, uint32_t off_shift, bool download);
+
+/*
+ * trax_seed_batch as two halves of its events through the streaming slots:
+ * the second half uploads while the first computes, and the first half's
+ * results download while the second computes.  Events are independent, so
+ * the halves' results, concatenated (the second half's hit indices and
+ * offsets shifted), are the whole batch's.
+ */
+trax_status trax_seed_batch(trax_ctx *ctx, const trax_event_batch *in, trax_batch_result *out)
+{
+    if (!ctx || !in || !out) return TRAX_ERR_BAD_ARG;
+    const uint32_t E = in->n_events, L = in->n_layers;
+    /* small batches (a serving slot's) gain nothing from the overlap and
+     * keep the one-piece form, without the streaming slots' buffers */
+    if (E < 2 || in->n_hits < kSplitSeedHits || !ctx->reserved || ctx->aslot[0].busy ||
+        ctx->aslot[1].busy || L != ctx->r_layers || E > ctx->r_events || in->n_hits > ctx->r_hits)
+        return seed_whole(ctx, in, out);
+    const uint32_t E1 = E / 2;
+    uint64_t n1 = 0;
+    for (size_t i = 0; i < (size_t)E1 * L; ++i) n1 += in->layer_nhits[i];
+    if (n1 > in->n_hits) return fail(ctx, TRAX_ERR_BAD_INPUT, "layer_nhits do not sum to n_hits");
+    trax_event_batch b1 = *in, b2 = *in;
+    b1.n_events = E1;
+    b1.n_hits = (uint32_t)n1;
+    b2.n_events = E - E1;
+    b2.n_hits = in->n_hits - (uint32_t)n1;
+    b2.x += n1; b2.y += n1; b2.z += n1;
+    b2.layer += n1; b2.detector_id += n1; b2.hit_id += n1; b2.event += n1;
+    b2.layer_nhits += (size_t)E1 * L;
+    uint32_t t1 = 0, t2 = 0;
+    trax_status s = submit_slot(ctx, &b1, out, 0, 0, &t1);
+    if (s != TRAX_OK) return s;
+    s = submit_slot(ctx, &b2, out, E1, (uint32_t)n1, &t2);
+    if (s != TRAX_OK) {
+        trax_batch_result r = *out;
+        wait_slot(ctx, t1, &r, 0, 0, false);
+        return s;
+    }
+    trax_batch_result r1 = *out, r2 = *out;
+    const trax_status s1 = wait_slot(ctx, t1, &r1, 0, 0, true);
+    const trax_status s2 = wait_slot(ctx, t2, &r2, s1 == TRAX_OK ? r1.n_tracklets : 0,
+                                     E1 * ctx->kp.n_lt, s1 == TRAX_OK);
+    trax_counts &c = out->counts;
+    c.n_hits = r1.counts.n_hits + r2.counts.n_hits;
+    c.n_pairs = r1.counts.n_pairs + r2.counts.n_pairs;
+    c.pair_slots = r1.counts.pair_slots + r2.counts.pair_slots;
+    c.n_candidates = r1.counts.n_candidates + r2.counts.n_candidates;
+    c.cand_slots = r1.counts.cand_slots + r2.counts.cand_slots;
+    c.cand_truncated = r1.counts.cand_truncated + r2.counts.cand_truncated;
+    c.n_tracklets = r1.counts.n_tracklets + r2.counts.n_tracklets;
+    c.status = r1.counts.status ? r1.counts.status : r2.counts.status;
+    c.error_detail = r1.counts.status ? r1.counts.error_detail : r2.counts.error_detail;
+    out->n_tracklets = r1.n_tracklets + r2.n_tracklets;
+    if (c.status != TRAX_OK) {
+        char buf[96];
+        snprintf(buf, sizeof buf, "device status %u detail %u", c.status, c.error_detail);
+        return fail(ctx, (trax_status)c.status, buf);
+    }
+    if (s1 != TRAX_OK || s2 != TRAX_OK || out->n_tracklets > out->capacity)
+        return fail(ctx, TRAX_ERR_CAPACITY, "result larger than the output capacity");
+    return TRAX_OK;
+}
+
 /* Creates a streaming slot's buffers at the reservation's sizes. */
 static trax_status ensure_slot(trax_ctx *ctx, AsyncSlot &a)
 {
@@ -1757,10 +1833,13 @@ static trax_status ensure_slot(trax_ctx *ctx, AsyncSlot &a)
     return TRAX_OK;
 }
 
-trax_status trax_submit_batch(trax_ctx *ctx, const trax_event_batch *in,
-                              const trax_batch_result *out, uint32_t *ticket)
+/* Queues one batch on a free slot.  event_base: the batch's hits carry
+ * event numbers from event_base on (rebased on the device); index_base is
+ * added to every returned hit index. */
+static trax_status submit_slot(trax_ctx *ctx, const trax_event_batch *in,
+                               const trax_batch_result *out, uint32_t event_base,
+                               uint32_t index_base, uint32_t *ticket)
 {
-    if (!ctx || !in || !out || !ticket) return TRAX_ERR_BAD_ARG;
     if (!ctx->reserved) return fail(ctx, TRAX_ERR_BAD_ARG, "trax_reserve not called");
     if (in->n_events > ctx->r_events || in->n_layers != ctx->r_layers || in->n_hits > ctx->r_hits)
         return fail(ctx, TRAX_ERR_CAPACITY, "batch larger than the reservation");
@@ -1791,6 +1870,9 @@ trax_status trax_submit_batch(trax_ctx *ctx, const trax_event_batch *in,
         if ((s = capture_pipeline(ctx, in_cols_of(a.in_cols), seg, &a.graph)) != TRAX_OK) return s;
     }
     CK(cudaStreamWaitEvent(ctx->stream, a.h2d_done, 0));
+    if (event_base && in->n_hits)
+        k_rebase_events<<<ctx->blk_small, 256, 0, ctx->stream>>>((uint32_t *)a.in_cols[6].p,
+                                                                in->n_hits, event_base);
     CK(cudaMemcpyAsync(ctx->d_state, seg + 2 * nseg_r, 8, cudaMemcpyDeviceToDevice, ctx->stream));
     CK(cudaGraphLaunch(a.graph, ctx->stream));
     const uint32_t n_off = in->n_events * ctx->kp.n_lt + 1;
@@ -1799,7 +1881,7 @@ trax_status trax_submit_batch(trax_ctx *ctx, const trax_event_batch *in,
         (const uint32_t *)ctx->trk_cols[0].p, (const uint32_t *)ctx->trk_cols[1].p,
         (const uint32_t *)ctx->trk_cols[2].p, ctx->r_trk, (uint32_t *)a.res[0].p,
         (uint32_t *)a.res[1].p, (uint32_t *)a.res[2].p, out->capacity,
-        (const uint32_t *)ctx->trk_off.p, (uint32_t *)a.res_off.p, n_off);
+        (const uint32_t *)ctx->trk_off.p, (uint32_t *)a.res_off.p, n_off, index_base);
     CK(cudaGetLastError());
     CK(cudaEventRecord(a.done, ctx->stream));
     a.busy = true;
@@ -1814,9 +1896,19 @@ trax_status trax_submit_batch(trax_ctx *ctx, const trax_event_batch *in,
     return TRAX_OK;
 }
 
-trax_status trax_wait_batch(trax_ctx *ctx, uint32_t ticket, trax_batch_result *out)
+trax_status trax_submit_batch(trax_ctx *ctx, const trax_event_batch *in,
+                              const trax_batch_result *out, uint32_t *ticket)
 {
-    if (!ctx || !out) return TRAX_ERR_BAD_ARG;
+    if (!ctx || !in || !out || !ticket) return TRAX_ERR_BAD_ARG;
+    return submit_slot(ctx, in, out, 0, 0, ticket);
+}
+
+/* Waits for a slot's batch and downloads its results to the slot's output
+ * pointers shifted by trk_shift tracklets (offsets: by off_shift entries, each
+ * plus trk_shift); the capacity counts from the unshifted start. */
+static trax_status wait_slot(trax_ctx *ctx, uint32_t ticket, trax_batch_result *out,
+                             uint32_t trk_shift, uint32_t off_shift, bool download)
+{
     AsyncSlot &a = ctx->aslot[ticket & 1];
     if (!a.busy || a.ticket != ticket) return fail(ctx, TRAX_ERR_BAD_ARG, "no batch in flight with this ticket");
     a.busy = false;
@@ -1837,18 +1929,27 @@ trax_status trax_wait_batch(trax_ctx *ctx, uint32_t ticket, trax_batch_result *o
         snprintf(buf, sizeof buf, "device status %u detail %u", st.status, st.detail);
         return fail(ctx, (trax_status)st.status, buf);
     }
-    if (st.n_trk > ctx->r_trk || st.n_trk > a.capacity)
+    if (st.n_trk > ctx->r_trk || (uint64_t)trk_shift + st.n_trk > a.capacity)
         return fail(ctx, TRAX_ERR_CAPACITY, "result larger than the output capacity");
+    if (!download) return TRAX_OK;
     /* the download, on its own stream: it overlaps the next batch's chain */
     for (int i = 0; i < 3; ++i)
         if (a.out[i] && st.n_trk)
-            CK(cudaMemcpyAsync(a.out[i], a.res[i].p, (size_t)st.n_trk * 4, cudaMemcpyDeviceToHost,
-                               ctx->d2h_stream));
+            CK(cudaMemcpyAsync(a.out[i] + trk_shift, a.res[i].p, (size_t)st.n_trk * 4,
+                               cudaMemcpyDeviceToHost, ctx->d2h_stream));
     if (a.out[3])
-        CK(cudaMemcpyAsync(a.out[3], a.res_off.p, (size_t)a.n_off * 4, cudaMemcpyDeviceToHost,
-                           ctx->d2h_stream));
+        CK(cudaMemcpyAsync(a.out[3] + off_shift, a.res_off.p, (size_t)a.n_off * 4,
+                           cudaMemcpyDeviceToHost, ctx->d2h_stream));
     CK(cudaStreamSynchronize(ctx->d2h_stream));
+    if (a.out[3] && trk_shift)
+        for (uint32_t g = 0; g < a.n_off; ++g) a.out[3][off_shift + g] += trk_shift;
     return TRAX_OK;
+}
+
+trax_status trax_wait_batch(trax_ctx *ctx, uint32_t ticket, trax_batch_result *out)
+{
+    if (!ctx || !out) return TRAX_ERR_BAD_ARG;
+    return wait_slot(ctx, ticket, out, 0, 0, true);
 }
 
 }  // extern "C"
