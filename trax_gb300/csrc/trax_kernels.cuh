@@ -382,17 +382,20 @@ __global__ void __launch_bounds__(256) k_scan(const uint32_t *in, uint32_t *out,
         for (int k = 0; k < ITEMS; ++k) sum += v[k];
         uint32_t agg;
         const uint32_t excl = block_exclusive_scan(sum, s_warp, &agg);
-        if (threadIdx.x == 0) {
+        if (threadIdx.x < 32) {
+            /* warp 0 looks back over 32 predecessors per poll */
             uint32_t prefix = 0;
             if (tile == 0) {
-                st_relaxed64(status, kFlagInc | agg);
+                if (threadIdx.x == 0) st_relaxed64(status, kFlagInc | agg);
             } else {
-                st_relaxed64(status + tile, kFlagAgg | agg);
-                prefix = lookback_prefix(status, tile, st);
-                st_relaxed64(status + tile, kFlagInc | (uint32_t)(prefix + agg));
+                if (threadIdx.x == 0) st_relaxed64(status + tile, kFlagAgg | agg);
+                prefix = warp_lookback(status, tile, st);
+                if (threadIdx.x == 0) st_relaxed64(status + tile, kFlagInc | (uint32_t)(prefix + agg));
             }
-            s_prefix = prefix;
-            if (tile == ntiles - 1 && total_out) *total_out = prefix + agg;
+            if (threadIdx.x == 0) {
+                s_prefix = prefix;
+                if (tile == ntiles - 1 && total_out) *total_out = prefix + agg;
+            }
         }
         __syncthreads();
         uint32_t run = s_prefix + excl;
