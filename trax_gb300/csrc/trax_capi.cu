@@ -28,7 +28,7 @@ using namespace trax;
 namespace {
 
 constexpr int kTimerSlots = 64;
-constexpr int kScanItems = 8;       /* items per thread in k_scan */
+constexpr int kScanItems = 16;      /* items per thread in k_scan */
 constexpr int kScanThreads = 256;
 constexpr int kTileItems = 32;      /* items per fused pair / predict tile (one warp) */
 constexpr uint32_t kSplitSeedHits = 1u << 20;  /* trax_seed_batch pipelines two halves from here */
