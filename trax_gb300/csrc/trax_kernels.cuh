@@ -1927,9 +1927,11 @@ __global__ void __launch_bounds__(256) k_predict_store(
         const uint32_t emitted =
             (p + 1 < n ? tile_prefix[(p + 1) >> 5] + in_tile[p + 1] : *total_ptr) - pos;
         if (emitted <= (uint32_t)kPredKeep) {
-            /* the count pass kept them: the first window-B accepts in visit order */
-            for (uint32_t q = 0; q < emitted; ++q)
-                if (pos + q < cand_cap) cands[pos + q] = make_uint2(p, r0.hit[q]);
+            /* the count pass kept them: the first window-B accepts in visit
+             * order (unrolled, so the record stays in registers) */
+#pragma unroll
+            for (uint32_t q = 0; q < (uint32_t)kPredKeep; ++q)
+                if (q < emitted && pos + q < cand_cap) cands[pos + q] = make_uint2(p, r0.hit[q]);
             continue;
         }
         const auto &rec = r0.win;
