@@ -166,117 +166,11 @@ constexpr unsigned long long kFlagAgg = 1ull << 32;
 constexpr unsigned long long kFlagInc = 2ull << 32;
 constexpr uint32_t kSpinLimit = 1u << 22;
 
-__device__ __forceinline__ uint32_t lookback_prefix(unsigned long long *status, uint32_t tile,
-                                                    DevState *st)
-{
-    uint32_t prefix = 0;
-    int64_t k = (int64_t)tile - 1;
-    uint32_t spins = 0;
-    while (k >= 0) {
-        unsigned long long s = ld_relaxed64(status + k);
-        const unsigned long long flag = s & (3ull << 32);
-        if (flag == 0) {
-            if (++spins > kSpinLimit) {
-                set_fault(st, TRAX_ERR_TIMEOUT, TRAX_DETAIL_SCAN_TIMEOUT);
-                break;
-            }
-            __nanosleep(32);
-            continue;
-        }
-        prefix += (uint32_t)s;
-        if (flag == kFlagInc) break;
-        --k;
-    }
-    return prefix;
-}
-
-/*
- * One persistent look-back scan over n items (n read from device memory by
- * the caller).  Producer: uint32_t(uint32_t idx) gives the item value;
- * Consumer: void(uint32_t idx, uint32_t exclusive, uint32_t value).
- * Returns nothing; `on_total` receives the grand total from the last tile.
- */
-template <int ITEMS, class Producer, class Consumer, class Total>
-__device__ __forceinline__ void lookback_scan(uint32_t n, uint32_t *tile_ctr,
-                                              unsigned long long *status, DevState *st,
-                                              Producer prod, Consumer cons, Total on_total)
-{
-    __shared__ uint32_t s_warp[33];
-    __shared__ uint32_t s_tile;
-    __shared__ uint32_t s_prefix;
-    const uint32_t tileItems = blockDim.x * ITEMS;
-    const uint32_t ntiles = (n + tileItems - 1) / tileItems;
-    for (;;) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(tile_ctr, 1u);
-        __syncthreads();
-        const uint32_t tile = s_tile;
-        if (tile >= ntiles) break;
-        const uint32_t base = tile * tileItems + threadIdx.x * ITEMS;
-        uint32_t v[ITEMS];
-        uint32_t sum = 0;
-#pragma unroll
-        for (int k = 0; k < ITEMS; ++k) {
-            v[k] = (base + k < n) ? prod(base + k) : 0u;
-            sum += v[k];
-        }
-        uint32_t agg;
-        const uint32_t excl = block_exclusive_scan(sum, s_warp, &agg);
-        if (threadIdx.x == 0) {
-            uint32_t prefix = 0;
-            if (tile == 0) {
-                st_relaxed64(status, kFlagInc | agg);
-            } else {
-                st_relaxed64(status + tile, kFlagAgg | agg);
-                prefix = lookback_prefix(status, tile, st);
-                st_relaxed64(status + tile, kFlagInc | (uint32_t)(prefix + agg));
-            }
-            s_prefix = prefix;
-            if (tile == ntiles - 1) on_total(prefix + agg);
-        }
-        __syncthreads();
-        uint32_t run = s_prefix + excl;
-#pragma unroll
-        for (int k = 0; k < ITEMS; ++k) {
-            if (base + k < n) cons(base + k, run, v[k]);
-            run += v[k];
-        }
-        __syncthreads();
-    }
-}
-
-/* Tile ticket for persistent look-back loops (thread 0 draws, all read). */
-__device__ __forceinline__ uint32_t next_tile(uint32_t *ctr, uint32_t *s_tile)
-{
-    if (threadIdx.x == 0) *s_tile = atomicAdd(ctr, 1u);
-    __syncthreads();
-    return *s_tile;
-}
-
-/* Publishes this tile's aggregate, looks back for its exclusive prefix and
- * publishes the inclusive prefix; every thread receives the prefix. */
-__device__ __forceinline__ uint32_t tile_prefix(uint32_t tile, uint32_t agg,
-                                                unsigned long long *status, DevState *st,
-                                                uint32_t *s_bcast)
-{
-    if (threadIdx.x == 0) {
-        uint32_t prefix = 0;
-        if (tile == 0) {
-            st_relaxed64(status, kFlagInc | agg);
-        } else {
-            st_relaxed64(status + tile, kFlagAgg | agg);
-            prefix = lookback_prefix(status, tile, st);
-            st_relaxed64(status + tile, kFlagInc | (uint32_t)(prefix + agg));
-        }
-        *s_bcast = prefix;
-    }
-    __syncthreads();
-    return *s_bcast;
-}
-
-/* Warp-wide decoupled look-back for a warp-sized tile: lane i inspects
- * predecessor tile - 1 - i, so 32 predecessors are examined per poll.  The
- * prefix is the sum of the aggregates up to and including the nearest
- * inclusive prefix.  Bounded like lookback_prefix. */
+/* Warp-wide decoupled look-back for a tile: lane i inspects predecessor
+ * tile - 1 - i, so 32 predecessors are examined per poll.  The prefix is the
+ * sum of the aggregates up to and including the nearest inclusive prefix.
+ * A predecessor that shows nothing for kSpinLimit polls records
+ * TRAX_ERR_TIMEOUT and ends the wait. */
 __device__ __forceinline__ uint32_t warp_lookback(unsigned long long *status, uint32_t tile,
                                                   DevState *st)
 {
