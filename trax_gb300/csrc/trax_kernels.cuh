@@ -607,17 +607,23 @@ template <class Visit>
 __device__ __forceinline__ void zscreen_walk(const uint16_t *ZH, uint32_t ra, uint32_t rb,
                                              const ZScreen &zs, Visit &&visit)
 {
-    for (uint32_t j8 = ra & ~7u; j8 < rb; j8 += 8) {
+    if (ra >= rb) return;
+    /* the run's first and last steps keep only the hits inside [ra, rb) */
+    const uint32_t first = ra & ~7u, last = (rb - 1) & ~7u;
+    const uint32_t first_mask = 0xffu & ~((1u << (ra & 7u)) - 1u);
+    const uint32_t last_mask = (2u << ((rb - 1) & 7u)) - 1u;
+    for (uint32_t j8 = first; j8 < rb; j8 += 8) {
         const uint4 q = *reinterpret_cast<const uint4 *>(ZH + j8);
         const uint32_t m0 = zscreen_word(q.x, zs), m1 = zscreen_word(q.y, zs);
         const uint32_t m2 = zscreen_word(q.z, zs), m3 = zscreen_word(q.w, zs);
         if ((m0 | m1 | m2 | m3) == 0u) continue;
-        uint32_t bits = (m0 & 1u) | ((m0 >> 15) & 2u) | ((m1 & 1u) << 2) | ((m1 >> 13) & 8u) |
-                        ((m2 & 1u) << 4) | ((m2 >> 11) & 0x20u) | ((m3 & 1u) << 6) |
-                        ((m3 >> 9) & 0x80u);
-        const uint32_t lo_off = ra > j8 ? ra - j8 : 0u;
-        const uint32_t hi_off = rb - j8 < 8u ? rb - j8 : 8u;
-        bits &= ((1u << hi_off) - 1u) & ~((1u << lo_off) - 1u);
+        /* one bit per half: a byte from each half (0x00 / 0xff), then the
+         * bytes' top bits gathered by a multiply that cannot carry */
+        const uint32_t t01 = __byte_perm(m0, m1, 0x7531u) & 0x80808080u;
+        const uint32_t t23 = __byte_perm(m2, m3, 0x7531u) & 0x80808080u;
+        uint32_t bits = ((t01 * 0x00204081u) >> 28) | (((t23 * 0x00204081u) >> 28) << 4);
+        if (j8 == first) bits &= first_mask;
+        if (j8 == last) bits &= last_mask;
         while (bits) {
             const uint32_t b = __ffs(bits) - 1;
             bits &= bits - 1;
