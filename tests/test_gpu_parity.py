@@ -240,3 +240,29 @@ def test_device_reciprocal_floor_div(gpu_ctx):
         want = np.floor(x / d).astype(np.float32)
     same = (bits(got) == bits(want)) | (np.isnan(got) & np.isnan(want))
     assert same.all(), x[~same][:8]
+
+
+def test_full_size_batch_events_independent(gpu_ctx):
+    """At the benchmark's full size (2048 multimuon events, 6.6 M hits) every
+    event's tracklets equal the event run alone -- events are independent, a
+    property that holds at any size -- checked on a spread of events, with
+    the batch's offsets monotone and ending at the tracklet count."""
+    w = gen.WORKLOADS["multimuon-1000trk"]
+    E = 2048
+    b = gen.generate_batch(w, E)
+    N = b.n_hits
+    T = w.n_triplets
+    p = Pipeline(gpu_ctx, w.config(), w.grid(E), E, N, 80 * N, 80 * N, 8 * N)
+    trk, off, counts = p.seed(b, input_indices=True)
+    assert counts["status"] == 0
+    assert off[0] == 0 and off[-1] == len(trk) == counts["n_tracklets"]
+    assert (np.diff(off.astype(np.int64)) >= 0).all()
+    eoff = b.event_offset
+    for e in (0, 1, 511, 1024, 1777, 2047):
+        one = b.slice_events(e, 1)
+        q = Pipeline(gpu_ctx, w.config(), w.grid(1), 1, one.n_hits, 80 * one.n_hits,
+                     80 * one.n_hits, 8 * one.n_hits)
+        t1, off1, _ = q.seed(one, input_indices=True)
+        lo, hi = off[e * T], off[(e + 1) * T]
+        assert np.array_equal(trk[lo:hi] - eoff[e], t1)
+        assert np.array_equal(off[e * T:(e + 1) * T + 1] - off[e * T], off1)
