@@ -266,3 +266,44 @@ def test_full_size_batch_events_independent(gpu_ctx):
         lo, hi = off[e * T], off[(e + 1) * T]
         assert np.array_equal(trk[lo:hi] - eoff[e], t1)
         assert np.array_equal(off[e * T:(e + 1) * T + 1] - off[e * T], off1)
+
+
+def _drop_buckets(b, drop):
+    """The batch without the hits of the (event, layer) buckets in `drop`
+    (layers 1-based); the emptied buckets stay in the layout with no hits."""
+    keep = np.ones(b.n_hits, bool)
+    ln = b.layer_nhits.copy()
+    for e, l in drop:
+        keep &= ~((b.event == e) & (b.layer == l))
+        ln[e, l - 1] = 0
+    return gen.EventBatch(b.x[keep], b.y[keep], b.z[keep], b.layer[keep], b.detector_id[keep],
+                          b.hit_id[keep], b.event[keep], ln)
+
+
+def test_ragged_batch_equals_oracle(gpu_ctx):
+    """Ragged batches through the batched chain: an empty first and last
+    event, an empty event in the middle, and events with an empty inner,
+    middle or outer layer -- tracklets and every per-(event, layer triplet)
+    offset equal the oracle's."""
+    w = gen.WORKLOADS["multimuon-1000trk"]
+    E, L = 7, w.n_layers
+    b = gen.generate_batch(w, E)
+    drop = [(0, l) for l in range(1, L + 1)] + [(3, l) for l in range(1, L + 1)] + \
+           [(E - 1, l) for l in range(1, L + 1)] + [(1, 1), (2, 2), (4, 3), (5, L)]
+    rb = _drop_buckets(b, drop)
+    assert rb.event_nhits[0] == rb.event_nhits[3] == rb.event_nhits[E - 1] == 0
+    N = rb.n_hits
+    p = Pipeline(gpu_ctx, w.config(), w.grid(E), E, N, 80 * N, 80 * N, 8 * N)
+    trk, off, counts = p.seed(rb)
+    assert counts["status"] == 0
+    r = oracle.run(rb, w.config(), w.grid(E), 4, n_threads=1)
+    assert np.array_equal(trk, oracle.canonical(r)["tracklets"])
+    assert np.array_equal(off, r["trk_offsets"])
+    T = w.n_triplets
+    for e in (0, 3, E - 1):
+        assert off[e * T] == off[(e + 1) * T]
+    # the same batch through the streaming slots and the per-stage calls
+    st = p.wait(p.submit(rb))
+    assert np.array_equal(st[0], trk) and np.array_equal(st[1], off)
+    d = gpu_stages(gpu_ctx, rb, w)
+    assert np.array_equal(d["trk"], trk) and np.array_equal(d["trk_offsets"], off)
