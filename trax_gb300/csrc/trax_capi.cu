@@ -237,14 +237,17 @@ trax_status check_grid(trax_ctx *ctx, const trax_grid_cfg *g, bool need_cfg = tr
 }
 
 /* Dynamic shared memory plan of k_grid_build: W warps with (W+1)*C words.
- * A warp should own about 128 hits of its segment: fewer warps waste the
- * per-warp cell tables, more leave warps idle. */
+ * A warp holds up to 32 * kGridItems hits of its segment in registers;
+ * enough warps for 1.5x the average segment keep the larger layers' segments
+ * on that path (a segment beyond it computes its cells twice), and more
+ * warps would waste the per-warp cell tables. */
 int grid_build_warps(const trax_ctx *ctx, uint32_t C, uint32_t avg_seg, uint32_t stage)
 {
     const size_t budget = std::min<size_t>(ctx->smem_optin, 200 * 1024);
     long w = (long)((budget - 8ull * stage) / (4ull * C)) - 1;
-    long want = 1;
-    while (want < 32 && want * 32 * kGridItems < (long)avg_seg) want <<= 1;
+    const long per_warp = 32 * kGridItems;
+    long want = (long)((3ull * avg_seg / 2 + per_warp - 1) / per_warp);
+    want = std::min<long>(std::max<long>(want, 1), 32);
     if (w > want) w = want;
     return (int)w;
 }

@@ -370,7 +370,14 @@ __global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols o
     const uint32_t nseg = st->n_events * kp.n_layers;
     const uint32_t lt_mask = lanemask_lt();
 
-    for (uint32_t seg = blockIdx.x; seg < nseg; seg += gridDim.x) {
+    /* round k gives CTA b segment k*G + (b + k) mod G: a permutation within
+     * every round that rotates which CTA takes which layer (a plain stride
+     * by G pins each CTA to one layer whenever G is a multiple of the layer
+     * count, and the layers' segment sizes differ) */
+    const uint32_t G = gridDim.x;
+    for (uint32_t k = 0, round = 0; round < nseg; ++k, round += G) {
+        const uint32_t seg = round + (blockIdx.x + k) % G;
+        if (seg >= nseg) continue;  /* block-uniform */
         const uint32_t e = seg / kp.n_layers, l = seg % kp.n_layers;
         const uint32_t start = seg_start[seg], n = seg_n[seg];
         for (uint32_t k = threadIdx.x; k < (uint32_t)W * C; k += blockDim.x) s_cnt[k] = 0;
