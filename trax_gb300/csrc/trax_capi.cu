@@ -327,6 +327,7 @@ trax_status enqueue_grid(trax_ctx *ctx, const InCols &in, const SortedCols &out,
     const size_t smem = ((size_t)(W + 1) * kp.C + 2ull * ctx->gb_stage) * 4;
     uint32_t blocks = std::min<uint32_t>(max_segs, (uint32_t)(ctx->sm_count * per_sm));
     if (blocks == 0) blocks = 1;
+    CK(cudaMemsetAsync(&ctx->d_state->gb_next, 0, 4, ctx->stream));  /* segment counter */
     k_grid_build<<<blocks, W * 32, smem, ctx->stream>>>(kp, in, out, seg_start, seg_n, grid,
                                                         ctx->gb_stage, ctx->d_state);
     CK(cudaGetLastError());

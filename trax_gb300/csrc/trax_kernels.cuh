@@ -71,6 +71,7 @@ struct DevState {
     uint32_t n_pwalk;        /* prediction store records that walk (after them) */
     uint32_t n_ptile;        /* 32-pair tiles of the prediction count pass */
     uint32_t n_ftile;        /* 32-candidate words of the filter's accept mask */
+    uint32_t gb_next;        /* grid build: the next segment a CTA takes */
 };
 
 struct SortedCols {
@@ -314,7 +315,8 @@ __global__ void __launch_bounds__(256) k_scan(const uint32_t *in, uint32_t *out,
 
 /* ------------------------------------------------------------------------
  * Stage 1: grid build.  One CTA per (event, layer) segment (persistent
- * loop).  Counting sort into (z, phi) cells, stable within a cell:
+ * CTAs taking segments from a counter).  Counting sort into (z, phi)
+ * cells, stable within a cell:
  *   pass 1  each warp owns a contiguous sub-range of the segment and counts
  *           its cells (warp match + one shared add per distinct cell);
  *   pass 2  per cell, exclusive prefix over warps and an exclusive scan over
@@ -370,14 +372,17 @@ __global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols o
     const uint32_t nseg = st->n_events * kp.n_layers;
     const uint32_t lt_mask = lanemask_lt();
 
-    /* round k gives CTA b segment k*G + (b + k) mod G: a permutation within
-     * every round that rotates which CTA takes which layer (a plain stride
-     * by G pins each CTA to one layer whenever G is a multiple of the layer
-     * count, and the layers' segment sizes differ) */
-    const uint32_t G = gridDim.x;
-    for (uint32_t k = 0, round = 0; round < nseg; ++k, round += G) {
-        const uint32_t seg = round + (blockIdx.x + k) % G;
-        if (seg >= nseg) continue;  /* block-uniform */
+    /* each CTA takes its next segment from a counter as it finishes one:
+     * the layers' segment sizes differ, and a fixed stride by the grid size
+     * would pin every CTA to one layer (the grid is a multiple of the layer
+     * count).  Every thread reads s_seg before the segment's last barrier,
+     * after which thread 0 may overwrite it. */
+    __shared__ uint32_t s_seg;
+    for (;;) {
+        if (threadIdx.x == 0) s_seg = atomicAdd(&st->gb_next, 1u);
+        __syncthreads();
+        const uint32_t seg = s_seg;
+        if (seg >= nseg) break;  /* block-uniform */
         const uint32_t e = seg / kp.n_layers, l = seg % kp.n_layers;
         const uint32_t start = seg_start[seg], n = seg_n[seg];
         for (uint32_t k = threadIdx.x; k < (uint32_t)W * C; k += blockDim.x) s_cnt[k] = 0;
