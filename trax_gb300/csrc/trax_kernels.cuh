@@ -385,7 +385,12 @@ __global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols o
         if (seg >= nseg) break;  /* block-uniform */
         const uint32_t e = seg / kp.n_layers, l = seg % kp.n_layers;
         const uint32_t start = seg_start[seg], n = seg_n[seg];
-        for (uint32_t k = threadIdx.x; k < (uint32_t)W * C; k += blockDim.x) s_cnt[k] = 0;
+        {
+            const uint32_t nw = (uint32_t)W * C, n4 = nw >> 2;
+            for (uint32_t k = threadIdx.x; k < n4; k += blockDim.x)
+                reinterpret_cast<uint4 *>(s_cnt)[k] = make_uint4(0u, 0u, 0u, 0u);
+            for (uint32_t k = (n4 << 2) + threadIdx.x; k < nw; k += blockDim.x) s_cnt[k] = 0;
+        }
         __syncthreads();
         const uint32_t chunk = (n + W - 1) / W;
         const uint32_t lo = min(n, w * chunk), hi = min(n, lo + chunk);
@@ -474,12 +479,10 @@ __global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols o
             }
         }
         __syncthreads();
-        for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
-            const uint32_t b = s_tot[c];  /* segment-relative */
-            grid[(size_t)seg * C + c] = start + b;
-            for (int q = 0; q < W; ++q) s_cnt[q * C + c] += b;
-        }
-        __syncthreads();
+        /* s_tot now holds the cell starts and s_cnt each warp's offset inside
+         * the cell: a hit's position is their sum plus its rank in the warp */
+        for (uint32_t c = threadIdx.x; c < C; c += blockDim.x)
+            grid[(size_t)seg * C + c] = start + s_tot[c];
 
         /* pass 3: positions (segment-relative) */
         if (staged && cached) {
@@ -489,7 +492,7 @@ __global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols o
                 if (b < hi) {  /* warp-uniform */
                     const bool valid = b + lane < hi;
                     uint32_t pos = 0;
-                    if (valid) pos = s_cnt[w * C + ccell[j]] + __popc(cpeers[j] & lt_mask);
+                    if (valid) pos = s_tot[ccell[j]] + s_cnt[w * C + ccell[j]] + __popc(cpeers[j] & lt_mask);
                     __syncwarp();
                     if (valid && lane == __ffs(cpeers[j]) - 1) s_cnt[w * C + ccell[j]] += __popc(cpeers[j]);
                     __syncwarp();
@@ -513,7 +516,7 @@ __global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols o
                     bool bad;
                     cell = hit_cell(kp, x, y, z, &phi, &bad);
                     peers = __match_any_sync(act, cell);
-                    pos = s_cnt[w * C + cell] + __popc(peers & lt_mask);
+                    pos = s_tot[cell] + s_cnt[w * C + cell] + __popc(peers & lt_mask);
                 }
                 __syncwarp();
                 if (valid && lane == __ffs(peers) - 1) s_cnt[w * C + cell] += __popc(peers);
