@@ -89,6 +89,7 @@ struct trax_ctx {
     DevBuf xyzp;  /* packed (x, y, z, phi) of the sorted hits */
     cudaEvent_t timers[kTimerSlots] = {};
     int blk_pair = 0, blk_pair0 = 0, blk_pair_lane = 0, blk_pair_count = 0, blk_pair_store = 0, blk_sector = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
+    int blk_pstore = 0, blk_fstore = 0;  /* the store passes: their own occupancy */
 
     /* batched pipeline */
     bool reserved = false;
@@ -463,7 +464,7 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
     k_scan<kScanItems><<<std::min<uint32_t>(ctx->blk_scan, ntile), kScanThreads, 0, ctx->stream>>>(
         ptile, ptile, &st->n_ptile, ptiles, &st->n_cands, 1, (unsigned long long *)ctx->st1.p, st);
     if ((s = mark(ctx, "predict_scan")) != TRAX_OK) return s;
-    k_predict_store<<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
+    k_predict_store<<<ctx->blk_pstore, kFusedThreads, 0, ctx->stream>>>(
         kp, grid, h.zphi, h.zh, recs,
         rec_cap, walk_cap, cexcl, ptile, &st->n_pairs, pair_cap, &st->n_cands, cands, cand_cap, st);
     if ((s = mark(ctx, "predict_store")) != TRAX_OK) return s;
@@ -502,7 +503,7 @@ trax_status enqueue_filter(trax_ctx *ctx, const SortedCols &h, const uint2 *pair
     k_scan<kScanItems><<<std::min<uint32_t>(ctx->blk_scan, ntile), kScanThreads, 0, ctx->stream>>>(
         wpos, wpos, &st->n_ftile, words, &st->n_trk, 2, (unsigned long long *)ctx->st2.p, st);
     if ((s = mark(ctx, "filter_scan")) != TRAX_OK) return s;
-    k_filter_store<<<ctx->blk_filter, 256, 0, ctx->stream>>>(pairs, cands, mask, wpos, t1, t2, t3,
+    k_filter_store<<<ctx->blk_fstore, 256, 0, ctx->stream>>>(pairs, cands, mask, wpos, t1, t2, t3,
                                                              trk_cap, st);
     if ((s = mark(ctx, "filter_store")) != TRAX_OK) return s;
     bool by_mask = cand_offsets != nullptr;
@@ -792,6 +793,12 @@ trax_status trax_ctx_create(trax_ctx **out, int device)
     ctx->blk_pred = ctx->sm_count * std::max(b, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_filter_count, 256, 0);
     ctx->blk_filter = ctx->sm_count * std::max(b, 1);
+    /* the store passes are bound by load latency and use fewer registers
+     * than their count passes: a full complement of their own blocks */
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_predict_store, kFusedThreads, 0);
+    ctx->blk_pstore = ctx->sm_count * std::max(b, 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_filter_store, 256, 0);
+    ctx->blk_fstore = ctx->sm_count * std::max(b, 1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_scan<kScanItems>, kScanThreads, 0);
     ctx->blk_scan = ctx->sm_count * std::max(b, 1);
     ctx->blk_small = ctx->sm_count * 2;
