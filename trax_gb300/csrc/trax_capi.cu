@@ -1882,12 +1882,14 @@ static trax_status submit_slot(trax_ctx *ctx, const trax_event_batch *in,
     }
     CK(cudaStreamWaitEvent(ctx->stream, a.h2d_done, 0));
     if (event_base && in->n_hits)
-        k_rebase_events<<<ctx->blk_small, 256, 0, ctx->stream>>>((uint32_t *)a.in_cols[6].p,
+        k_rebase_events<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>((uint32_t *)a.in_cols[6].p,
                                                                 in->n_hits, event_base);
     CK(cudaMemcpyAsync(ctx->d_state, seg + 2 * nseg_r, 8, cudaMemcpyDeviceToDevice, ctx->stream));
     CK(cudaGraphLaunch(a.graph, ctx->stream));
     const uint32_t n_off = in->n_events * ctx->kp.n_lt + 1;
-    k_emit<<<ctx->blk_small, 256, 0, ctx->stream>>>(
+    /* a full grid: the input-position mapping is a dependent gather per
+     * tracklet hit, bound by load latency */
+    k_emit<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(
         ctx->d_state, a.h_snap, out->input_indices ? (const uint32_t *)ctx->srt_cols[8].p : nullptr,
         (const uint32_t *)ctx->trk_cols[0].p, (const uint32_t *)ctx->trk_cols[1].p,
         (const uint32_t *)ctx->trk_cols[2].p, ctx->r_trk, (uint32_t *)a.res[0].p,
