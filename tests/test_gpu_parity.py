@@ -307,3 +307,23 @@ def test_ragged_batch_equals_oracle(gpu_ctx):
     assert np.array_equal(st[0], trk) and np.array_equal(st[1], off)
     d = gpu_stages(gpu_ctx, rb, w)
     assert np.array_equal(d["trk"], trk) and np.array_equal(d["trk_offsets"], off)
+
+
+def test_mixed_segment_sizes_equal_oracle(gpu_ctx):
+    """One pile-up-200 event batched with multimuon events (one
+    configuration): the grid build's plan follows the average segment, so
+    the pile-up segments take the unstaged path that scatters each column
+    while the multimuon segments are staged in shared memory -- both kinds
+    in one launch, with tracklets and offsets equal to the oracle's."""
+    wp = gen.WORKLOADS["pileup200"]
+    wm = gen.WORKLOADS["multimuon-1000trk"]
+    b = gen.EventBatch.concat([gen.generate_batch(wp, 1), gen.generate_batch(wm, 3)])
+    E, N = b.n_events, b.n_hits
+    assert b.layer_nhits.max() > 2 * N / (E * b.n_layers)
+    cfg = wp.config()
+    p = Pipeline(gpu_ctx, cfg, wp.grid(E), E, N, 80 * N, 80 * N, 8 * N)
+    trk, off, counts = p.seed(b)
+    assert counts["status"] == 0
+    r = oracle.run(b, cfg, wp.grid(E), 4, n_threads=1, omp_threads=4)
+    assert np.array_equal(trk, oracle.canonical(r)["tracklets"])
+    assert np.array_equal(off, r["trk_offsets"])
