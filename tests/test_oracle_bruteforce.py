@@ -1,4 +1,5 @@
-"""The oracle's pair and prediction stages against brute force.
+"""The oracle's pair, prediction and filter stages against numpy
+restatements (brute force for the windows).
 
 The reference visits only the grid cells its windows' sector ranges cover
 (PairGeneratorBeamspot.h:172-230, TripletThetaPhiPredictor.h:170-233 and
@@ -11,7 +12,9 @@ order), test EVERY hit of the event's target layer against them, and check:
   oracle's numbers, and the stored candidates are the first min(A, B)
   window-B accepts in the reference's visit order: z row, then (with
   wrap-around) the cells from phiLowSector to the row end before those from
-  the row start, then position.
+  the row start, then position;
+- the filter's cuts, restated from the kernel text, accept exactly the
+  oracle's tracklets.
 """
 import numpy as np
 import pytest
@@ -195,3 +198,62 @@ def test_prediction_equals_brute_force(name, n_ev):
     assert slots == r["stats"]["cand_slots"]
     assert truncated == r["stats"]["cand_truncated"]
     assert got == want
+
+
+def _atan2(y, x):
+    return oracle.math_batch(0, np.asarray(y, F), np.asarray(x, F))
+
+
+@pytest.mark.parametrize("name,n_ev", CASES)
+def test_filter_equals_numpy_restatement(name, n_ev):
+    """filterCount (TripletThetaPhiFilter.h:50-168) restated in numpy from
+    the kernel text -- dTheta ratio, dPhi with wrap fix, the circle fit on the
+    paraboloid (normalize(v) = v / sqrt(dot(v, v)), the project's reading of
+    the OpenCL built-in), TIP and minimum radius -- applied to every oracle
+    candidate: the accepted candidates, in candidate order, are the oracle's
+    tracklets, and each (event, layer triplet) offset counts the accepted
+    candidates before the group's first candidate."""
+    w, cfg, r, rminc = _run(name, n_ev, 4)
+    X, Y, Z = r["sorted_x"], r["sorted_y"], r["sorted_z"]
+    LAY = r["sorted_layer"].astype(np.int64)
+    cv = r["cand_valid"].astype(bool)
+    cands, pairs = r["cands"], r["pairs"]
+    h1 = pairs[cands[:, 0], 0].astype(np.int64)
+    h2 = pairs[cands[:, 0], 1].astype(np.int64)
+    h3 = cands[:, 1].astype(np.int64)
+    lt = LAY[h1] - 1
+    d_theta = np.array([cfg.triplets[t].dtheta_cut for t in range(cfg.n_layer_triplets)], F)[lt]
+    d_phi_cut = np.array([cfg.triplets[t].dphi_cut for t in range(cfg.n_layer_triplets)], F)[lt]
+    tip_cut = np.array([cfg.triplets[t].tip_cut for t in range(cfg.n_layer_triplets)], F)[lt]
+    x1, y1, z1, x2, y2, z2, x3, y3, z3 = X[h1], Y[h1], Z[h1], X[h2], Y[h2], Z[h2], X[h3], Y[h3], Z[h3]
+    a1 = _atan2(np.sqrt((x2 - x1) * (x2 - x1) + (y2 - y1) * (y2 - y1)), z2 - z1)
+    a2 = _atan2(np.sqrt((x3 - x2) * (x3 - x2) + (y3 - y2) * (y3 - y2)), z3 - z2)
+    delta = np.abs(a2 / a1)
+    valid = (F(1) - d_theta <= delta) & (delta <= F(1) + d_theta)
+    a1 = _atan2(y2 - y1, x2 - x1)
+    a2 = _atan2(y3 - y2, x3 - x2)
+    delta = a2 - a1
+    delta = delta + np.where(delta > PI, F(-2) * PI, np.where(delta < -PI, F(2) * PI, F(0)))
+    valid &= np.abs(delta) <= d_phi_cut
+    p1z, p2z, p3z = x1 * x1 + y1 * y1, x2 * x2 + y2 * y2, x3 * x3 + y3 * y3
+    ax, ay, az = x2 - x1, y2 - y1, p2z - p1z
+    bx, by, bz = x3 - x1, y3 - y1, p3z - p1z
+    nx, ny, nz = ay * bz - az * by, az * bx - ax * bz, ax * by - ay * bx
+    nlen = np.sqrt(nx * nx + ny * ny + nz * nz)
+    nx, ny, nz = nx / nlen, ny / nlen, nz / nlen
+    cox, coy = (-nx) / (F(2) * nz), (-ny) / (F(2) * nz)
+    c = -(nx * x1 + ny * y1 + nz * p1z)
+    c_r = np.sqrt((F(1) - nz * nz - F(4) * c * nz) / (F(4) * nz * nz))
+    vx, vy = -cox, -coy
+    vlen = np.sqrt(vx * vx + vy * vy)
+    vx, vy = vx / vlen, vy / vlen
+    pcx, pcy = cox + c_r * vx, coy + c_r * vy
+    tip = pcx * pcx + pcy * pcy
+    valid &= tip <= tip_cut * tip_cut
+    valid &= c_r >= rminc
+    valid &= cv
+    trk = np.stack([h1[valid], h2[valid], h3[valid]], axis=1)
+    got = np.stack([r["trk_h1"], r["trk_h2"], r["trk_h3"]], axis=1).astype(np.int64)
+    assert np.array_equal(got, trk)
+    before = np.concatenate([[0], np.cumsum(valid)])
+    assert np.array_equal(r["trk_offsets"].astype(np.int64), before[r["cand_offsets"]])
