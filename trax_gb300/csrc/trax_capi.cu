@@ -741,14 +741,24 @@ float trax_min_radius_curvature(float min_pt, float bz)
 
 trax_status trax_ctx_create(trax_ctx **out, int device)
 {
-    if (!out) return TRAX_ERR_BAD_ARG;
+    if (!out) {
+        g_create_error = "trax_ctx_create: out is NULL";
+        return TRAX_ERR_BAD_ARG;
+    }
     *out = nullptr;
     int n = 0;
-    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    const cudaError_t ce = cudaGetDeviceCount(&n);
+    if (ce != cudaSuccess || n == 0) {
+        g_create_error = std::string("trax_ctx_create: no CUDA device (") +
+                         (ce != cudaSuccess ? cudaGetErrorString(ce) : "device count 0") + ")";
         cudaGetLastError();
         return TRAX_ERR_NO_DEVICE;
     }
-    if (device < 0 || device >= n) return TRAX_ERR_BAD_ARG;
+    if (device < 0 || device >= n) {
+        g_create_error = "trax_ctx_create: device " + std::to_string(device) + " of " +
+                         std::to_string(n);
+        return TRAX_ERR_BAD_ARG;
+    }
     trax_ctx *ctx = new trax_ctx();
     ctx->device = device;
     auto bail = [&](cudaError_t e) {
