@@ -162,7 +162,9 @@ typedef struct trax_counts {
 #define TRAX_DETAIL_SCAN_TIMEOUT 7u
 #define TRAX_DETAIL_BAD_TRIPLET_INDEX 8u
 
-/* ---- context ---------------------------------------------------------- */
+/* ---- context ----------------------------------------------------------
+ * Replaces the clever::context the reference's operators take
+ * (createContext, TripletBuilder.cpp:52-92): one CUDA device and a stream. */
 
 const char *trax_version(void);
 trax_status trax_ctx_create(trax_ctx **out, int device);
@@ -222,7 +224,9 @@ trax_status trax_set_pair_generator(trax_ctx *ctx, int generator);
 int trax_get_pair_generator(const trax_ctx *ctx);
 trax_status trax_get_tuning(const trax_ctx *ctx, trax_tuning *t);
 
-/* ---- device memory helpers (for hosts without their own CUDA binding) -- */
+/* ---- device memory helpers (for hosts without their own CUDA binding) --
+ * Stand in for clever::OpenCLTransfer's initBuffers / toDevice / fromDevice
+ * on the collections (HitCollection.h:57, TripletBuilder.cpp:225-238). */
 
 trax_status trax_dev_alloc(trax_ctx *ctx, void **ptr, size_t bytes);
 trax_status trax_dev_free(trax_ctx *ctx, void *ptr);
@@ -231,7 +235,9 @@ trax_status trax_host_free_pinned(trax_ctx *ctx, void *ptr);
 trax_status trax_memcpy_h2d(trax_ctx *ctx, void *dst, const void *src, size_t bytes);
 trax_status trax_memcpy_d2h(trax_ctx *ctx, void *dst, const void *src, size_t bytes);
 trax_status trax_memset_d(trax_ctx *ctx, void *dst, int value, size_t bytes);
-/* CUDA-event timing on the context stream: record marks, read elapsed ms. */
+/* CUDA-event timing on the context stream: record marks, read elapsed ms
+ * (the per-stage times the reference's RuntimeRecord collects from OpenCL
+ * events, RuntimeRecord.h:67). */
 trax_status trax_timer_record(trax_ctx *ctx, int slot);
 trax_status trax_timer_elapsed_ms(trax_ctx *ctx, int slot_begin, int slot_end, float *ms);
 
@@ -469,7 +475,10 @@ trax_status trax_eval_math(trax_ctx *ctx, int fn, const float *d_a, const float 
                            float *d_out, uint32_t n);
 trax_status trax_reset_counts(trax_ctx *ctx);
 
-/* ---- batched pipeline ------------------------------------------------- */
+/* ---- batched pipeline -------------------------------------------------
+ * The body of the reference's event-group loop (TripletBuilder.cpp:186-263:
+ * addEvent, uploads, the four stages, the result downloads) as one call on
+ * reserved buffers and one CUDA graph. */
 
 /* Host-side batch of events, bucketed as HitCollection::addEvent does. */
 typedef struct trax_event_batch {
@@ -538,7 +547,9 @@ trax_status trax_kernel_times(trax_ctx *ctx, float *ms, const char **names, int 
 /* Kernels launched by the last pipeline enqueue (graph capture or eager). */
 int trax_kernel_launches(const trax_ctx *ctx);
 
-/* ---- continuous-batching server -------------------------------------- */
+/* ---- continuous-batching server --------------------------------------
+ * No counterpart in the reference, which runs its event groups one after
+ * another (TripletBuilder.cpp:186). */
 
 /* Requests are single events.  `slots` worker threads each own a context
  * (stream, reserved buffers, graph); each takes every request that has
