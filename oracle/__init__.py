@@ -1,7 +1,8 @@
 """ctypes driver for the CPU oracle (trax_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and the CPU-baseline
-leg of bench.py use it as the checker.  Parity status: parity unpinned (see
+leg of bench.py use it as the checker.  Parity status: pinned to the
+reference's own kernels (oracle/ref.py, tests/test_ref_pin.py; see
 trax_oracle.h).
 """
 from __future__ import annotations

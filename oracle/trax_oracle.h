@@ -7,13 +7,16 @@
  * at each function in trax_oracle.c), using the same project FP32 math
  * (trax_gb300/csrc/trax_math.h) as the CUDA kernels.
  *
- * Parity status: parity unpinned.  The reference cannot be built or run in
- * this environment (empty `clever` submodule, no OpenCL headers or device,
- * no Boost, no protobuf-2.4 runtime) and its own tests hold no golden
- * vectors for this path.  The oracle is pinned only by the reference's two
- * self-checks -- the all-ones scan (src/trax_test/trax_test.cpp:473-479) and
- * the GridBuilder::verifyGrid invariants (GridBuilder.cpp:187-224) -- and by
- * hand-derived known-answer events in tests/.
+ * Parity status: pinned to the reference's own kernels.  The reference's host
+ * side cannot be built here (empty `clever` submodule, no OpenCL headers or
+ * device, no Boost, no protobuf-2.4 runtime), but its OpenCL kernel text can:
+ * oracle/ref_build.py compiles it for the host into oracle/_ref, and
+ * tests/test_ref_pin.py shows this restatement equal to it element for
+ * element (grid, sorted columns, pair and candidate slots, tracklets, every
+ * offset array, slot totals) on every workload, at the reference's
+ * work-group sizes, for every kernel variant and both pair generators, and on
+ * the reference's own ttbar events.  The golden vectors of tests/golden/ are
+ * the reference kernels' output.
  */
 #ifndef TRAX_ORACLE_H
 #define TRAX_ORACLE_H

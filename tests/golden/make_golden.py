@@ -1,11 +1,20 @@
-"""Writes the golden fixtures: seeded synthetic inputs and the oracle's
+"""Writes the golden fixtures: seeded synthetic inputs and the reference's
 outputs for them (grid, sorted order, pairs, candidates as hit triples,
 tracklets, offsets, slot counts).
 
     python tests/golden/make_golden.py
 
-The oracle is the CPU restatement in oracle/; these files pin it against
-itself across machines and pin the GPU path against stored vectors.
+The outputs come from the reference's own OpenCL kernels, compiled for the
+host by oracle/ref_build.py (it needs the reference tree, so this script runs
+where the tree is), with one work-item per grid work-group so that the
+within-cell order is the input order.  The input position of each sorted hit
+is read back through the DetectorId column, which the seeding kernels only
+copy: the run gives each hit its own position there.  The one figure the
+reference's chain does not produce -- how many store-window accepts the
+prediction store drops at the count -- comes from the CPU restatement in
+oracle/, after checking that the restatement reproduces every other output.
+These files pin the restatement on any machine (tests/test_golden.py) and the
+GPU path against stored vectors.
 """
 import os
 import sys
@@ -17,6 +26,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 import oracle  # noqa: E402
+from oracle import ref  # noqa: E402
 from trax_gb300 import gen  # noqa: E402
 
 CASES = (("single-muon-100trk", 3), ("multimuon-1000trk", 1), ("pileup50-batch100", 1))
@@ -37,9 +47,17 @@ def main():
         w = gen.WORKLOADS[name]
         b = gen.generate_batch(w, n_ev)
         cfg, g = w.config(), w.grid(n_ev)
-        r = oracle.run(b, cfg, g, 4, n_threads=1)
+        tagged = gen.EventBatch(b.x, b.y, b.z, b.layer, np.arange(b.n_hits, dtype=np.uint32),
+                                b.hit_id, b.event, b.layer_nhits)
+        r = ref.run(tagged, cfg, g, 4, n_threads=1, grid_threads=1)
+        assert r["stats"]["status"] == 0, r["stats"]
+        r["sorted_orig"] = r["sorted_det"]
+        o = oracle.run(b, cfg, g, 4, n_threads=1)
+        for k in ("grid", "sorted_orig", "pair_offsets", "cand_offsets", "trk_h1", "trk_h2",
+                  "trk_h3", "trk_offsets"):
+            assert np.array_equal(o[k], r[k]), k
         c = oracle.canonical(r)
-        st = r["stats"]
+        st = dict(r["stats"], cand_truncated=o["stats"]["cand_truncated"])
         np.savez_compressed(
             os.path.join(HERE, f"{name}_{n_ev}ev.npz"),
             x=b.x, y=b.y, z=b.z, layer=b.layer, detector_id=b.detector_id, hit_id=b.hit_id,

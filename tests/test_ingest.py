@@ -12,7 +12,9 @@ from pb_util import container, encode_event, event_store, synth_events, _ld, _u,
 from trax_gb300 import ingest
 from trax_gb300.runtime import TraxError
 
-TTBAR = "/root/reference/plotting/data/physics/hits.ttBar.pb"
+from oracle.ref_build import DEFAULT_REFERENCE  # noqa: E402
+
+TTBAR = os.path.join(DEFAULT_REFERENCE, "plotting", "data", "physics", "hits.ttBar.pb")
 COLS = ("run", "lumi", "event_number", "hit_offset", "x", "y", "z", "detector_type", "layer",
         "detector_id", "hit_id", "sim_track_id", "sim_track_pt")
 

@@ -13,8 +13,9 @@ import oracle
 from trax_gb300 import gen, ingest
 from trax_gb300._abi import make_config
 
-REF = "/root/reference"
-TTBAR = REF + "/plotting/data/physics/hits.ttBar.pb"
+from oracle.ref_build import DEFAULT_REFERENCE as REF  # noqa: E402
+
+TTBAR = os.path.join(REF, "plotting", "data", "physics", "hits.ttBar.pb")
 
 
 @pytest.fixture(scope="module")
