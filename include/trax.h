@@ -289,24 +289,49 @@ trax_status trax_triplet_filter(trax_ctx *ctx, const trax_sorted_hits *hits,
 trax_status trax_prefix_sum(trax_ctx *ctx, const uint32_t *d_in, uint32_t *d_out, uint32_t n,
                             uint32_t *d_total);
 
-/* Allocation-free exclusive scan.  No counterpart in the reference: it is
- * for callers that cannot call cudaMalloc -- code running inside another
- * framework's memory pool or allocator lock, or inside a stream capture
- * where allocation is not allowed.  Same result as trax_prefix_sum, but no
- * context and no allocation: the kernel's look-back scratch is a file-scope
- * device array of about 33 KB that every GPU loading this library holds
- * until the process exits.  n is limited to TRAX_PREFIX_SUM_NOALLOC_MAX
- * (larger n returns TRAX_ERR_BAD_ARG; the message is in
- * trax_prefix_sum_noalloc_error()).  Runs on the current device and on
+/* Allocation-free exclusive scan.  No counterpart in the reference.  Some
+ * callers of this library cannot call cudaMalloc at the point where they
+ * need a scan: code that runs inside another framework's memory pool or
+ * allocator callback (a cudaMalloc there re-enters that allocator or waits
+ * on its lock), code whose device memory a pool has already reserved in
+ * full (a cudaMalloc there fails), and latency-critical paths that cannot
+ * take cudaMalloc's implicit device synchronisation.  For them this entry
+ * point takes no context and allocates nothing: the look-back scratch of its
+ * kernel is a file-scope device array of (TRAX_PREFIX_SUM_NOALLOC_MAX / 4096
+ * + 1) 8-byte tile words plus about 100 bytes of counters -- 16.5 KB -- that
+ * every GPU which loads this library holds until the process exits.  Same
+ * result as trax_prefix_sum.  n is limited to TRAX_PREFIX_SUM_NOALLOC_MAX;
+ * a larger n returns TRAX_ERR_BAD_ARG, with the message in
+ * trax_prefix_sum_noalloc_error().  Runs on the current device and on
  * `stream` (a cudaStream_t, NULL = the legacy default stream).  The first
  * call on each device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
- * Every call clears and reuses the same array, so calls that overlap on the
- * GPU (different streams, or threads without ordering) race: serialise them. */
+ * (cudaGetSymbolAddress) and caches it; make that first call before any
+ * stream capture.  Every call clears and reuses the same array, so calls
+ * that overlap on the GPU (different streams, or threads without ordering)
+ * race: serialise them.
+ *
+ * The kernel's waits are bounded; a wait that gives up is recorded in the
+ * array and makes that call's output invalid.  trax_prefix_sum_noalloc_status
+ * synchronises `stream` and returns TRAX_OK or the status the last call on
+ * the current device recorded (TRAX_ERR_TIMEOUT); the next call clears it.
+ * trax_prefix_sum_noalloc_error() returns the calling thread's last message;
+ * the pointer stays valid until that thread's next failing call. */
 #define TRAX_PREFIX_SUM_NOALLOC_MAX 8388608u
 trax_status trax_prefix_sum_noalloc(const uint32_t *d_in, uint32_t *d_out, uint32_t n,
                                     uint32_t *d_total, void *stream);
+trax_status trax_prefix_sum_noalloc_status(void *stream);
 const char *trax_prefix_sum_noalloc_error(void);
+
+/* Self-test of the bounded waits (no counterpart in the reference: it has no
+ * kernel-side error reporting).  Runs trax_prefix_sum's scan kernel over n
+ * elements (n > 4096, device pointers) with tile 0 never taken, so the next
+ * tile's look-back waits for a predecessor that never publishes, and with a
+ * look-back limit of spin_limit polls for this launch only.  The wait gives
+ * up, the kernel records TRAX_ERR_TIMEOUT / TRAX_DETAIL_SCAN_TIMEOUT in the
+ * context's status (trax_counts) and returns; d_out is then not a scan.  The
+ * context stays usable (trax_reset_counts clears the status). */
+trax_status trax_selftest_lookback_timeout(trax_ctx *ctx, const uint32_t *d_in, uint32_t *d_out,
+                                           uint32_t n, uint32_t spin_limit);
 
 /* TripletConnectivity::run (src/algorithms/TripletConnectivity.h:52-54,
  * .cpp:21-71): following_con[f] += sum over base tracklets b that chain

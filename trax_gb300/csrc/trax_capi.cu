@@ -618,7 +618,10 @@ static __device__ __align__(256) unsigned long long g_noalloc_scratch[kNoAllocWo
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mutex;
 void *g_noalloc_addr[kMaxDevices] = {};
-std::string g_noalloc_error;
+/* per calling thread: a failure on one thread never overwrites another
+ * thread's message, and the pointer trax_prefix_sum_noalloc_error() returns
+ * stays valid until this thread's next failing call */
+thread_local std::string g_noalloc_error;
 
 __global__ void k_set_u32(uint32_t *dst, uint32_t v) { *dst = v; }
 
@@ -626,7 +629,11 @@ __global__ void k_set_u32(uint32_t *dst, uint32_t v) { *dst = v; }
  * once per device (the host-side symbol is only a stand-in). */
 trax_status noalloc_scratch(int dev, unsigned long long **out)
 {
-    if (dev < 0 || dev >= kMaxDevices) return TRAX_ERR_BAD_ARG;
+    if (dev < 0 || dev >= kMaxDevices) {
+        g_noalloc_error = "trax_prefix_sum_noalloc: device " + std::to_string(dev) +
+                          " beyond the " + std::to_string(kMaxDevices) + " devices it serves";
+        return TRAX_ERR_BAD_ARG;
+    }
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
     if (!g_noalloc_addr[dev]) {
         void *ptr = nullptr;
@@ -1094,6 +1101,59 @@ trax_status trax_prefix_sum_noalloc(const uint32_t *d_in, uint32_t *d_out, uint3
 }
 
 const char *trax_prefix_sum_noalloc_error(void) { return g_noalloc_error.c_str(); }
+
+trax_status trax_prefix_sum_noalloc_status(void *stream)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        g_noalloc_error = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
+        cudaGetLastError();
+        return TRAX_ERR_NO_DEVICE;
+    }
+    unsigned long long *scratch = nullptr;
+    trax_status s = noalloc_scratch(dev, &scratch);
+    if (s != TRAX_OK) return s;
+    uint32_t word[2] = {0, 0};  /* DevState::status, DevState::detail */
+    const DevState *ds = (const DevState *)scratch;
+    cudaStream_t st = (cudaStream_t)stream;
+    e = cudaMemcpyAsync(word, &ds->status, sizeof(word), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        g_noalloc_error = std::string("trax_prefix_sum_noalloc_status: ") + cudaGetErrorString(e);
+        cudaGetLastError();
+        return TRAX_ERR_DEVICE;
+    }
+    if (word[0] != TRAX_OK) {
+        g_noalloc_error = "trax_prefix_sum_noalloc: the look-back wait gave up (detail " +
+                          std::to_string(word[1]) + "); that call's output is not a valid scan";
+        return (trax_status)word[0];
+    }
+    return TRAX_OK;
+}
+
+trax_status trax_selftest_lookback_timeout(trax_ctx *ctx, const uint32_t *d_in, uint32_t *d_out,
+                                           uint32_t n, uint32_t spin_limit)
+{
+    const uint32_t items = kScanThreads * kScanItems;
+    if (!ctx || !d_in || !d_out || n <= items || spin_limit == 0) return TRAX_ERR_BAD_ARG;
+    trax_status s = ensure(ctx, ctx->st3, (size_t)tiles_for(n, items) * 8);
+    if (s != TRAX_OK) return s;
+    DevState *st = ctx->d_state;
+    CK(cudaMemsetAsync(ctx->st3.p, 0, (size_t)tiles_for(n, items) * 8, ctx->stream));
+    k_set_u32<<<1, 1, 0, ctx->stream>>>(&st->aux_n, n);
+    k_set_u32<<<1, 1, 0, ctx->stream>>>(&st->spin_limit, spin_limit);
+    /* tickets start at 1: no CTA ever takes tile 0, so tile 1 waits for a
+     * predecessor that never publishes */
+    k_set_u32<<<1, 1, 0, ctx->stream>>>(&st->tile_ctr[3], 1u);
+    const uint32_t blocks = std::max(1u, std::min<uint32_t>((n + items - 1) / items,
+                                                            (uint32_t)ctx->blk_scan));
+    k_scan<kScanItems><<<blocks, kScanThreads, 0, ctx->stream>>>(
+        d_in, d_out, &st->aux_n, n, nullptr, 3, (unsigned long long *)ctx->st3.p, st);
+    k_set_u32<<<1, 1, 0, ctx->stream>>>(&st->spin_limit, 0u);
+    CK(cudaGetLastError());
+    return TRAX_OK;
+}
 
 trax_status trax_ingest(trax_ctx *ctx, const trax_raw_hits *raw, const trax_ingest_cfg *cfg,
                         const uint32_t *d_det_ids, uint32_t n_det_ids, trax_hits_out *out,

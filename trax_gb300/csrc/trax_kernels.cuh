@@ -72,6 +72,7 @@ struct DevState {
     uint32_t n_ptile;        /* 32-pair tiles of the prediction count pass */
     uint32_t n_ftile;        /* 32-candidate words of the filter's accept mask */
     uint32_t gb_next;        /* grid build: the next segment a CTA takes */
+    uint32_t spin_limit;     /* look-back polls before a wait gives up; 0 = kSpinLimit */
 };
 
 struct SortedCols {
@@ -160,8 +161,9 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *s
  * Decoupled look-back (Merrill & Garland, "Single-pass Parallel Prefix Scan
  * with Decoupled Look-back", 2016).  Tile status words pack a 2-bit flag
  * (1 aggregate, 2 inclusive prefix) above a 32-bit value.  Waits are
- * bounded: after kSpinLimit polls the tile records TRAX_ERR_TIMEOUT and
- * treats the missing predecessor as 0, so the kernel always terminates.
+ * bounded: after kSpinLimit polls (DevState::spin_limit when set) the tile
+ * records TRAX_ERR_TIMEOUT and treats the missing predecessor as 0, so the
+ * kernel always terminates.
  * ---------------------------------------------------------------------- */
 constexpr unsigned long long kFlagAgg = 1ull << 32;
 constexpr unsigned long long kFlagInc = 2ull << 32;
@@ -188,7 +190,7 @@ __device__ __forceinline__ uint32_t warp_lookback(unsigned long long *status, ui
         const uint32_t first_inc = inc ? (uint32_t)(__ffs(inc) - 1) : 32u;
         const uint32_t upto = first_inc < 32 ? ((first_inc == 31) ? kFull : ((2u << first_inc) - 1u)) : kFull;
         if (zero & upto) {
-            if (++spins > kSpinLimit) {
+            if (++spins > (st->spin_limit ? st->spin_limit : kSpinLimit)) {
                 if (lane == 0) set_fault(st, TRAX_ERR_TIMEOUT, TRAX_DETAIL_SCAN_TIMEOUT);
                 break;
             }

@@ -92,6 +92,9 @@ _SIGS = {
     "trax_prefix_sum_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                           C.c_void_p]),
     "trax_prefix_sum_noalloc_error": (C.c_char_p, []),
+    "trax_prefix_sum_noalloc_status": (C.c_int, [C.c_void_p]),
+    "trax_selftest_lookback_timeout": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
+                                                 C.c_uint32]),
     "trax_reset_counts": (C.c_int, [C.c_void_p]),
     "trax_config_validate": (C.c_int, [C.POINTER(A.TraxConfig), C.POINTER(A.TraxGridCfg)]),
     "trax_layout_validate": (C.c_int, [C.POINTER(A.TraxLayout), C.c_uint32]),
