@@ -2,7 +2,10 @@
 """Benchmark of the GB300 triplet-seeding path; prints one JSON line.
 
 A step is one pass of the whole path (grid build -> pairs -> prediction ->
-filter) over one batch of synthetic events of the named workload.
+filter) over one batch of synthetic events of the named workload.  The
+headline workload is the high-pile-up configuration (Poisson(200) pile-up
+vertices, 256 events per step), where the batched-versus-per-event and HBM
+targets of this path are set.
   value  events/s with the batch already resident in HBM (CUDA-graph replay)
   e2e    events/s through the streaming API (trax_submit_batch /
          trax_wait_batch) with pinned host buffers: every step uploads the hit
@@ -10,23 +13,30 @@ filter) over one batch of synthetic events of the named workload.
          with one step's upload overlapping the previous step's chain (the
          one-at-a-time trax_seed_batch figure is reported beside it)
 Also reported: pairs/s and triplets/s, the plain per-event GPU form (one
-event per launch sequence, no graph), per-kernel times, the dominant
-kernel's HBM roofline, the CPU oracle on all host cores, and SM clocks
-sampled during the timed region.
+event per launch sequence, no graph) and the batched/per-event ratio,
+per-kernel times and HBM fractions, the dominant kernel's roofline, parity of
+the timed batch's tracklets against the CPU oracle, the pile-up-50 batch of
+100 events and the multi-muon batch as further sections, the grid autotuner
+on pile-up-200 events, the streaming server under Poisson load, the CPU
+oracle on all host cores and on one, and SM clocks sampled during the timed
+region.
 
---impl reference times the CPU restatement of the reference's algorithm
-(the reference itself cannot be built here: no OpenCL, clever, Boost or
-protobuf-2.4), on all host threads, on a bounded sample of the same workload.
+--impl reference times the reference's own kernels compiled for the host
+(oracle/_ref: its OpenCL C kernel text built by oracle/ref_build.py, run by a
+work-group emulator over all host cores) when that library can be built,
+else the CPU restatement of its algorithm, on a bounded sample of the same
+workload.
 
-Multi-GPU: replicas only (events are independent); every rank runs its own
-batch, the time is the max over ranks, value = all ranks' events / time.
+Multi-GPU: replicas only (events are independent).  Under torchrun every
+rank runs its own batch; `--gpus N` without torchrun starts N such ranks
+itself.  The time is the max over ranks, value = all ranks' events / time.
 """
 from __future__ import annotations
 
 import argparse
 import json
-import math
 import os
+import socket
 import statistics
 import subprocess
 import sys
@@ -39,27 +49,34 @@ sys.path.insert(0, ROOT)
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
+HEADLINE = "pileup200"
+# (workload, events per launch) measured beside the headline
+SECTIONS = (("pileup50-batch100", 100), ("multimuon-1000trk", 2048))
+# capacities per hit (pairs, candidates, tracklets) of the first sizing run
+SIZING_CAPS = (48, 96, 8)
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="multimuon-1000trk")
-    ap.add_argument("--events", type=int, default=2048, help="events per step (batch)")
-    ap.add_argument("--per-event-sample", type=int, default=64)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--workload", default=HEADLINE)
+    ap.add_argument("--events", type=int, default=256, help="events per step (batch)")
+    ap.add_argument("--per-event-sample", type=int, default=32)
+    ap.add_argument("--parity-events", type=int, default=4,
+                    help="events of the timed batch checked against the CPU oracle")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--serve-rates", default="5000,20000",
+    ap.add_argument("--no-sections", action="store_true")
+    ap.add_argument("--serve-rates", default="1000,5000,20000,50000",
                     help="Poisson arrival rates (events/s) for the streaming measurement")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--serve-pool", type=int, default=128)
-    ap.add_argument("--autotune", action="store_true",
-                    help="grid sweep on pile-up-200 events (config 4), reported under 'autotune'")
-    ap.add_argument("--autotune-events", type=int, default=64)
-    return ap.parse_args()
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--autotune-events", type=int, default=32)
+    return ap.parse_args(argv)
 
 
 # --------------------------------------------------------------------------
@@ -113,6 +130,29 @@ def aggregate_rate(dist: "Dist", events_this_rank: int, steps: int, ms_this_rank
     return events * steps / (ms / 1000.0), ms, events
 
 
+def _free_port() -> int:
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def launch_replicas(n: int, argv) -> int:
+    """`--gpus N` without a launcher: starts N ranks of this script (one per
+    GPU, RANK / LOCAL_RANK / WORLD_SIZE set, gloo rendezvous on 127.0.0.1),
+    forwards rank 0's output and returns the worst exit code."""
+    port = _free_port()
+    procs = []
+    for r in range(n):
+        env = dict(os.environ, RANK=str(r), LOCAL_RANK=str(r), WORLD_SIZE=str(n),
+                   MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, os.path.abspath(__file__)] + list(argv),
+                                      env=env,
+                                      stdout=None if r == 0 else subprocess.DEVNULL))
+    return max(abs(p.wait()) for p in procs)
+
+
 # --------------------------------------------------------------------------
 # clocks sampled during the timed region
 
@@ -125,6 +165,7 @@ class ClockSampler:
     def __init__(self, device: int):
         self.proc = None
         self.device = device
+        self.out = ""
 
     def __enter__(self):
         try:
@@ -174,18 +215,24 @@ class ClockSampler:
 # --------------------------------------------------------------------------
 # algorithmic bytes per kernel (traffic a perfect kernel must move)
 
+def layer_sums(b, w):
+    ln = b.layer_nhits.astype(np.int64)
+    cfg = w.config()
+    T = range(cfg.n_layer_triplets)
+    return tuple(sum(int(ln[:, getattr(cfg.triplets[t], f"layer{k}") - 1].sum()) for t in T)
+                 for k in (1, 2, 3))
+
+
 def algorithmic_bytes(kernel, b, w, counts):
+    """Bytes per launch a kernel must move at least.  grid_build is the
+    reference-equivalent figure: xyz read for the cells, the 7 columns read
+    and written, the grid counted, scanned and written (68 B/hit)."""
     N = b.n_hits
     E, L = b.n_events, b.n_layers
     C = (w.n_sectors_z + 1) * (w.n_sectors_phi + 1)
     M, K, R = counts["n_pairs"], counts["n_candidates"], counts["n_tracklets"]
-    ln = b.layer_nhits.astype(np.int64)
-    cfg = w.config()
-    n1 = sum(int(ln[:, cfg.triplets[t].layer1 - 1].sum()) for t in range(cfg.n_layer_triplets))
-    n2 = sum(int(ln[:, cfg.triplets[t].layer2 - 1].sum()) for t in range(cfg.n_layer_triplets))
-    n3 = sum(int(ln[:, cfg.triplets[t].layer3 - 1].sum()) for t in range(cfg.n_layer_triplets))
+    n1, n2, n3 = layer_sums(b, w)
     table = {
-        # x, y, z read for the cells, 7 columns read and written, the grid
         "grid_build": N * (12 + 28 + 28) + E * L * C * 4 * 3,
         # both layers' hits once, the per-outer-hit counts, the pairs
         "pair_gen": 12 * (n1 + n2) + 4 * n2 * 2 + 8 * M,
@@ -200,6 +247,15 @@ def algorithmic_bytes(kernel, b, w, counts):
     return table.get(kernel)
 
 
+def grid_build_actual_bytes(b, w):
+    """What the batched chain's grid build itself must move: x, y, z read
+    once; layer, event, input position, packed (z, phi), half z and
+    (x, y, z, phi) written (38 B); the grid row per segment written."""
+    E, L = b.n_events, b.n_layers
+    C = (w.n_sectors_z + 1) * (w.n_sectors_phi + 1)
+    return b.n_hits * (12 + 38) + E * L * C * 4
+
+
 def hbm_peak():
     try:
         with open(PEAKS_FILE) as f:
@@ -208,36 +264,49 @@ def hbm_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def issue_from_profiles(kernel, workload):
-    """smsp__issue_active of `kernel` from the committed ncu summary."""
+def profile_entry(workload, key):
+    """An entry of the committed ncu summary (profiles/ncu_traffic.json)."""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
         with open(p) as f:
-            return json.load(f)[workload]["_sm_issue_active"][kernel]
-    except (OSError, KeyError, ValueError):
-        return None
-
-
-def traffic_from_profiles(kernel, workload):
-    """Per-launch DRAM bytes for `kernel` from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
-    try:
-        with open(p) as f:
-            t = json.load(f)
-        e = t[workload][kernel]
-        return e
-    except (OSError, KeyError, ValueError):
+            return json.load(f)[workload][key]
+    except (OSError, KeyError, ValueError, TypeError):
         return None
 
 
 # --------------------------------------------------------------------------
-# CPU restatement (oracle) timing
+# CPU oracle: timing and parity
+
+def oracle_tracklets(batch, w, threads):
+    """The oracle's tracklets as input positions, and its offsets."""
+    import oracle
+    r = oracle.run(batch, w.config(), w.grid(batch.n_events), 4, 256, threads)
+    so = r["sorted_orig"]
+    trk = np.stack([so[r["trk_h1"]], so[r["trk_h2"]], so[r["trk_h3"]]], axis=1) \
+        if r["trk_h1"].size else np.zeros((0, 3), np.uint32)
+    return trk, r["trk_offsets"], r["stats"]
+
+
+def parity_check(b, w, got_trk, got_off, n_events, threads):
+    """Compares the GPU's tracklets (input positions) of the first n_events
+    of batch b with the oracle run on those events alone."""
+    n = min(n_events, b.n_events)
+    sample = b.slice_events(0, n)
+    want, want_off, _ = oracle_tracklets(sample, w, threads)
+    T = w.n_triplets
+    k = int(got_off[n * T])
+    ok = (np.array_equal(np.asarray(got_trk)[:k], want)
+          and np.array_equal(np.asarray(got_off)[: n * T + 1], want_off))
+    return {"parity": "bit-exact" if ok else "MISMATCH", "events_checked": n,
+            "tracklets_checked": int(k), "against": "CPU oracle (pinned to the reference kernels)"}
+
 
 def cpu_events_per_s(b, w, seconds, threads):
+    """The oracle on a bounded sample of b (about `seconds` of CPU work)."""
     import oracle
     cfg = w.config()
     t0 = time.perf_counter()
-    probe = b.slice_events(0, min(4, b.n_events))
+    probe = b.slice_events(0, min(2, b.n_events))
     oracle.run(probe, cfg, w.grid(probe.n_events), 4, 256, threads)
     dt = max(time.perf_counter() - t0, 1e-3)
     n = int(max(1, min(b.n_events, probe.n_events * seconds / dt)))
@@ -248,33 +317,54 @@ def cpu_events_per_s(b, w, seconds, threads):
     return n / dt, n, dt, r["stats"]
 
 
+# --------------------------------------------------------------------------
+# reference arm
+
+def reference_runner(threads):
+    """The reference's own kernels on the host when oracle/_ref builds here,
+    else the CPU restatement of its algorithm."""
+    from oracle import ref
+    try:
+        if ref.available():
+            ref.lib()
+            return "reference", lambda s, w: ref.run(s, w.config(), w.grid(s.n_events), 4,
+                                                     n_threads=256, grid_threads=1,
+                                                     workers=threads)["stats"]
+    except (OSError, FileNotFoundError, subprocess.CalledProcessError):
+        pass
+    import oracle
+    return "port", lambda s, w: oracle.run(s, w.config(), w.grid(s.n_events), 4, 256,
+                                           threads)["stats"]
+
+
 def run_reference(args, dist):
     from trax_gb300 import gen
     w = gen.WORKLOADS[args.workload]
     if dist.rank != 0:
         return
     threads = os.cpu_count() or 1
+    kind, runner = reference_runner(threads)
     b = gen.generate_batch(w, args.events)
     per_step_s = max(2.0, 150.0 / max(1, args.steps + args.warmup))
-    import oracle
-    cfg = w.config()
     t0 = time.perf_counter()
-    probe = b.slice_events(0, min(4, b.n_events))
-    oracle.run(probe, cfg, w.grid(probe.n_events), 4, 256, threads)
+    probe = b.slice_events(0, min(2, b.n_events))
+    runner(probe, w)
     dt = max(time.perf_counter() - t0, 1e-3)
     n = int(max(1, min(b.n_events, probe.n_events * per_step_s / dt)))
     sample = b.slice_events(0, n)
     for _ in range(args.warmup):
-        oracle.run(sample, cfg, w.grid(n), 4, 256, threads)
+        runner(sample, w)
     times = []
     stats = None
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        r = oracle.run(sample, cfg, w.grid(n), 4, 256, threads)
+        stats = runner(sample, w)
         times.append(time.perf_counter() - t0)
-        stats = r["stats"]
     total = sum(times)
     value = n * args.steps / total
+    what = ("the reference's OpenCL kernels compiled for the host (oracle/_ref), "
+            f"work-groups spread over {threads} threads" if kind == "reference" else
+            f"CPU restatement of the reference's algorithm, OpenMP over {threads} threads")
     line = {
         "impl": "reference", "metric": "events/s", "value": round(value, 3), "unit": "events/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -284,45 +374,83 @@ def run_reference(args, dist):
                    "grid": f"{w.n_sectors_z}x{w.n_sectors_phi}", "layer_triplets": w.n_triplets,
                    "sample": f"first {n} of the {args.events}-event batch per step"},
         "cpu_baseline": {"value": round(value, 3), "unit": "events/s", "cores": threads,
-                         "kind": "port",
-                         "sample": f"{n} events per step, OpenMP over {threads} threads"},
+                         "kind": kind, "sample": f"{n} events per step, {what}"},
         "e2e": {"value": round(value, 3), "unit": "events/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "triplets_per_s": round(stats["tracklets"] * args.steps / total, 1),
         "pairs_per_s": round(stats["pairs"] * args.steps / total, 1),
-        "note": "reference OpenCL path unbuildable here; CPU restatement of its algorithm",
+        "note": ("reference host side (clever, Boost, protobuf 2.4, OpenCL runtime) unbuildable "
+                 "here; " + what),
     }
     print(json.dumps(line), flush=True)
 
 
 # --------------------------------------------------------------------------
+# GPU arm
 
-def run_autotune(args, ctx):
-    """Config 4: pile-up-200 events, grid sweep {8..64} x {16..128} with the
-    walk tuned per grid; per-kernel HBM fractions at the best grid and the
-    plain per-event form at that grid."""
-    import ctypes as C
-    from trax_gb300 import gen
-    from trax_gb300.autotune import sweep_grids, tune_walk, density_class
+def sized_pipeline(ctx, w, b, caps_per_hit=SIZING_CAPS):
+    """A Pipeline whose capacities fit b: a first run at generous per-hit
+    capacities (doubled while an output overflows), then one sized from the
+    counts it reported."""
     from trax_gb300.ops import Pipeline
-    w = gen.WORKLOADS["pileup200"]
-    b = gen.generate_batch(w, args.autotune_events)
-    from trax_gb300.autotune import GRID_Z, GRID_PHI
-    grids = [(z, ph) for z in GRID_Z for ph in GRID_PHI] + [(12, 32)]
-    rows = sweep_grids(ctx, w, b, grids=grids, reps=3)
-    best = rows[0]
-    wk = gen.Workload(w.name, w.config_id, w.n_layers, w.noise, w.pt_range,
-                      best["n_sectors_z"], best["n_sectors_phi"], w.n_triplets,
-                      pileup_mean=w.pileup_mean)
+    from trax_gb300.runtime import TraxError
     N = b.n_hits
-    p = Pipeline(ctx, wk.config(), wk.grid(b.n_events), b.n_events, N, 80 * N, 80 * N, 8 * N)
+    caps = [c * N + 4096 for c in caps_per_hit]
+    counts = None
+    for _ in range(4):
+        p = Pipeline(ctx, w.config(), w.grid(b.n_events), b.n_events, N, *caps)
+        try:
+            _, _, counts = p.seed(b)
+        except TraxError as exc:
+            if exc.status != 5:
+                raise
+            counts = ctx.counts()
+        if counts["status"] == 0:
+            break
+        caps = [2 * c for c in caps]
+        del p
+    if counts is None or counts["status"] != 0:
+        raise SystemExit(f"device status {counts}")
+    need = (counts["n_pairs"], counts["n_candidates"], counts["n_tracklets"])
+    caps = [int(1.1 * v) + 4096 for v in need]
+    del p
+    p = Pipeline(ctx, w.config(), w.grid(b.n_events), b.n_events, N, *caps)
     _, _, counts = p.seed(b)
-    ctx.set_tuning(*best["walk"])
-    p.stage(b)
+    if counts["status"] != 0:
+        raise SystemExit(f"device status {counts}")
+    return p, counts
+
+
+def per_event_form(ctx, w, b, sample):
+    """The plain per-event GPU form: one event per launch sequence, no
+    graph, a host synchronisation per event."""
+    S = min(sample, b.n_events)
+    singles = [b.slice_events(e, 1) for e in range(S)]
+    from trax_gb300.ops import Pipeline
+    N1 = max(s.n_hits for s in singles) + 1
+    pe = Pipeline(ctx, w.config(), w.grid(1), 1, N1,
+                  *[c * N1 + 4096 for c in SIZING_CAPS])
+    for s in singles[:2]:
+        pe.stage(s)
+        ctx._check(ctx.lib.trax_run_staged_eager(ctx.h))
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for s in singles:
+        pe.stage(s)
+        ctx._check(ctx.lib.trax_run_staged_eager(ctx.h))
+        ctx.synchronize()
+    rate = S / (time.perf_counter() - t0)
+    del pe
+    return {"value": round(rate, 2), "unit": "events/s",
+            "sample": f"{S} events, one launch sequence each, no graph"}
+
+
+def kernel_times(ctx, p, reps=20):
+    import ctypes as C
     ctx._check(ctx.lib.trax_set_profiling(ctx.h, 1))
-    p.run_staged()
+    p.run_staged()  # captures the profiled graph
     kt = {}
-    for _ in range(5):
+    for _ in range(reps):
         p.run_staged()
         ms = (C.c_float * 64)()
         names = (C.c_char_p * 64)()
@@ -331,38 +459,84 @@ def run_autotune(args, ctx):
         for i in range(n.value):
             kt.setdefault(names[i].decode(), []).append(ms[i])
     ctx._check(ctx.lib.trax_set_profiling(ctx.h, 0))
-    peak, _ = hbm_peak()
-    kernels = {}
-    for k, v in kt.items():
-        m = statistics.median(v)
-        alg = algorithmic_bytes(k, b, wk, counts)
-        kernels[k] = {"ms": round(m, 4)}
-        if alg and m > 0:
-            kernels[k]["hbm_frac"] = round(alg / (m / 1000) / 1e9 / peak, 5)
-    # plain per-event form at the best grid
-    S = min(16, b.n_events)
-    singles = [b.slice_events(e, 1) for e in range(S)]
-    pe = Pipeline(ctx, wk.config(), wk.grid(1), 1, max(x.n_hits for x in singles) + 1,
-                  80 * N // b.n_events * 4, 80 * N // b.n_events * 4, 8 * N // b.n_events * 4)
-    ctx.set_tuning(*best["walk"])
-    for x in singles[:2]:
-        pe.stage(x)
-        ctx._check(ctx.lib.trax_run_staged_eager(ctx.h))
+    return {k: statistics.median(v) for k, v in kt.items()}
+
+
+def resident_rate(ctx, p, b, steps, warmup, dist, clocks=None):
+    """events/s of graph replays on the staged batch, CUDA events on the
+    context stream, K steps between barriers."""
+    p.stage(b)
+    for _ in range(warmup):
+        p.run_staged()
+    ctx.synchronize()
+    dist.barrier()
+    if clocks is not None:
+        clocks.__enter__()
+    ctx.synchronize()
+    ctx.timer_record(62)
+    for _ in range(steps):
+        p.run_staged()
+    ctx.timer_record(63)
+    ctx.synchronize()
+    if clocks is not None:
+        clocks.__exit__()
+    dist.barrier()
+    return aggregate_rate(dist, b.n_events, steps, ctx.timer_elapsed_ms(62, 63))
+
+
+def measure_section(ctx, w, B, args, dist, threads):
+    """A further workload: resident value, one-at-a-time e2e, the per-event
+    form, and parity of its tracklets against the oracle."""
+    from trax_gb300 import gen
+    b = gen.generate_batch(w, B, first_event=replica_first_event(dist.rank, B))
+    p, counts = sized_pipeline(ctx, w, b)
+    from trax_gb300.autotune import tune_walk
+    best_walk, _ = tune_walk(ctx, p, b, reps=3)
+    steps = max(3, args.steps // 2)
+    value, ms_total, events_all = resident_rate(ctx, p, b, steps, args.warmup, dist)
+    trk, off, _ = p.seed(b, input_indices=True)
     ctx.synchronize()
     t0 = time.perf_counter()
-    for x in singles:
-        pe.stage(x)
-        ctx._check(ctx.lib.trax_run_staged_eager(ctx.h))
-        ctx.synchronize()
-    per_event = S / (time.perf_counter() - t0)
-    ctx.set_tuning(48, 16)
+    for _ in range(steps):
+        trk, off, _ = p.seed(b, input_indices=True)
+    sync_s = dist.max(time.perf_counter() - t0)
+    par = parity_check(b, w, trk, off, B if B <= 128 else args.parity_events, threads)
+    del p
+    pe = per_event_form(ctx, w, b, args.per_event_sample)
+    return {"workload": w.name, "events_per_step": B, "hits_per_step": b.n_hits,
+            "grid": f"{w.n_sectors_z}x{w.n_sectors_phi}", "value": round(value, 2),
+            "unit": "events/s", "ms_per_step": round(ms_total / steps, 4),
+            "e2e_sync": {"value": round(events_all * steps / sync_s, 2),
+                         "form": "trax_seed_batch, one batch at a time (pinned H2D + D2H)"},
+            "triplets_per_s": round(counts["n_tracklets"] * dist.world * steps /
+                                    (ms_total / 1000), 1),
+            "per_event_form": pe,
+            "batched_over_per_event": round(value / dist.world / pe["value"], 2),
+            "walk": list(best_walk), **par}
+
+
+def run_autotune(args, ctx):
+    """Config 4: pile-up-200 events, grid sweep {8..64} x {16..128} with the
+    walk tuned per grid, the plain per-event form at the best grid."""
+    from trax_gb300 import gen
+    from trax_gb300.autotune import sweep_grids, density_class, GRID_Z, GRID_PHI
+    w = gen.WORKLOADS["pileup200"]
+    b = gen.generate_batch(w, args.autotune_events)
+    grids = [(z, ph) for z in GRID_Z for ph in GRID_PHI] + [(12, 32)]
+    t0 = time.perf_counter()
+    rows = sweep_grids(ctx, w, b, grids=grids, reps=3)
+    best = rows[0]
+    wk = gen.Workload(w.name, w.config_id, w.n_layers, w.noise, w.pt_range,
+                      best["n_sectors_z"], best["n_sectors_phi"], w.n_triplets,
+                      pileup_mean=w.pileup_mean)
+    pe = per_event_form(ctx, wk, b, 16)
     return {"workload": w.name, "events": b.n_events,
-            "hits_per_event": round(N / b.n_events, 1),
-            "class": density_class(N / b.n_events), "best": best,
+            "hits_per_event": round(b.n_hits / b.n_events, 1),
+            "class": density_class(b.n_hits / b.n_events), "best": best,
             "default_12x32": next((r for r in rows if r.get("grid") == "12x32"), None),
-            "kernels_at_best": kernels,
-            "per_event_form_events_per_s": round(per_event, 1),
-            "batched_over_per_event": round(best["events_per_s"] / per_event, 2),
+            "per_event_form_at_best": pe,
+            "batched_over_per_event_at_best": round(best["events_per_s"] / pe["value"], 2),
+            "sweep_s": round(time.perf_counter() - t0, 1),
             "sweep": [{k: r[k] for k in ("grid", "events_per_s", "walk") if k in r}
                       for r in rows]}
 
@@ -406,106 +580,78 @@ def run_serving(args):
 
 def run_ours(args, dist):
     from trax_gb300 import Context, gen
-    from trax_gb300.ops import Pipeline
     from trax_gb300.runtime import PinnedBuffer
-    import ctypes as C
+    from trax_gb300.autotune import tune_walk
 
+    threads = os.cpu_count() or 1
     w = gen.WORKLOADS[args.workload]
     ctx = Context(dist.local)
     B = args.events
     b = gen.generate_batch(w, B, first_event=replica_first_event(dist.rank, B))
-    cfg, grid = w.config(), w.grid(B)
     N = b.n_hits
-    caps = [12 * N + 4096, 12 * N + 4096, 2 * N + 4096]
-    from trax_gb300.runtime import TraxError
-    for _ in range(3):
-        p = Pipeline(ctx, cfg, grid, B, N, *caps)
-        try:
-            _, _, counts = p.seed(b)
-        except TraxError as exc:  # an output overflowed: counts hold the sizes needed
-            if exc.status != 5:
-                raise
-            counts = ctx.counts()
-        if counts["status"] != 5:
-            break
-        caps = [max(c, 2 * int(v)) for c, v in zip(
-            caps, (counts["n_pairs"], counts["n_candidates"], counts["n_tracklets"]))]
-    if counts["status"] != 0:
-        raise SystemExit(f"device status {counts}")
+    p, counts = sized_pipeline(ctx, w, b)
 
     # ---- result-neutral walk tuning on the resident batch ------------------
-    from trax_gb300.autotune import tune_walk
     best_walk, walk_ms = tune_walk(ctx, p, b, reps=3)
     tuning = {"run_walk": best_walk[0], "index_min": best_walk[1], "pair_record": best_walk[2],
               "candidates_ms": {"/".join(map(str, k)): round(v, 4) for k, v in walk_ms.items()}}
 
     # ---- device-resident value: graph replay on staged inputs -------------
-    p.stage(b)
-    for _ in range(args.warmup):
-        p.run_staged()
-    ctx.synchronize()
-    dist.barrier()
-    with ClockSampler(dist.local) as clk:
-        ctx.synchronize()
-        ctx.timer_record(62)
-        for _ in range(args.steps):
-            p.run_staged()
-        ctx.timer_record(63)
-        ctx.synchronize()
-    dist.barrier()
-    value, ms_total, events_all = aggregate_rate(dist, B, args.steps,
-                                                 ctx.timer_elapsed_ms(62, 63))
+    clk = ClockSampler(dist.local)
+    value, ms_total, events_all = resident_rate(ctx, p, b, args.steps, args.warmup, dist, clk)
     launches = int(ctx.lib.trax_kernel_launches(ctx.h))
     counts = ctx.counts()
     if counts["status"] != 0:
         raise SystemExit(f"device status after timed run {counts}")
 
-    # ---- per-kernel times (separate profiled run) ------------------------
-    ctx._check(ctx.lib.trax_set_profiling(ctx.h, 1))
-    p.run_staged()  # captures the profiled graph
-    kt = {}
-    reps = 20
-    for _ in range(reps):
-        p.run_staged()
-        ms = (C.c_float * 64)()
-        names = (C.c_char_p * 64)()
-        n = C.c_int()
-        ctx._check(ctx.lib.trax_kernel_times(ctx.h, ms, names, 64, C.byref(n)))
-        for i in range(n.value):
-            kt.setdefault(names[i].decode(), []).append(ms[i])
-    ctx._check(ctx.lib.trax_set_profiling(ctx.h, 0))
-    kernel_ms = {k: statistics.median(v) for k, v in kt.items()}
+    # ---- per-kernel times (separate profiled run) and roofline ------------
+    kernel_ms = kernel_times(ctx, p)
     top = max(kernel_ms, key=kernel_ms.get)
     peak, peak_src = hbm_peak()
+    kernels = {}
+    for k, v in kernel_ms.items():
+        alg = algorithmic_bytes(k, b, w, counts)
+        e = {"ms": round(v, 4)}
+        if alg and v > 0:
+            e["gbs"] = round(alg / (v / 1000) / 1e9, 1)
+            e["hbm_frac"] = round(alg / (v / 1000) / 1e9 / peak, 4)
+        kernels[k] = e
+    if "grid_build" in kernel_ms:
+        act = grid_build_actual_bytes(b, w)
+        g = kernels["grid_build"]
+        g["reference_equivalent_bytes"] = algorithmic_bytes("grid_build", b, w, counts)
+        g["actual_column_bytes"] = act
+        g["hbm_frac_actual_columns"] = round(act / (kernel_ms["grid_build"] / 1000) / 1e9 / peak, 4)
+    pair_ms = sum(kernel_ms.get(k, 0) for k in ("pair_gen", "pair_scan", "pair_store"))
+    if pair_ms > 0:
+        pb = algorithmic_bytes("pair_gen", b, w, counts)
+        kernels["pair_stage_total"] = {"ms": round(pair_ms, 4),
+                                       "hbm_frac": round(pb / (pair_ms / 1000) / 1e9 / peak, 4)}
     alg = algorithmic_bytes(top, b, w, counts)
     roofline = None
     if alg is not None:
         achieved = alg / (kernel_ms[top] / 1000.0) / 1e9
-        traffic = traffic_from_profiles(top, args.workload)
         roofline = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 2),
                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5),
-                    "traffic": traffic, "algorithmic_bytes": int(alg),
-                    "launch_ms": round(kernel_ms[top], 4), "peak_source": peak_src,
-                    "sm_issue_active": issue_from_profiles(top, args.workload),
+                    "traffic": profile_entry(args.workload, top),
+                    "algorithmic_bytes": int(alg), "launch_ms": round(kernel_ms[top], 4),
+                    "peak_source": peak_src,
+                    "sm_issue_active": (profile_entry(args.workload, "_sm_issue_active") or {}).get(top),
+                    "timing": "median of 20 profiled graph replays, CUDA events between kernels "
+                              "(the events add about 3 % to each kernel)",
                     "note": "not DRAM-bound: the hits of a layer stay in L1/L2; the kernel is "
                             "bound by instruction issue and load latency (sm_issue_active from ncu)"}
-    stage_bytes = {k: algorithmic_bytes(k, b, w, counts) for k in kernel_ms}
-    kernels = {k: {"ms": round(v, 4),
-                   "gbs": (round(stage_bytes[k] / (v / 1000) / 1e9, 1) if stage_bytes[k] and v > 0
-                           else None)} for k, v in kernel_ms.items()}
 
-    # ---- e2e through trax_seed_batch with pinned host buffers ------------
+    # ---- e2e through the streaming API with pinned host buffers -----------
     cols = b.columns()
-    pinned = []
-    pb = []
+    pinned, pb_cols = [], []
     for c in cols:
         buf = PinnedBuffer(ctx, c.nbytes, c.dtype)
         buf.array[:] = c
         pinned.append(buf)
-        pb.append(buf.array)
+        pb_cols.append(buf.array)
     from trax_gb300.gen import EventBatch
-    pinned_batch = EventBatch(*pb, b.layer_nhits)
-    # synchronous form: upload, chain, download, one batch at a time
+    pinned_batch = EventBatch(*pb_cols, b.layer_nhits)
     for _ in range(args.warmup):
         p.seed(pinned_batch, copy=False)
     dist.barrier()
@@ -515,9 +661,7 @@ def run_ours(args, dist):
     for _ in range(args.steps):
         trk, off, c2 = p.seed(pinned_batch, copy=False)
     sync_s = dist.max(time.perf_counter() - t0)
-    # streaming form (trax_submit_batch / trax_wait_batch): two batches in
-    # flight, each step's upload overlapping the previous step's chain; every
-    # step still uploads its inputs and reads back its result
+
     def stream(k):
         tickets = []
         res = None
@@ -546,20 +690,17 @@ def run_ours(args, dist):
     for x in pinned:
         x.free()
 
+    # ---- parity of the timed batch against the oracle ----------------------
+    trk_in, off_in, _ = p.seed(b, input_indices=True)
+    parity = parity_check(b, w, trk_in, off_in, args.parity_events, threads)
+    if parity["parity"] != "bit-exact":
+        print(json.dumps({"error": "GPU tracklets differ from the oracle", **parity}),
+              file=sys.stderr)
+        raise SystemExit(3)
+    del p
+
     # ---- plain per-event GPU form (no graph, one event per sequence) -----
-    S = min(args.per_event_sample, B)
-    singles = [b.slice_events(e, 1) for e in range(S)]
-    pe = Pipeline(ctx, cfg, w.grid(1), 1, max(s.n_hits for s in singles) + 1, *caps)
-    for s in singles[:2]:
-        pe.stage(s)
-        ctx._check(ctx.lib.trax_run_staged_eager(ctx.h))
-    ctx.synchronize()
-    t0 = time.perf_counter()
-    for s in singles:
-        pe.stage(s)
-        ctx._check(ctx.lib.trax_run_staged_eager(ctx.h))
-        ctx.synchronize()
-    per_event = S / (time.perf_counter() - t0)
+    pe = per_event_form(ctx, w, b, args.per_event_sample)
 
     # ---- PrefixSum micro-benchmark: 1 Mi uint32, the reference's own
     # prefix-sum benchmark shape (src/trax_test/trax_test.cpp:436-479)
@@ -578,9 +719,21 @@ def run_ours(args, dist):
                   "gbs": round(8 * n_scan / (scan_ms / 1000) / 1e9, 1),
                   "note": "in place, 4 B read + 4 B written per element"}
 
-    # ---- autotuned sweep (config 4), optional ------------------------------
+    # ---- further workloads (configs 3 and 2) -------------------------------
+    sections = {}
+    if not args.no_sections:
+        for name, ev in SECTIONS:
+            if name == args.workload:
+                continue
+            sections[name] = measure_section(ctx, gen.WORKLOADS[name], ev, args, dist, threads)
+            if sections[name]["parity"] != "bit-exact":
+                print(json.dumps({"error": "GPU tracklets differ from the oracle",
+                                  "section": name}), file=sys.stderr)
+                raise SystemExit(3)
+
+    # ---- autotuned sweep (config 4) --------------------------------------
     autotune = None
-    if args.autotune and dist.world == 1:
+    if not args.no_autotune and dist.world == 1:
         autotune = run_autotune(args, ctx)
 
     # ---- streaming serving load (config 5) --------------------------------
@@ -591,10 +744,12 @@ def run_ours(args, dist):
     # ---- CPU baseline (rank 0, N=1 only) ----------------------------------
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
         v, n, dt, _ = cpu_events_per_s(b, w, args.cpu_seconds, threads)
+        v1, n1, dt1, _ = cpu_events_per_s(b, w, max(2.0, args.cpu_seconds / 2), 1)
         cpu = {"value": round(v, 3), "unit": "events/s", "cores": threads, "kind": "port",
-               "sample": f"first {n} events of the batch, {dt:.1f} s, OpenMP oracle"}
+               "sample": f"first {n} events of the batch, {dt:.1f} s, OpenMP oracle",
+               "one_thread": {"value": round(v1, 3), "cores": 1,
+                              "sample": f"first {n1} events, {dt1:.1f} s"}}
 
     clocks = clk.summary()
     if dist.rank == 0:
@@ -605,6 +760,7 @@ def run_ours(args, dist):
             "ms_per_step": round(ms_total / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": args.workload, "events_per_step": B, "hits_per_step": N,
+                       "hits_per_event": round(N / B, 1),
                        "layers": w.n_layers, "layer_triplets": w.n_triplets,
                        "grid": f"{w.n_sectors_z}x{w.n_sectors_phi}",
                        "form": "batched: one CUDA graph per step",
@@ -613,13 +769,14 @@ def run_ours(args, dist):
             "e2e": e2e,
             "pairs_per_s": round(counts["n_pairs"] * dist.world * args.steps / (ms_total / 1000), 1),
             "triplets_per_s": round(counts["n_tracklets"] * dist.world * args.steps / (ms_total / 1000), 1),
-            "per_event_form": {"value": round(per_event, 2), "unit": "events/s",
-                               "sample": f"{S} events, one launch sequence each, no graph"},
-            "batched_over_per_event": round(value / dist.world / per_event, 2),
+            "per_event_form": pe,
+            "batched_over_per_event": round(value / dist.world / pe["value"], 2),
+            "parity": parity["parity"], "parity_detail": parity,
             "roofline": roofline,
             "kernels": kernels,
             "cpu_baseline": cpu,
             "prefix_sum_1mi": prefix_sum,
+            "sections": sections,
             "serving": serving,
             "tuning": tuning,
             "autotune": autotune,
@@ -633,8 +790,15 @@ def run_ours(args, dist):
     ctx.close()
 
 
-def main():
-    args = parse()
+def main(argv=None):
+    argv = sys.argv[1:] if argv is None else argv
+    args = parse(argv)
+    if "WORLD_SIZE" not in os.environ and args.gpus > 1:
+        return launch_replicas(args.gpus, argv)
+    if "WORLD_SIZE" in os.environ and int(os.environ["WORLD_SIZE"]) != args.gpus:
+        print(f"--gpus {args.gpus} disagrees with WORLD_SIZE={os.environ['WORLD_SIZE']}",
+              file=sys.stderr)
+        return 2
     dist = Dist()
     try:
         if args.impl == "reference":
@@ -643,7 +807,8 @@ def main():
             run_ours(args, dist)
     finally:
         dist.close()
+    return 0
 
 
 if __name__ == "__main__":
-    main()
+    sys.exit(main())

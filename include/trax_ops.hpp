@@ -56,9 +56,20 @@ public:
         check(h_, trax_read_counts(h_, &c), "trax_read_counts");
         return c;
     }
+    /* The configuration an operator last installed on this context (its
+     * GeometrySupplement serves operators whose reference signature takes
+     * none), or null before the first one. */
+    const trax_config *config() const { return has_config_ ? &config_ : nullptr; }
+    void remember(const trax_config &c)
+    {
+        config_ = c;
+        has_config_ = true;
+    }
 
 private:
     trax_ctx *h_ = nullptr;
+    trax_config config_{};
+    bool has_config_ = false;
 };
 
 /* A device array owned through the context. */
@@ -293,6 +304,21 @@ inline void configure(Context &ctx, const TripletConfigurations &lt, const Geome
 {
     trax_config c = lt.config(geom);
     check(ctx.get(), trax_configure(ctx.get(), &c), "trax_configure");
+    ctx.remember(c);
+}
+
+/* The layer triplets of `lt` with the geometry the context was last
+ * configured with. */
+inline void configure_cuts(Context &ctx, const TripletConfigurations &lt, const char *who)
+{
+    const trax_config *prev = ctx.config();
+    if (!prev)
+        throw Error(TRAX_ERR_BAD_ARG, std::string(who) +
+                                          ": no GeometrySupplement configured on this context yet");
+    GeometrySupplement geom;
+    geom.minRadius.assign(prev->min_radius, prev->min_radius + prev->n_geom_layers);
+    geom.maxRadius.assign(prev->max_radius, prev->max_radius + prev->n_geom_layers);
+    configure(ctx, lt, geom);
 }
 }  // namespace detail
 
@@ -383,12 +409,31 @@ public:
 class TripletThetaPhiFilter : public KernelWrapper {
 public:
     using KernelWrapper::KernelWrapper;
+    /* The reference's signature (TripletThetaPhiFilter.h:46-48): the cuts
+     * come from `lt`, the layer radii from the GeometrySupplement the
+     * context was configured with by the pair generator or predictor. */
+    TrackletCollection *run(HitCollection &hits, const Grid &grid, const Pairing &pairs,
+                            const Pairing &tripletCandidates, int nThreads,
+                            const TripletConfigurations &lt)
+    {
+        detail::configure_cuts(ctx_, lt, "TripletThetaPhiFilter::run");
+        return filter(hits, grid, pairs, tripletCandidates, nThreads, lt);
+    }
+    /* The same with the geometry given explicitly. */
     TrackletCollection *run(HitCollection &hits, const Grid &grid, const Pairing &pairs,
                             const Pairing &tripletCandidates, int nThreads,
                             const TripletConfigurations &lt, const GeometrySupplement &geom)
     {
-        (void)nThreads;
         detail::configure(ctx_, lt, geom);
+        return filter(hits, grid, pairs, tripletCandidates, nThreads, lt);
+    }
+
+private:
+    TrackletCollection *filter(HitCollection &hits, const Grid &grid, const Pairing &pairs,
+                               const Pairing &tripletCandidates, int nThreads,
+                               const TripletConfigurations &lt)
+    {
+        (void)nThreads;
         trax_sorted_hits h = hits.sorted();
         trax_grid_cfg g = grid.config.c();
         uint32_t cap = tripletCandidates.count + 1024u;

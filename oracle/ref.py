@@ -4,8 +4,9 @@ reference's host chain (restated in oracle/ref_host.cpp).
 
 TEST INFRASTRUCTURE ONLY.  It pins the CPU restatement (trax_oracle.c) to
 the reference: tests run both on the same inputs and compare every stage's
-output.  It needs the reference tree to build; where the tree is absent and
-no library was built before, `available()` is False.
+output; bench.py's reference arm times it.  It builds from the reference
+tree, or from an extraction of the kernels made earlier (which travels with
+the working tree); with neither, `available()` is False.
 """
 from __future__ import annotations
 
@@ -36,20 +37,21 @@ def reference_present() -> bool:
 
 
 def available() -> bool:
-    return os.path.exists(ref_build.LIB_PATH) or reference_present()
+    """The library can be loaded: the reference tree or an earlier
+    extraction of its kernels is here to build it from."""
+    return reference_present() or os.path.exists(ref_build.INC_PATH)
 
 
 def lib():
     global _lib
     with _lock:
         if _lib is None:
-            if reference_present():
-                ref_build.build()
+            ref_build.build()
             L = C.CDLL(ref_build.LIB_PATH)
             L.ref_run.restype = C.c_void_p
             L.ref_run.argtypes = [C.POINTER(TraxConfig), C.POINTER(TraxGridCfg)] + \
                 [C.c_void_p] * 7 + [C.c_uint32] + [C.c_void_p] * 3 + \
-                [C.c_int, C.c_uint32, C.c_uint32, C.c_int, C.c_int]
+                [C.c_int, C.c_uint32, C.c_uint32, C.c_int, C.c_int, C.c_int]
             L.ref_size.restype = C.c_uint64
             L.ref_size.argtypes = [C.c_void_p, C.c_int]
             L.ref_data.restype = C.c_void_p
@@ -64,12 +66,14 @@ def _ptr(a):
 
 
 def run(batch, cfg: TraxConfig, grid: TraxGridCfg, n_stages=4, n_threads=256, grid_threads=1,
-        pair_gen="beamspot", variant=0):
+        pair_gen="beamspot", variant=0, workers=1):
     """Runs the reference's kernels on an EventBatch; returns a dict shaped
     like oracle.run's (no sorted_phi / sorted_orig: the reference keeps
     neither; stats["cand_truncated"] is not measured).  grid_threads is the
     grid stage's work-group size: 1 fixes gridStore's racy within-cell order
-    to the input order, the order the restatement and the CUDA kernels use."""
+    to the input order, the order the restatement and the CUDA kernels use.
+    workers > 1 runs work-groups on that many threads (timing only: racy
+    kernels then give no fixed result)."""
     L = lib()
     cols = [np.ascontiguousarray(c) for c in batch.columns()]
     eo = np.ascontiguousarray(batch.event_offset, dtype=np.uint32)
@@ -77,7 +81,7 @@ def run(batch, cfg: TraxConfig, grid: TraxGridCfg, n_stages=4, n_threads=256, gr
     lo = np.ascontiguousarray(batch.layer_offset.reshape(-1), dtype=np.uint32)
     h = L.ref_run(C.byref(cfg), C.byref(grid), *[_ptr(c) for c in cols], batch.n_hits,
                   _ptr(eo), _ptr(ln), _ptr(lo), n_stages, n_threads, grid_threads,
-                  PAIR_GENERATORS[pair_gen], variant)
+                  PAIR_GENERATORS[pair_gen], variant, workers)
     out = {}
     try:
         for i, name in enumerate(ITEMS):

@@ -127,16 +127,24 @@ def generate(reference: str) -> str:
     return "".join(parts)
 
 
+INC_PATH = os.path.join(OUT_DIR, "ref_kernels.inc")
+
+
 def build(reference: str = DEFAULT_REFERENCE, verbose: bool = False) -> str:
-    if not os.path.isdir(os.path.join(reference, "src", "algorithms")):
-        raise FileNotFoundError(f"reference tree not found at {reference}")
-    os.makedirs(OUT_DIR, exist_ok=True)
-    inc = os.path.join(OUT_DIR, "ref_kernels.inc")
-    text = generate(reference)
-    old = open(inc).read() if os.path.exists(inc) else None
-    if old != text:
-        with open(inc, "w") as f:
-            f.write(text)
+    """Extracts the kernels when the reference tree is present, then compiles.
+    Without the tree an extraction made earlier (oracle/_ref/ref_kernels.inc,
+    which travels with the working tree) is compiled as it is."""
+    inc = INC_PATH
+    if os.path.isdir(os.path.join(reference, "src", "algorithms")):
+        os.makedirs(OUT_DIR, exist_ok=True)
+        text = generate(reference)
+        old = open(inc).read() if os.path.exists(inc) else None
+        if old != text:
+            with open(inc, "w") as f:
+                f.write(text)
+    elif not os.path.exists(inc):
+        raise FileNotFoundError(f"reference tree not found at {reference} and no earlier "
+                                f"extraction in {OUT_DIR}")
     src = os.path.join(HERE, "ref_host.cpp")
     deps = [inc, src, os.path.join(HERE, "ref_cl.h"), os.path.join(HERE, "trax_oracle.h"),
             os.path.join(HERE, "..", "trax_gb300", "csrc", "trax_math.h")]
@@ -144,7 +152,7 @@ def build(reference: str = DEFAULT_REFERENCE, verbose: bool = False) -> str:
                                         for d in deps):
         return LIB_PATH
     cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++20", "-fPIC", "-shared",
-           "-ffp-contract=off", "-fno-fast-math", "-fno-strict-aliasing", "-I", OUT_DIR, "-o", LIB_PATH + ".tmp", src]
+           "-ffp-contract=off", "-fno-fast-math", "-fno-strict-aliasing", "-pthread", "-I", OUT_DIR, "-o", LIB_PATH + ".tmp", src]
     if verbose:
         print(" ".join(cmd))
     subprocess.check_call(cmd)

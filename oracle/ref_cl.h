@@ -23,10 +23,12 @@
  *   - float-to-integer conversions of floor() results: trax_f2u / trax_f2i,
  *     a two's-complement target (floor() returns a value type whose integer
  *     conversions route through them);
- *   - atomics are plain read-modify-writes: work-items of a group run one at
- *     a time, in local-id order, switching only at barrier().
- * Work-groups run one after another in group-id order (x fastest), so every
- * racy ordering in the reference resolves to the sequential one.
+ *   - work-items of a group run one at a time, in local-id order, switching
+ *     only at barrier(); atomics are relaxed read-modify-writes.
+ * With one worker, work-groups run one after another in group-id order (x
+ * fastest), so every racy ordering in the reference resolves to the
+ * sequential one.  With several workers (timing only) work-groups run in
+ * parallel, as on an OpenCL CPU device, and the races are real again.
  */
 #ifndef TRAX_REF_CL_H
 #define TRAX_REF_CL_H
@@ -117,9 +119,15 @@ inline int min(int a, int b) { return b < a ? b : a; }
 inline uint max(uint a, uint b) { return a < b ? b : a; }
 inline uint min(uint a, uint b) { return b < a ? b : a; }
 
-template <class T> inline T atomic_inc(T *p) { T o = *p; *p = o + 1; return o; }
-template <class T, class V> inline T atomic_add(T *p, V v) { T o = *p; *p = o + (T)v; return o; }
-template <class T, class V> inline T atomic_or(T *p, V v) { T o = *p; *p = o | (T)v; return o; }
+template <class T> inline T atomic_inc(T *p) { return __atomic_fetch_add(p, (T)1, __ATOMIC_RELAXED); }
+template <class T, class V> inline T atomic_add(T *p, V v)
+{
+    return __atomic_fetch_add(p, (T)v, __ATOMIC_RELAXED);
+}
+template <class T, class V> inline T atomic_or(T *p, V v)
+{
+    return __atomic_fetch_or(p, (T)v, __ATOMIC_RELAXED);
+}
 template <class T> inline void prefetch(const T *, size_t) {}
 
 /* ---- NDRange and work-group emulation ----------------------------------- */
@@ -133,7 +141,7 @@ struct WorkItem {
 };
 
 extern const NDRange *g_range;
-extern const WorkItem *g_item;
+extern thread_local const WorkItem *g_item;
 
 inline size_t get_global_id(uint d) { return g_item->gid[d]; }
 inline size_t get_local_id(uint d) { return g_item->lid[d]; }

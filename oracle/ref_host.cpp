@@ -37,8 +37,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <functional>
 #include <memory>
+#include <thread>
 #include <vector>
 
 #include <ucontext.h>
@@ -56,10 +58,12 @@
 
 #include "trax_oracle.h"
 
+typedef uint32_t u32_t;
+
 namespace refcl {
 
 const NDRange *g_range = nullptr;
-const WorkItem *g_item = nullptr;
+thread_local const WorkItem *g_item = nullptr;
 
 namespace {
 
@@ -69,19 +73,87 @@ struct Fiber {
     bool done;
 };
 
-constexpr size_t kFiberStack = 128 * 1024;
-ucontext_t g_sched;
-std::vector<Fiber> g_fibers;
-std::vector<std::unique_ptr<char[]>> g_stacks;
-size_t g_cur = 0;
-bool g_fibered = false;
-const std::function<void()> *g_body = nullptr;
+/* Fiber state belongs to the OS thread that runs the work-group: a fiber
+ * never moves between threads. */
+constexpr size_t kFiberStack = 64 * 1024;
+thread_local ucontext_t g_sched;
+thread_local std::vector<Fiber> g_fibers;
+thread_local std::vector<std::unique_ptr<char[]>> g_stacks;
+thread_local size_t g_cur = 0;
+thread_local bool g_fibered = false;
+thread_local const std::function<void()> *g_body = nullptr;
+int g_workers = 1;
 
 void fiber_main()
 {
     (*g_body)();
     g_fibers[g_cur].done = true;
     swapcontext(&g_fibers[g_cur].ctx, &g_sched);
+}
+
+/* One work-group.  A kernel with barriers gets one fiber per work-item; the
+ * fibers take turns in local-id order from one barrier to the next.  Returns
+ * false when the work-items disagree on the number of barriers. */
+bool run_group(const NDRange &r, const size_t grp[3], bool fibered,
+               const std::function<void()> &body)
+{
+    if (!fibered) {
+        WorkItem wi;
+        for (size_t lz = 0; lz < r.local[2]; ++lz)
+            for (size_t ly = 0; ly < r.local[1]; ++ly)
+                for (size_t lx = 0; lx < r.local[0]; ++lx) {
+                    const size_t lid[3] = {lx, ly, lz};
+                    for (int d = 0; d < 3; ++d) {
+                        wi.lid[d] = lid[d];
+                        wi.grp[d] = grp[d];
+                        wi.gid[d] = grp[d] * r.local[d] + lid[d];
+                    }
+                    g_item = &wi;
+                    body();
+                }
+        return true;
+    }
+    const size_t n_local = r.local[0] * r.local[1] * r.local[2];
+    if (g_fibers.size() < n_local) g_fibers.resize(n_local);
+    while (g_stacks.size() < n_local) g_stacks.emplace_back(new char[kFiberStack]);
+    g_fibered = true;
+    g_body = &body;
+    size_t i = 0;
+    for (size_t lz = 0; lz < r.local[2]; ++lz)
+        for (size_t ly = 0; ly < r.local[1]; ++ly)
+            for (size_t lx = 0; lx < r.local[0]; ++lx, ++i) {
+                Fiber &f = g_fibers[i];
+                const size_t lid[3] = {lx, ly, lz};
+                for (int d = 0; d < 3; ++d) {
+                    f.wi.lid[d] = lid[d];
+                    f.wi.grp[d] = grp[d];
+                    f.wi.gid[d] = grp[d] * r.local[d] + lid[d];
+                }
+                f.done = false;
+                getcontext(&f.ctx);
+                f.ctx.uc_stack.ss_sp = g_stacks[i].get();
+                f.ctx.uc_stack.ss_size = kFiberStack;
+                f.ctx.uc_link = nullptr;
+                makecontext(&f.ctx, fiber_main, 0);
+            }
+    bool ok = true;
+    for (;;) {
+        size_t n_done = 0;
+        for (size_t k = 0; k < n_local; ++k) {
+            if (g_fibers[k].done) continue;
+            g_cur = k;
+            g_item = &g_fibers[k].wi;
+            swapcontext(&g_sched, &g_fibers[k].ctx);
+            n_done += g_fibers[k].done;
+        }
+        if (n_done == n_local) break;
+        if (n_done != 0) {
+            ok = false;
+            break;
+        }
+    }
+    g_fibered = false;
+    return ok;
 }
 
 }  // namespace
@@ -92,10 +164,10 @@ void barrier(int)
     swapcontext(&g_fibers[g_cur].ctx, &g_sched);
 }
 
-/* Runs `body` once per work-item of the NDRange, group after group.  A
- * kernel with barriers gets one fiber per work-item of a group; the fibers
- * take turns in local-id order from one barrier to the next.  Returns false
- * when the work-items of a group disagree on the number of barriers. */
+/* Runs `body` once per work-item of the NDRange.  With one worker the groups
+ * run in group-id order on the calling thread; with more, worker threads
+ * take groups from a shared counter.  Returns false when a group's
+ * work-items disagree on the number of barriers. */
 static bool launch(const NDRange &r, bool barriers, const std::function<void()> &body)
 {
     size_t ng[3];
@@ -104,76 +176,40 @@ static bool launch(const NDRange &r, bool barriers, const std::function<void()> 
         ng[d] = r.global[d] / r.local[d];
     }
     g_range = &r;
-    const size_t n_local = r.local[0] * r.local[1] * r.local[2];
-    const bool fibered = barriers && n_local > 1;
-    if (fibered) {
-        g_fibers.resize(n_local);
-        while (g_stacks.size() < n_local) g_stacks.emplace_back(new char[kFiberStack]);
-    }
-    for (size_t gz = 0; gz < ng[2]; ++gz)
-        for (size_t gy = 0; gy < ng[1]; ++gy)
-            for (size_t gx = 0; gx < ng[0]; ++gx) {
-                const size_t grp[3] = {gx, gy, gz};
-                if (!fibered) {
-                    g_fibered = false;
-                    WorkItem wi;
-                    for (size_t lz = 0; lz < r.local[2]; ++lz)
-                        for (size_t ly = 0; ly < r.local[1]; ++ly)
-                            for (size_t lx = 0; lx < r.local[0]; ++lx) {
-                                const size_t lid[3] = {lx, ly, lz};
-                                for (int d = 0; d < 3; ++d) {
-                                    wi.lid[d] = lid[d];
-                                    wi.grp[d] = grp[d];
-                                    wi.gid[d] = grp[d] * r.local[d] + lid[d];
-                                }
-                                g_item = &wi;
-                                body();
-                            }
-                    continue;
-                }
-                g_fibered = true;
-                g_body = &body;
-                size_t i = 0;
-                for (size_t lz = 0; lz < r.local[2]; ++lz)
-                    for (size_t ly = 0; ly < r.local[1]; ++ly)
-                        for (size_t lx = 0; lx < r.local[0]; ++lx, ++i) {
-                            Fiber &f = g_fibers[i];
-                            const size_t lid[3] = {lx, ly, lz};
-                            for (int d = 0; d < 3; ++d) {
-                                f.wi.lid[d] = lid[d];
-                                f.wi.grp[d] = grp[d];
-                                f.wi.gid[d] = grp[d] * r.local[d] + lid[d];
-                            }
-                            f.done = false;
-                            getcontext(&f.ctx);
-                            f.ctx.uc_stack.ss_sp = g_stacks[i].get();
-                            f.ctx.uc_stack.ss_size = kFiberStack;
-                            f.ctx.uc_link = nullptr;
-                            makecontext(&f.ctx, fiber_main, 0);
-                        }
-                for (;;) {
-                    size_t n_done = 0;
-                    for (size_t k = 0; k < n_local; ++k) {
-                        if (g_fibers[k].done) continue;
-                        g_cur = k;
-                        g_item = &g_fibers[k].wi;
-                        swapcontext(&g_sched, &g_fibers[k].ctx);
-                        n_done += g_fibers[k].done;
-                    }
-                    if (n_done == n_local) break;
-                    if (n_done != 0) {
-                        g_fibered = false;
-                        return false;
-                    }
-                }
-                g_fibered = false;
-            }
-    return true;
+    const bool fibered = barriers && r.local[0] * r.local[1] * r.local[2] > 1;
+    const size_t total = ng[0] * ng[1] * ng[2];
+    std::atomic<size_t> next{0};
+    std::atomic<bool> ok{true};
+    auto work = [&] {
+        for (;;) {
+            const size_t g = next.fetch_add(1, std::memory_order_relaxed);
+            if (g >= total) break;
+            const size_t grp[3] = {g % ng[0], (g / ng[0]) % ng[1], g / (ng[0] * ng[1])};
+            if (!run_group(r, grp, fibered, body)) ok = false;
+        }
+    };
+    const size_t workers = std::min<size_t>((size_t)std::max(1, g_workers), total);
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < workers; ++t) pool.emplace_back(work);
+    work();
+    for (auto &t : pool) t.join();
+    return ok;
+}
+
+/* __local memory of a kernel argument: one buffer per slot and OS thread,
+ * shared by the work-items of the group that thread runs. */
+static u32_t *local_buf(int slot, size_t n)
+{
+    thread_local std::vector<u32_t> bufs[2];
+    std::vector<u32_t> &b = bufs[slot];
+    if (b.size() < n) b.resize(n);
+    return b.data();
 }
 
 }  // namespace refcl
 
 using refcl::NDRange;
+using refcl::local_buf;
 using refcl::uint2;
 typedef uint32_t u32;
 
@@ -245,19 +281,19 @@ struct PrefixSum {
         using namespace refcl::PrefixSum;
         const u32 nGroups = groups_f(size, wg << 1);
         const u32 padding = (wg << 1) / MEMORY_BANK_COUNT;
-        std::vector<u32> local((wg << 1) + padding + kPad);
+        const size_t nlocal = (wg << 1) + padding + kPad;
         if (nGroups == 1) { /* :72-86 */
             u32 localSize = (u32)std::max(1.0f, std::ceil(((float)size) / 2));
             localSize = next_pow2(localSize);
             NDRange r = range1(localSize, localSize);
             ok &= refcl::launch(r, prefixSumWG_barriers,
-                                [&] { prefixSumWG(input, size, local.data()); });
+                                [&] { prefixSumWG(input, size, local_buf(0, nlocal)); });
             return;
         }
         u32 *part = partial[level].data(); /* :87-124 */
         NDRange r = range1((size_t)wg * nGroups, wg);
         ok &= refcl::launch(r, prefixSumPartial_barriers,
-                            [&] { prefixSumPartial(input, size, part, local.data()); });
+                            [&] { prefixSumPartial(input, size, part, local_buf(0, nlocal)); });
         scan(part, nGroups, level + 1);
         ok &= refcl::launch(r, prefixSumUniformAdd_barriers,
                             [&] { prefixSumUniformAdd(input, size, part); });
@@ -330,12 +366,12 @@ struct Chain {
         /* gridCount takes its hit columns without const */
         float *xm = const_cast<float *>(x), *ym = const_cast<float *>(y), *zm = const_cast<float *>(z);
         grid.assign((size_t)E * L * C + kPad, 0u);
-        std::vector<u32> lGrid(C + kPad), written(C + kPad);
+        const size_t nlocal = C + kPad;
         NDRange r = range3(nThreads, L, E, nThreads);
         if (count_variant == 0)
             ok &= refcl::launch(r, gridCount_barriers, [&] {
                 gridCount(eventOffsets, layerHits, layerOffsets, L, grid.data(), minZ, szZ, Z,
-                          minPhi, szP, P, xm, ym, zm, lGrid.data());
+                          minPhi, szP, P, xm, ym, zm, local_buf(0, nlocal));
             });
         else
             ok &= refcl::launch(r, gridNoLocalCount_barriers, [&] {
@@ -353,14 +389,14 @@ struct Chain {
                 gridStore(eventOffsets, layerHits, layerOffsets, L, grid.data(), minZ, szZ, Z,
                           minPhi, szP, P, x, y, z, lay, dt, hid, ev, X.data(), Y.data(),
                           Zc.data(), layer.data(), det.data(), hitid.data(), event.data(),
-                          lGrid.data(), written.data());
+                          local_buf(0, nlocal), local_buf(1, nlocal));
             });
         else if (store_variant == 1)
             ok &= refcl::launch(r, gridWrittenLocalStore_barriers, [&] {
                 gridWrittenLocalStore(eventOffsets, layerHits, layerOffsets, L, grid.data(), minZ,
                                       szZ, Z, minPhi, szP, P, x, y, z, lay, dt, hid, ev, X.data(),
                                       Y.data(), Zc.data(), layer.data(), det.data(),
-                                      hitid.data(), event.data(), written.data());
+                                      hitid.data(), event.data(), local_buf(1, nlocal));
             });
         else {
             std::vector<u32> gWritten((size_t)E * L * C + kPad, 0u);
@@ -407,7 +443,7 @@ struct Chain {
         const u32 totalMaxPairs = bitmap_offsets(oracleOffset);
         std::vector<u32> oracle((size_t)std::ceil(totalMaxPairs / 32.0) + kPad, 0u);
         std::vector<u32> prefixSum((size_t)E * T * nThreads + 1 + kPad, 0u);
-        std::vector<u32> lGrid(C + kPad);
+        const size_t nlocal = C + kPad;
         NDRange r = range3(nThreads, T, E, nThreads);
         if (sector) {
             using namespace refcl::PairGeneratorSector;
@@ -415,7 +451,7 @@ struct Chain {
                 pairCount(layer1.data(), layer2.data(), L, grid.data(), minZ, szZ, Z, minPhi,
                           szP, P, pairSpreadZ.data(), pairSpreadPhi.data(), X.data(), Y.data(),
                           Zc.data(), oracle.data(), oracleOffset.data(), prefixSum.data(),
-                          lGrid.data());
+                          local_buf(0, nlocal));
             });
         } else {
             using namespace refcl::PairGeneratorBeamspot;
@@ -428,7 +464,7 @@ struct Chain {
                               grid.data(), minZ, szZ, Z, minPhi, szP, P, z0.data(), sigmaPhiBuf,
                               sigmaZ.data(), tipCut.data(), minRadiusCurvature, X.data(),
                               Y.data(), Zc.data(), oracle.data(), oracleOffset.data(),
-                              prefixSum.data(), lGrid.data());
+                              prefixSum.data(), local_buf(0, nlocal));
                 });
             else
                 ok &= refcl::launch(r, pairNoLocalCount_barriers, [&] {
@@ -560,6 +596,8 @@ extern "C" {
  * (event, layer) makes gridStore's racy within-cell order the input order.
  * variant: bit 0 gridNoLocalCount, bits 1-2 store (0 gridStore,
  * 1 gridWrittenLocalStore, 2 gridNoLocalStore), bit 3 pairNoLocalCount.
+ * workers > 1 spreads the work-groups of every launch over that many threads
+ * (for timing: the reference's races then resolve in no fixed order).
  * Stats: ORS_STATUS 0, or 1 when a work-group's barriers disagreed, or 2 when
  * the pair stage left slots unwritten (the chain stops there), or 3 when a
  * work-group size is not a power of two (PrefixSum's tree walks need one);
@@ -568,8 +606,10 @@ void *ref_run(const trax_config *cfg, const trax_grid_cfg *grid, const float *x,
               const float *z, const uint32_t *layer, const uint32_t *det, const uint32_t *hitid,
               const uint32_t *event, uint32_t n_hits, const uint32_t *event_offset,
               const uint32_t *layer_nhits, const uint32_t *layer_offset, int n_stages,
-              uint32_t n_threads, uint32_t grid_threads, int pair_generator, int variant)
+              uint32_t n_threads, uint32_t grid_threads, int pair_generator, int variant,
+              int workers)
 {
+    refcl::g_workers = workers > 0 ? workers : 1;
     Result *res = new Result();
     res->size[OR_STATS] = OR_NSTATS;
     Chain c;

@@ -97,7 +97,7 @@ int main(int argc, char **argv)
         std::unique_ptr<trax::Pairing> cands(trax::TripletThetaPhiPredictor(ctx).run(
             hits, nullptr, geom, nullptr, 256, lt, grid, *pairs));
         std::unique_ptr<trax::TrackletCollection> trk(
-            trax::TripletThetaPhiFilter(ctx).run(hits, grid, *pairs, *cands, 256, lt, geom));
+            trax::TripletThetaPhiFilter(ctx).run(hits, grid, *pairs, *cands, 256, lt));
 
         std::vector<uint32_t> h1 = trk->hit1.download(trk->size()),
                               h2 = trk->hit2.download(trk->size()),
