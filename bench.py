@@ -248,12 +248,13 @@ def algorithmic_bytes(kernel, b, w, counts):
 
 
 def grid_build_actual_bytes(b, w):
-    """What the batched chain's grid build itself must move: x, y, z read
-    once; layer, event, input position, packed (z, phi), half z and
-    (x, y, z, phi) written (38 B); the grid row per segment written."""
+    """What the batched chain's grid build itself must move: x, y, z, layer
+    and event read once (20 B); layer, event, input position, packed
+    (z, phi), half z and (x, y, z, phi) written (38 B); the grid row per
+    segment written."""
     E, L = b.n_events, b.n_layers
     C = (w.n_sectors_z + 1) * (w.n_sectors_phi + 1)
-    return b.n_hits * (12 + 38) + E * L * C * 4
+    return b.n_hits * (20 + 38) + E * L * C * 4
 
 
 def hbm_peak():
@@ -278,9 +279,11 @@ def profile_entry(workload, key):
 # CPU oracle: timing and parity
 
 def oracle_tracklets(batch, w, threads):
-    """The oracle's tracklets as input positions, and its offsets."""
+    """The oracle's tracklets as input positions, and its offsets.  Work-group
+    size 1 puts its pairs -- and so its candidates and tracklets -- in the
+    order the CUDA path writes them (outer hit, then inner hit)."""
     import oracle
-    r = oracle.run(batch, w.config(), w.grid(batch.n_events), 4, 256, threads)
+    r = oracle.run(batch, w.config(), w.grid(batch.n_events), 4, 1, threads)
     so = r["sorted_orig"]
     trk = np.stack([so[r["trk_h1"]], so[r["trk_h2"]], so[r["trk_h3"]]], axis=1) \
         if r["trk_h1"].size else np.zeros((0, 3), np.uint32)

@@ -1,0 +1,109 @@
+"""GPU parity at benchmark scale: the batched chain's tracklets and offsets
+against the CPU oracle (pinned to the reference kernels) on the workloads
+the benchmark times -- 100 pile-up-50 events in one launch, 16 and 64
+pile-up-200 events, the grids the autotuner picks for pile-up 200 -- and the
+serving stream's results against the oracle.  Bit-exact: integer index
+sets, equality is the tolerance."""
+import numpy as np
+import pytest
+
+import oracle
+from trax_gb300 import gen
+from trax_gb300.ops import Pipeline
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_trk(b, w, grid=None, threads=16):
+    g = grid if grid is not None else w.grid(b.n_events)
+    r = oracle.run(b, w.config(), g, 4, n_threads=1, omp_threads=threads)
+    assert r["stats"]["status"] == 0
+    return oracle.canonical(r)["tracklets"], r["trk_offsets"], r["stats"]
+
+
+def pipeline_for(ctx, w, b, grid=None, per_hit=(48, 96, 8)):
+    N = b.n_hits
+    g = grid if grid is not None else w.grid(b.n_events)
+    return Pipeline(ctx, w.config(), g, b.n_events, N, *[k * N + 4096 for k in per_hit])
+
+
+@pytest.mark.parametrize("name,n_ev", [("pileup50-batch100", 100), ("pileup200", 16)])
+def test_batched_chain_equals_oracle_at_scale(gpu_ctx, name, n_ev):
+    w = gen.WORKLOADS[name]
+    b = gen.generate_batch(w, n_ev)
+    p = pipeline_for(gpu_ctx, w, b)
+    trk, off, counts = p.seed(b)
+    assert counts["status"] == 0
+    want, want_off, st = oracle_trk(b, w)
+    assert len(want) > 1000
+    assert np.array_equal(trk, want)
+    assert np.array_equal(off, want_off)
+    assert counts["n_pairs"] == st["pairs"] and counts["pair_slots"] == st["pair_slots"]
+    assert counts["n_candidates"] == st["cands"] and counts["cand_slots"] == st["cand_slots"]
+    assert counts["cand_truncated"] == st["cand_truncated"]
+
+
+def test_pileup200_64_events_streaming_equals_oracle(gpu_ctx):
+    """The benchmark's streaming form (two batches in flight) on 64
+    pile-up-200 events, 1.6 M hits, against the oracle."""
+    w = gen.WORKLOADS["pileup200"]
+    b = gen.generate_batch(w, 64, first_event=1000)
+    p = pipeline_for(gpu_ctx, w, b)
+    t1 = p.submit(b)
+    t2 = p.submit(b)
+    trk1, off1, c1 = p.wait(t1)
+    trk2, off2, c2 = p.wait(t2)
+    assert c1["status"] == 0 and np.array_equal(trk1, trk2) and np.array_equal(off1, off2)
+    want, want_off, _ = oracle_trk(b, w)
+    assert np.array_equal(trk1, want)
+    assert np.array_equal(off1, want_off)
+
+
+@pytest.mark.parametrize("zp", [(64, 64), (64, 128), (32, 64)])
+def test_autotuned_grids_equal_oracle(gpu_ctx, zp):
+    """The grids the autotuner selects on pile-up 200 (the truncated
+    candidate set depends on the grid, so the oracle runs at the same one),
+    with every walk setting the tuner tries."""
+    from trax_gb300.autotune import WALK_CANDIDATES
+    w = gen.WORKLOADS["pileup200"]
+    b = gen.generate_batch(w, 8, first_event=2000)
+    g = gen.Workload(w.name, w.config_id, w.n_layers, w.noise, w.pt_range, zp[0], zp[1],
+                     w.n_triplets, pileup_mean=w.pileup_mean)
+    grid = g.grid(b.n_events)
+    want, want_off, _ = oracle_trk(b, g, grid)
+    p = pipeline_for(gpu_ctx, g, b, grid)
+    for rw, zi in WALK_CANDIDATES[:4]:
+        for rec in (3, 1):
+            gpu_ctx.set_tuning(rw, zi, rec)
+            trk, off, counts = p.seed(b)
+            assert counts["status"] == 0
+            assert np.array_equal(trk, want), (rw, zi, rec)
+            assert np.array_equal(off, want_off)
+    gpu_ctx.set_tuning(48, 16, 3)
+
+
+def test_serving_stream_equals_oracle(gpu_ctx):
+    """Events of the streaming workload (pile-up ~ U{0..200}) arriving as a
+    Poisson stream through the continuous-batching server: every event's
+    tracklets equal the oracle's for that event alone."""
+    from trax_gb300.serve import Server, poisson_arrivals
+    w = gen.WORKLOADS["stream-pileup-u200"]
+    events = [gen.generate_batch(w, 1, first_event=300 + i) for i in range(24)]
+    cfg = w.config()
+    with Server(cfg, w.n_layers, w.n_sectors_z, w.n_sectors_phi, slots=3,
+                max_batch_events=8, memory_budget_bytes=6 << 30) as srv:
+        t0 = srv.now_ns() + 20_000_000
+        arrivals = poisson_arrivals(len(events), 2000.0, t0, seed=5)
+        tickets = [srv.submit(e, int(a)) for e, a in zip(events, arrivals)]
+        got = {}
+        while len(got) < len(events):
+            r = srv.poll(timeout_ms=20_000)
+            assert r is not None, "server stalled"
+            assert r["status"] == 0
+            got[r["ticket"]] = r
+    for t, e in zip(tickets, events):
+        r = oracle.run(e, cfg, w.grid(1), 4, n_threads=1, omp_threads=8)
+        so = r["sorted_orig"]
+        want = np.stack([so[r["trk_h1"]], so[r["trk_h2"]], so[r["trk_h3"]]], axis=1) \
+            if r["trk_h1"].size else np.zeros((0, 3), np.uint32)
+        assert np.array_equal(got[t]["tracklets"], want)

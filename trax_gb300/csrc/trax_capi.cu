@@ -169,11 +169,13 @@ void free_async(trax_ctx *ctx)
             return fail(ctx, TRAX_ERR_DEVICE, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-trax_status ensure(trax_ctx *ctx, DevBuf &b, size_t bytes)
+/* in_graph: the buffer may be referenced by a captured graph (every scratch
+ * buffer of the chain); st3, used only by the standalone scan, is not. */
+trax_status ensure(trax_ctx *ctx, DevBuf &b, size_t bytes, bool in_graph = true)
 {
     if (bytes == 0) bytes = 16;
     if (b.bytes >= bytes) return TRAX_OK;
-    if (ctx->reserved && has_graph(ctx)) {
+    if (in_graph && ctx->reserved && has_graph(ctx)) {
         /* buffers captured in the graph must not move */
         return fail(ctx, TRAX_ERR_OOM, "scratch beyond the reserved size");
     }
@@ -1040,7 +1042,7 @@ trax_status trax_prefix_sum(trax_ctx *ctx, const uint32_t *d_in, uint32_t *d_out
 {
     if (!ctx || (n && (!d_in || !d_out))) return TRAX_ERR_BAD_ARG;
     const uint32_t items = kScanThreads * kScanItems;
-    trax_status s = ensure(ctx, ctx->st3, (size_t)tiles_for(n, items) * 8);
+    trax_status s = ensure(ctx, ctx->st3, (size_t)tiles_for(n, items) * 8, false);
     if (s != TRAX_OK) return s;
     if ((s = ensure_stage(ctx, 1)) != TRAX_OK) return s;
     ctx->h_stage[0] = n;
@@ -1137,7 +1139,7 @@ trax_status trax_selftest_lookback_timeout(trax_ctx *ctx, const uint32_t *d_in, 
 {
     const uint32_t items = kScanThreads * kScanItems;
     if (!ctx || !d_in || !d_out || n <= items || spin_limit == 0) return TRAX_ERR_BAD_ARG;
-    trax_status s = ensure(ctx, ctx->st3, (size_t)tiles_for(n, items) * 8);
+    trax_status s = ensure(ctx, ctx->st3, (size_t)tiles_for(n, items) * 8, false);
     if (s != TRAX_OK) return s;
     DevState *st = ctx->d_state;
     CK(cudaMemsetAsync(ctx->st3.p, 0, (size_t)tiles_for(n, items) * 8, ctx->stream));
