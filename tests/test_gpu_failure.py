@@ -26,7 +26,8 @@ def test_lookback_wait_gives_up_and_context_stays_usable(gpu_ctx):
     ctx.reset_counts()
     st = ctx.lib.trax_selftest_lookback_timeout(ctx.h, d_in.ptr, d_out.ptr, n, 2000)
     assert st == 0
-    ctx.synchronize()
+    # synchronising returns the device status word: the wait gave up
+    assert ctx.lib.trax_ctx_synchronize(ctx.h) == TRAX_ERR_TIMEOUT
     c = ctx.counts()
     assert c["status"] == TRAX_ERR_TIMEOUT and c["error_detail"] == TRAX_DETAIL_SCAN_TIMEOUT, c
 
