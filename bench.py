@@ -638,8 +638,11 @@ def run_ours(args, dist):
     if counts["status"] != 0:
         raise SystemExit(f"device status after timed run {counts}")
     if args.only_resident:
+        kms = {k: round(v, 4) for k, v in kernel_times(ctx, p, reps=5).items()} \
+            if os.environ.get("TRAX_BENCH_KERNELS") else None
         if dist.rank == 0:
             print(json.dumps({"metric": "events/s", "value": round(value, 2), "unit": "events/s",
+                              "kernels_ms": kms,
                               "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
                               "ms_per_step": round(ms_total / args.steps, 4),
                               "config": {"workload": args.workload, "events_per_step": B,

@@ -107,3 +107,29 @@ def test_serving_stream_equals_oracle(gpu_ctx):
         want = np.stack([so[r["trk_h1"]], so[r["trk_h2"]], so[r["trk_h3"]]], axis=1) \
             if r["trk_h1"].size else np.zeros((0, 3), np.uint32)
         assert np.array_equal(got[t]["tracklets"], want)
+
+
+@pytest.mark.parametrize("zp,zscale", [((64, 128), 8.0), ((64, 128), 1.0), ((48, 96), 10.0)])
+def test_grid_build_in_row_bands_equals_oracle(gpu_ctx, zp, zscale):
+    """Fine grids whose cell tables do not fit shared memory are built in
+    bands of z rows.  Hits stretched along z (x zscale) occupy most rows and
+    so several bands; the grid, the sorted order and the tracklets equal the
+    oracle's."""
+    w0 = gen.WORKLOADS["multimuon-1000trk"]
+    w = gen.Workload(w0.name, w0.config_id, w0.n_layers, w0.noise, w0.pt_range, zp[0], zp[1],
+                     w0.n_triplets, tracks=w0.tracks)
+    b = gen.generate_batch(w, 3)
+    b.z = (b.z * np.float32(zscale)).astype(np.float32)
+    grid = w.grid(b.n_events)
+    r = oracle.run(b, w.config(), grid, 4, n_threads=1, omp_threads=8)
+    assert r["stats"]["status"] == 0
+    p = pipeline_for(gpu_ctx, w, b, grid)
+    trk, off, counts = p.seed(b)
+    assert counts["status"] == 0
+    assert np.array_equal(trk, oracle.canonical(r)["tracklets"])
+    assert np.array_equal(off, r["trk_offsets"])
+    # the stage call's grid and sorted order as well
+    from trax_gb300.ops import build_triplets
+    hits, g, _, _, _ = build_triplets(gpu_ctx, b, w.config(), zp[0], zp[1])
+    assert np.array_equal(g.download(), r["grid"])
+    assert np.array_equal(hits.download()["orig"], r["sorted_orig"])

@@ -97,9 +97,10 @@ struct trax_ctx {
     trax_grid_cfg r_grid{};
     DevBuf in_cols[7], srt_cols[9], grid_buf, pairs_buf, pair_off, cands_buf, cand_off;
     DevBuf trk_cols[3], trk_off, trk_map[3], r_seg;
-    uint32_t gb_C = 0, gb_avg = 0;        /* cached k_grid_build launch plan */
+    uint32_t gb_C = 0, gb_P1 = 0, gb_avg = 0;  /* cached k_grid_build launch plan */
     int gb_warps = 0, gb_per_sm = 0;
     uint32_t gb_stage = 0;                /* k_grid_build staged-segment capacity */
+    uint32_t gb_cells = 0;                /* k_grid_build per-warp table cells */
     cudaGraphExec_t graph = nullptr;
     uint32_t staged_events = 0, staged_hits = 0;
     /* streaming submission: two slots, uploads on their own stream */
@@ -239,45 +240,52 @@ trax_status check_grid(trax_ctx *ctx, const trax_grid_cfg *g, bool need_cfg = tr
     return TRAX_OK;
 }
 
-/* Dynamic shared memory plan of k_grid_build: W warps with (W+1)*C words.
- * A warp holds up to 32 * kGridItems hits of its segment in registers;
- * enough warps for 1.5x the average segment keep the larger layers' segments
- * on that path (a segment beyond it computes its cells twice), and more
- * warps would waste the per-warp cell tables. */
-int grid_build_warps(const trax_ctx *ctx, uint32_t C, uint32_t avg_seg, uint32_t stage)
-{
-    const size_t budget = std::min<size_t>(ctx->smem_optin, 200 * 1024);
-    long w = (long)((budget - 8ull * stage) / (4ull * C)) - 1;
-    const long per_warp = 32 * kGridItems;
-    long want = (long)((3ull * avg_seg / 2 + per_warp - 1) / per_warp);
-    want = std::min<long>(std::max<long>(want, 1), 32);
-    if (w > want) w = want;
-    return (int)w;
-}
-
-/* Warps and resident CTAs of k_grid_build for C cells; computed outside
- * any stream capture and cached. */
+/* Launch plan of k_grid_build for C cells of nphi + 1 columns and segments
+ * of avg_seg hits on average; computed outside any stream capture and
+ * cached.
+ *   staging  segments up to 1.5x the average (at least 512 hits) are staged
+ *            in shared memory for coalesced column writes, within half of
+ *            the shared-memory budget;
+ *   warps    enough for 1.5x the average segment at kGridItems * 32 hits a
+ *            warp (at most 32);
+ *   tables   per-warp cell tables of Ct cells: the whole grid when it fits,
+ *            else whole z rows -- at least min(8, Z + 1) of them, with fewer
+ *            warps if need be -- and the kernel works in bands of rows. */
 trax_status grid_plan(trax_ctx *ctx, uint32_t C, uint32_t avg_seg)
 {
-    if (ctx->gb_C == C && ctx->gb_avg == avg_seg && ctx->gb_warps > 0) return TRAX_OK;
-    /* staged segments up to 1.5x the average size (at least 512 hits), while
-     * the staging stays within a quarter of the shared-memory budget */
-    uint32_t stage = std::max<uint32_t>(512, (3 * avg_seg / 2 + 255) / 256 * 256);
+    const uint32_t P1 = ctx->kp.nphi + 1, rows = C / P1;
+    if (ctx->gb_C == C && ctx->gb_P1 == P1 && ctx->gb_avg == avg_seg && ctx->gb_warps > 0)
+        return TRAX_OK;
     const size_t budget = std::min<size_t>(ctx->smem_optin, 200 * 1024);
-    while (stage > 256 && 8ull * stage > budget / 4) stage -= 256;
-    int W = grid_build_warps(ctx, C, avg_seg, stage);
-    if (W < 1) {
+    uint32_t stage = std::max<uint32_t>(512, (3 * avg_seg / 2 + 255) / 256 * 256);
+    while (stage > 256 && 8ull * stage > budget / 2) stage -= 256;
+    const long per_warp = 32 * kGridItems;
+    long W = (long)((3ull * avg_seg / 2 + per_warp - 1) / per_warp);
+    W = std::min<long>(std::max<long>(W, 1), 32);
+    auto table = [&](long w) -> uint64_t { return (budget - 8ull * stage) / (4ull * (w + 1)); };
+    const uint64_t want = C <= table(W) ? C : (uint64_t)std::min<uint32_t>(8, rows) * P1;
+    while (W > 1 && table(W) < want) --W;
+    uint64_t Ct = std::min<uint64_t>(table(W), C);
+    if (Ct < C) Ct = Ct / P1 * P1;
+    if (Ct < P1) {
         stage = 0;
-        W = grid_build_warps(ctx, C, avg_seg, 0);
+        W = 1;
+        Ct = std::min<uint64_t>(table(1), C);
+        if (Ct < C) Ct = Ct / P1 * P1;
     }
-    if (W < 1) return fail(ctx, TRAX_ERR_BAD_ARG, "grid too large for shared memory");
+    if (Ct < P1) return fail(ctx, TRAX_ERR_BAD_ARG, "grid too large for shared memory");
     int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_grid_build, W * 32,
-                                                     ((size_t)(W + 1) * C + 2ull * stage) * 4));
+    const size_t smem = ((size_t)(W + 1) * Ct + 2ull * stage) * 4;
+    if (Ct < C)
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_grid_build<true>, (int)W * 32, smem));
+    else
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_grid_build<false>, (int)W * 32, smem));
     ctx->gb_stage = stage;
     ctx->gb_C = C;
+    ctx->gb_P1 = P1;
     ctx->gb_avg = avg_seg;
-    ctx->gb_warps = W;
+    ctx->gb_warps = (int)W;
+    ctx->gb_cells = (uint32_t)Ct;
     ctx->gb_per_sm = per_sm < 1 ? 1 : per_sm;
     return TRAX_OK;
 }
@@ -327,12 +335,16 @@ trax_status enqueue_grid(trax_ctx *ctx, const InCols &in, const SortedCols &out,
     trax_status s = grid_plan(ctx, kp.C, max_segs ? n_hits / max_segs : 0);
     if (s != TRAX_OK) return s;
     const int W = ctx->gb_warps, per_sm = ctx->gb_per_sm;
-    const size_t smem = ((size_t)(W + 1) * kp.C + 2ull * ctx->gb_stage) * 4;
+    const size_t smem = ((size_t)(W + 1) * ctx->gb_cells + 2ull * ctx->gb_stage) * 4;
     uint32_t blocks = std::min<uint32_t>(max_segs, (uint32_t)(ctx->sm_count * per_sm));
     if (blocks == 0) blocks = 1;
     CK(cudaMemsetAsync(&ctx->d_state->gb_next, 0, 4, ctx->stream));  /* segment counter */
-    k_grid_build<<<blocks, W * 32, smem, ctx->stream>>>(kp, in, out, seg_start, seg_n, grid,
-                                                        ctx->gb_stage, ctx->d_state);
+    if (ctx->gb_cells < kp.C)
+        k_grid_build<true><<<blocks, W * 32, smem, ctx->stream>>>(
+            kp, in, out, seg_start, seg_n, grid, ctx->gb_stage, ctx->gb_cells, ctx->d_state);
+    else
+        k_grid_build<false><<<blocks, W * 32, smem, ctx->stream>>>(
+            kp, in, out, seg_start, seg_n, grid, ctx->gb_stage, ctx->gb_cells, ctx->d_state);
     CK(cudaGetLastError());
     return mark(ctx, "grid_build");
 }
@@ -791,9 +803,11 @@ trax_status trax_ctx_create(trax_ctx **out, int device)
     for (int i = 0; i < kTimerSlots; ++i)
         if ((e = cudaEventCreate(&ctx->timers[i])) != cudaSuccess) return bail(e);
     cudaFuncAttributes fa{};
-    if ((e = cudaFuncGetAttributes(&fa, k_grid_build)) != cudaSuccess) return bail(e);
+    if ((e = cudaFuncGetAttributes(&fa, k_grid_build<true>)) != cudaSuccess) return bail(e);
     ctx->smem_optin = (size_t)optin - fa.sharedSizeBytes;
-    if ((e = cudaFuncSetAttribute(k_grid_build, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if ((e = cudaFuncSetAttribute(k_grid_build<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)ctx->smem_optin)) != cudaSuccess) return bail(e);
+    if ((e = cudaFuncSetAttribute(k_grid_build<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)ctx->smem_optin)) != cudaSuccess) return bail(e);
     int b = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_fused<true>, kFusedThreads, 0);

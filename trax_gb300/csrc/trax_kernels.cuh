@@ -355,55 +355,94 @@ constexpr int kGridItems = 4; /* hits per lane held in registers across passes *
  *           gathered from inside the segment (L1/L2 resident).
  * Larger segments scatter each column directly (4-byte stores to random
  * positions: one L2 sector per store).  Within a cell, hits keep input order.
- * Dynamic shared memory: (W + 1) * C + 2 * stage words.
+ *
+ * The per-warp cell tables hold Ct cells.  When the grid has more (fine
+ * grids: 64 x 128 bins are 8385 cells per layer), passes 1-3 run per band of
+ * Ct / (P + 1) z rows, over the rows the segment's hits occupy (pass 0 finds
+ * them; a band covers the whole occupied range in one go for hits within a
+ * few z rows, as barrel layers give), and the grid rows outside that range
+ * get the segment's start or end.  Cells are row-major, so a band's hits are
+ * one contiguous part of the sorted segment.
+ * Dynamic shared memory: (W + 1) * Ct + 2 * stage words.  BANDED is Ct < C
+ * (the instance with bands has 64 registers, the other 48).
  */
-__global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols out,
-                                                     const uint32_t *seg_start,
-                                                     const uint32_t *seg_n, uint32_t *grid,
-                                                     uint32_t stage, DevState *st)
+template <bool BANDED>
+__global__ void __maxnreg__(BANDED ? 64 : 48) k_grid_build(KParams kp, InCols in, SortedCols out,
+                                                           const uint32_t *seg_start,
+                                                           const uint32_t *seg_n, uint32_t *grid,
+                                                           uint32_t stage, uint32_t Ct,
+                                                           DevState *st)
 {
     extern __shared__ uint32_t smem[];
     __shared__ uint32_t s_warp[33];
-    const uint32_t C = kp.C;
+    const uint32_t C = kp.C, P1 = kp.nphi + 1;
     const int W = blockDim.x >> 5;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    uint32_t *s_cnt = smem;                 /* [W][C] */
-    uint32_t *s_tot = smem + W * C;         /* [C] */
-    uint32_t *s_src = s_tot + C;            /* [stage] segment-relative input index */
+    uint32_t *s_cnt = smem;                 /* [W][Ct] */
+    uint32_t *s_tot = smem + W * Ct;        /* [Ct] */
+    uint32_t *s_src = s_tot + Ct;           /* [stage] segment-relative input index */
     float *s_phi = (float *)(s_src + stage);  /* [stage] */
     const uint32_t nseg = st->n_events * kp.n_layers;
     const uint32_t lt_mask = lanemask_lt();
+    /* BANDED: the grid's Z + 1 rows do not fit one table (Ct < C) */
+    const uint32_t R = BANDED ? Ct / P1 : kp.nz + 1;  /* z rows per band, >= 1 */
+    const bool banded = BANDED;
 
     /* each CTA takes its next segment from a counter as it finishes one:
      * the layers' segment sizes differ, and a fixed stride by the grid size
      * would pin every CTA to one layer (the grid is a multiple of the layer
-     * count).  Every thread reads s_seg before the segment's last barrier,
-     * after which thread 0 may overwrite it. */
-    __shared__ uint32_t s_seg;
+     * count).  Every thread reads s_seg (and the row range) before the
+     * segment's last barrier, after which thread 0 may overwrite them. */
+    __shared__ uint32_t s_seg, s_rlo, s_rhi;
     for (;;) {
-        if (threadIdx.x == 0) s_seg = atomicAdd(&st->gb_next, 1u);
+        if (threadIdx.x == 0) {
+            s_seg = atomicAdd(&st->gb_next, 1u);
+            s_rlo = 0xffffffffu;
+            s_rhi = 0u;
+        }
         __syncthreads();
         const uint32_t seg = s_seg;
         if (seg >= nseg) break;  /* block-uniform */
         const uint32_t e = seg / kp.n_layers, l = seg % kp.n_layers;
         const uint32_t start = seg_start[seg], n = seg_n[seg];
-        {
-            const uint32_t nw = (uint32_t)W * C, n4 = nw >> 2;
-            for (uint32_t k = threadIdx.x; k < n4; k += blockDim.x)
-                reinterpret_cast<uint4 *>(s_cnt)[k] = make_uint4(0u, 0u, 0u, 0u);
-            for (uint32_t k = (n4 << 2) + threadIdx.x; k < nw; k += blockDim.x) s_cnt[k] = 0;
-        }
-        __syncthreads();
         const uint32_t chunk = (n + W - 1) / W;
         const uint32_t lo = min(n, w * chunk), hi = min(n, lo + chunk);
         /* chunks of at most kGridItems * 32 hits keep cell, phi and peer mask
          * in registers from pass 1 to pass 3 */
         const bool cached = chunk <= (uint32_t)(kGridItems * 32);
         const bool staged = n <= stage;
+        uint32_t *gseg = grid + (size_t)seg * C;
+
+        /* pass 0: the z rows the segment's hits occupy */
+        uint32_t rlo = 0, rhi = kp.nz;
+        if (banded) {
+            uint32_t mn = 0xffffffffu, mx = 0u;
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+                uint32_t zs = trax_f2u(trax_floor_div(in.z[start + i] - TRAX_MIN_Z, kp.sz_z, kp.inv_sz_z));
+                if (zs > kp.nz) zs = kp.nz;
+                mn = min(mn, zs);
+                mx = max(mx, zs);
+            }
+#pragma unroll
+            for (int d = 16; d; d >>= 1) {
+                mn = min(mn, __shfl_xor_sync(kFull, mn, d));
+                mx = max(mx, __shfl_xor_sync(kFull, mx, d));
+            }
+            if (lane == 0) {
+                atomicMin(&s_rlo, mn);
+                atomicMax(&s_rhi, mx);
+            }
+            __syncthreads();
+            rlo = s_rlo;
+            rhi = s_rhi;
+            if (rlo > rhi) rlo = rhi = 0;  /* no hits */
+            /* rows below the occupied range start at the segment start */
+            for (uint32_t c = threadIdx.x; c < rlo * P1; c += blockDim.x) gseg[c] = start;
+            for (uint32_t c = (rhi + 1) * P1 + threadIdx.x; c < C; c += blockDim.x) gseg[c] = start + n;
+        }
+
         float cphi[kGridItems];
         uint32_t ccell[kGridItems], cpeers[kGridItems];
-
-        /* pass 1: per-warp cell counts */
         if (cached) {
             float cx[kGridItems], cy[kGridItems], cz[kGridItems];
 #pragma unroll
@@ -427,125 +466,161 @@ __global__ void __maxnreg__(48) k_grid_build(KParams kp, InCols in, SortedCols o
             if (anybad) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_OUTSIDE_GRID);
 #pragma unroll
             for (int j = 0; j < kGridItems; ++j) {
+                cpeers[j] = 0;
                 const uint32_t b = lo + j * 32;
                 if (b < hi) {  /* warp-uniform */
                     const bool valid = b + lane < hi;
                     const uint32_t act = __ballot_sync(kFull, valid);
-                    if (valid) {
-                        cpeers[j] = __match_any_sync(act, ccell[j]);
-                        if (lane == __ffs(cpeers[j]) - 1) s_cnt[w * C + ccell[j]] += __popc(cpeers[j]);
-                    }
-                    __syncwarp();
+                    if (valid) cpeers[j] = __match_any_sync(act, ccell[j]);
                 }
             }
-        } else {
-            for (uint32_t b = lo; b < hi; b += 32) {
-                const uint32_t i = b + lane;
-                const bool valid = i < hi;
-                const uint32_t act = __ballot_sync(kFull, valid);
-                if (valid) {
-                    const uint32_t h = start + i;
-                    float phi;
-                    bool bad;
-                    const uint32_t cell = hit_cell(kp, in.x[h], in.y[h], in.z[h], &phi, &bad);
-                    if (bad) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_OUTSIDE_GRID);
-                    const uint32_t peers = __match_any_sync(act, cell);
-                    if (lane == __ffs(peers) - 1) s_cnt[w * C + cell] += __popc(peers);
-                }
-                __syncwarp();
-            }
         }
-        __syncthreads();
 
-        /* pass 2: prefix over warps per cell, then scan over cells */
-        for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
-            uint32_t run = 0;
-            for (int q = 0; q < W; ++q) {
-                const uint32_t t = s_cnt[q * C + c];
-                s_cnt[q * C + c] = run;
-                run += t;
+        uint32_t band_base = 0;  /* hits in the rows below the band */
+        for (uint32_t rb = rlo; rb <= rhi; rb += R) {  /* block-uniform */
+            const uint32_t cb0 = rb * P1;
+            const uint32_t nb = min(R, rhi + 1 - rb) * P1;  /* the band's cells */
+            {
+                const uint32_t nw = (uint32_t)W * Ct, n4 = nw >> 2;
+                for (uint32_t k = threadIdx.x; k < n4; k += blockDim.x)
+                    reinterpret_cast<uint4 *>(s_cnt)[k] = make_uint4(0u, 0u, 0u, 0u);
+                for (uint32_t k = (n4 << 2) + threadIdx.x; k < nw; k += blockDim.x) s_cnt[k] = 0;
             }
-            s_tot[c] = run;
-        }
-        __syncthreads();
-        {
-            const uint32_t per = (C + blockDim.x - 1) / blockDim.x;
-            const uint32_t c0 = min(C, threadIdx.x * per), c1 = min(C, c0 + per);
-            uint32_t sum = 0;
-            for (uint32_t c = c0; c < c1; ++c) sum += s_tot[c];
-            uint32_t run = block_exclusive_scan(sum, s_warp, nullptr);
-            for (uint32_t c = c0; c < c1; ++c) {
-                const uint32_t t = s_tot[c];
-                s_tot[c] = run;
-                run += t;
-            }
-        }
-        __syncthreads();
-        /* s_tot now holds the cell starts and s_cnt each warp's offset inside
-         * the cell: a hit's position is their sum plus its rank in the warp */
-        for (uint32_t c = threadIdx.x; c < C; c += blockDim.x)
-            grid[(size_t)seg * C + c] = start + s_tot[c];
+            __syncthreads();
 
-        /* pass 3: positions (segment-relative) */
-        if (staged && cached) {
+            /* pass 1: per-warp counts of the band's cells */
+            if (cached) {
 #pragma unroll
-            for (int j = 0; j < kGridItems; ++j) {
-                const uint32_t b = lo + j * 32;
-                if (b < hi) {  /* warp-uniform */
-                    const bool valid = b + lane < hi;
-                    uint32_t pos = 0;
-                    if (valid) pos = s_tot[ccell[j]] + s_cnt[w * C + ccell[j]] + __popc(cpeers[j] & lt_mask);
+                for (int j = 0; j < kGridItems; ++j) {
+                    const uint32_t b = lo + j * 32;
+                    if (b < hi) {  /* warp-uniform */
+                        const uint32_t lc = ccell[j] - cb0;
+                        if (b + lane < hi && lc < nb && lane == __ffs(cpeers[j]) - 1)
+                            s_cnt[w * Ct + lc] += __popc(cpeers[j]);
+                        __syncwarp();
+                    }
+                }
+            } else {
+                for (uint32_t b = lo; b < hi; b += 32) {
+                    const uint32_t i = b + lane;
+                    bool valid = i < hi;
+                    uint32_t cell = 0;
+                    if (valid) {
+                        const uint32_t h = start + i;
+                        float phi;
+                        bool bad;
+                        cell = hit_cell(kp, in.x[h], in.y[h], in.z[h], &phi, &bad);
+                        if (bad && rb == rlo) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_OUTSIDE_GRID);
+                        valid = cell - cb0 < nb;
+                    }
+                    const uint32_t act = __ballot_sync(kFull, valid);
+                    if (valid) {
+                        const uint32_t peers = __match_any_sync(act, cell);
+                        if (lane == __ffs(peers) - 1) s_cnt[w * Ct + (cell - cb0)] += __popc(peers);
+                    }
                     __syncwarp();
-                    if (valid && lane == __ffs(cpeers[j]) - 1) s_cnt[w * C + ccell[j]] += __popc(cpeers[j]);
+                }
+            }
+            __syncthreads();
+
+            /* pass 2: prefix over warps per cell, then scan over cells */
+            for (uint32_t c = threadIdx.x; c < nb; c += blockDim.x) {
+                uint32_t run = 0;
+                for (int q = 0; q < W; ++q) {
+                    const uint32_t t = s_cnt[q * Ct + c];
+                    s_cnt[q * Ct + c] = run;
+                    run += t;
+                }
+                s_tot[c] = run;
+            }
+            __syncthreads();
+            uint32_t band_n;
+            {
+                const uint32_t per = (nb + blockDim.x - 1) / blockDim.x;
+                const uint32_t c0 = min(nb, threadIdx.x * per), c1 = min(nb, c0 + per);
+                uint32_t sum = 0;
+                for (uint32_t c = c0; c < c1; ++c) sum += s_tot[c];
+                uint32_t run = block_exclusive_scan(sum, s_warp, &band_n);
+                for (uint32_t c = c0; c < c1; ++c) {
+                    const uint32_t t = s_tot[c];
+                    s_tot[c] = run;
+                    run += t;
+                }
+            }
+            __syncthreads();
+            /* s_tot now holds the band's cell starts and s_cnt each warp's
+             * offset inside the cell: a hit's position is band_base plus
+             * their sum plus its rank in the warp */
+            for (uint32_t c = threadIdx.x; c < nb; c += blockDim.x)
+                gseg[cb0 + c] = start + band_base + s_tot[c];
+
+            /* pass 3: positions (segment-relative) */
+            if (staged && cached) {
+#pragma unroll
+                for (int j = 0; j < kGridItems; ++j) {
+                    const uint32_t b = lo + j * 32;
+                    if (b < hi) {  /* warp-uniform */
+                        const uint32_t lc = ccell[j] - cb0;
+                        const bool valid = b + lane < hi && lc < nb;
+                        uint32_t pos = 0;
+                        if (valid) pos = band_base + s_tot[lc] + s_cnt[w * Ct + lc] + __popc(cpeers[j] & lt_mask);
+                        __syncwarp();
+                        if (valid && lane == __ffs(cpeers[j]) - 1) s_cnt[w * Ct + lc] += __popc(cpeers[j]);
+                        __syncwarp();
+                        if (valid) {
+                            s_src[pos] = b + lane;
+                            s_phi[pos] = cphi[j];
+                        }
+                    }
+                }
+            } else {
+                for (uint32_t b = lo; b < hi; b += 32) {
+                    const uint32_t i = b + lane;
+                    bool valid = i < hi;
+                    uint32_t pos = 0, peers = 0, cell = 0;
+                    float x = 0.f, y = 0.f, z = 0.f, phi = 0.f;
+                    uint32_t h = 0;
+                    if (valid) {
+                        h = start + i;
+                        x = in.x[h]; y = in.y[h]; z = in.z[h];
+                        bool bad;
+                        cell = hit_cell(kp, x, y, z, &phi, &bad);
+                        valid = cell - cb0 < nb;
+                    }
+                    const uint32_t act = __ballot_sync(kFull, valid);
+                    if (valid) {
+                        peers = __match_any_sync(act, cell);
+                        pos = band_base + s_tot[cell - cb0] + s_cnt[w * Ct + (cell - cb0)] +
+                              __popc(peers & lt_mask);
+                    }
+                    __syncwarp();
+                    if (valid && lane == __ffs(peers) - 1) s_cnt[w * Ct + (cell - cb0)] += __popc(peers);
                     __syncwarp();
                     if (valid) {
-                        s_src[pos] = b + lane;
-                        s_phi[pos] = cphi[j];
-                    }
-                }
-            }
-        } else {
-            for (uint32_t b = lo; b < hi; b += 32) {
-                const uint32_t i = b + lane;
-                const bool valid = i < hi;
-                const uint32_t act = __ballot_sync(kFull, valid);
-                uint32_t pos = 0, peers = 0, cell = 0;
-                float x = 0.f, y = 0.f, z = 0.f, phi = 0.f;
-                uint32_t h = 0;
-                if (valid) {
-                    h = start + i;
-                    x = in.x[h]; y = in.y[h]; z = in.z[h];
-                    bool bad;
-                    cell = hit_cell(kp, x, y, z, &phi, &bad);
-                    peers = __match_any_sync(act, cell);
-                    pos = s_tot[cell] + s_cnt[w * C + cell] + __popc(peers & lt_mask);
-                }
-                __syncwarp();
-                if (valid && lane == __ffs(peers) - 1) s_cnt[w * C + cell] += __popc(peers);
-                __syncwarp();
-                if (valid) {
-                    if (staged) {
-                        s_src[pos] = i;
-                        s_phi[pos] = phi;
-                    } else {
-                        const uint32_t ly = in.layer[h], ev = in.event[h];
-                        if (ly != l + 1 || ev != e) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_LAYER_MISMATCH);
-                        const uint32_t d = start + pos;
-                        if (out.x) {
-                            out.x[d] = x; out.y[d] = y; out.z[d] = z; out.phi[d] = phi;
-                            out.det[d] = in.det[h]; out.hitid[d] = in.hitid[h];
-                        }
-                        out.layer[d] = ly; out.event[d] = ev; out.orig[d] = h;
-                        if (out.zphi) {
-                            out.zphi[d] = make_float2(z, phi);
-                            out.zh[d] = __half_as_ushort(__float2half_rn(z));
-                            out.xyzp[d] = make_float4(x, y, z, phi);
+                        if (staged) {
+                            s_src[pos] = i;
+                            s_phi[pos] = phi;
+                        } else {
+                            const uint32_t ly = in.layer[h], ev = in.event[h];
+                            if (ly != l + 1 || ev != e) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_LAYER_MISMATCH);
+                            const uint32_t d = start + pos;
+                            if (out.x) {
+                                out.x[d] = x; out.y[d] = y; out.z[d] = z; out.phi[d] = phi;
+                                out.det[d] = in.det[h]; out.hitid[d] = in.hitid[h];
+                            }
+                            out.layer[d] = ly; out.event[d] = ev; out.orig[d] = h;
+                            if (out.zphi) {
+                                out.zphi[d] = make_float2(z, phi);
+                                out.zh[d] = __half_as_ushort(__float2half_rn(z));
+                                out.xyzp[d] = make_float4(x, y, z, phi);
+                            }
                         }
                     }
                 }
             }
+            band_base += band_n;
+            __syncthreads();
         }
-        __syncthreads();
 
         /* pass 4: coalesced column writes of a staged segment */
         if (staged) {
