@@ -541,6 +541,18 @@ trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers
  * the result is the same. */
 trax_status trax_seed_batch(trax_ctx *ctx, const trax_event_batch *in, trax_batch_result *out);
 
+/* Admission bound for serving (no counterpart in the reference, which sizes
+ * its Pairing after a blocking download of the scanned pair count,
+ * PairGeneratorBeamspot.cpp:117-136).  Stages the batch like
+ * trax_stage_batch, runs the grid build and the pair stage's count passes --
+ * per outer hit its distinct pairs, their scan, the per-(event, layer
+ * triplet) offsets -- and writes each event's pair total to
+ * event_pairs[n_events] (host).  Nothing is stored; synchronous.  These are
+ * exactly the pairs trax_seed_batch would store for the event, in any batch.
+ * Needs the beam-spot pair generator. */
+trax_status trax_count_pairs_batch(trax_ctx *ctx, const trax_event_batch *in,
+                                   uint32_t *event_pairs);
+
 /* Streaming form of trax_seed_batch (the reference's per-group loop in
  * TripletBuilder.cpp:183-285, with the next group's upload overlapping this
  * group's chain).  trax_submit_batch queues one batch -- its upload on the
@@ -616,6 +628,9 @@ typedef struct trax_server_stats {
     uint64_t slot_max_hits;        /* hit capacity of one slot's batch */
     uint64_t p50_ns, p99_ns, max_ns;   /* arrival -> result latency */
     double sustained_events_per_s;     /* events / (last result - first arrival) */
+    uint64_t slot_max_pairs;       /* pair capacity of one slot's batch */
+    uint64_t count_passes;         /* admission pair-count passes run */
+    uint64_t deferred;             /* requests sent back to the queue by the pair bound */
 } trax_server_stats;
 
 uint64_t trax_now_ns(void);  /* monotonic clock used for arrivals and latencies */

@@ -133,7 +133,9 @@ class TraxServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("events", C.c_uint64), ("batches", C.c_uint64),
                 ("batched_events", C.c_uint64), ("splits", C.c_uint64), ("errors", C.c_uint64),
                 ("slot_max_hits", C.c_uint64), ("p50_ns", C.c_uint64), ("p99_ns", C.c_uint64),
-                ("max_ns", C.c_uint64), ("sustained_events_per_s", C.c_double)]
+                ("max_ns", C.c_uint64), ("sustained_events_per_s", C.c_double),
+                ("slot_max_pairs", C.c_uint64), ("count_passes", C.c_uint64),
+                ("deferred", C.c_uint64)]
 
     def as_dict(self):
         return {k: (float(getattr(self, k)) if t is C.c_double else int(getattr(self, k)))

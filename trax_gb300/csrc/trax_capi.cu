@@ -247,7 +247,7 @@ trax_status check_grid(trax_ctx *ctx, const trax_grid_cfg *g, bool need_cfg = tr
  *            in shared memory for coalesced column writes, within half of
  *            the shared-memory budget;
  *   warps    enough for 1.5x the average segment at kGridItems * 32 hits a
- *            warp (at most 32);
+ *            warp (kGridItemsBanded with bands; at most 32);
  *   tables   per-warp cell tables of Ct cells: the whole grid when it fits,
  *            else whole z rows -- at least min(8, Z + 1) of them, with fewer
  *            warps if need be -- and the kernel works in bands of rows. */
@@ -259,10 +259,15 @@ trax_status grid_plan(trax_ctx *ctx, uint32_t C, uint32_t avg_seg)
     const size_t budget = std::min<size_t>(ctx->smem_optin, 200 * 1024);
     uint32_t stage = std::max<uint32_t>(512, (3 * avg_seg / 2 + 255) / 256 * 256);
     while (stage > 256 && 8ull * stage > budget / 2) stage -= 256;
-    const long per_warp = 32 * kGridItems;
-    long W = (long)((3ull * avg_seg / 2 + per_warp - 1) / per_warp);
-    W = std::min<long>(std::max<long>(W, 1), 32);
     auto table = [&](long w) -> uint64_t { return (budget - 8ull * stage) / (4ull * (w + 1)); };
+    auto warps_for = [&](long items) {
+        const long per_warp = 32 * items;
+        const long w = (long)((3ull * avg_seg / 2 + per_warp - 1) / per_warp);
+        return std::min<long>(std::max<long>(w, 1), 32);
+    };
+    /* the banded instance holds more hits per lane */
+    long W = warps_for(kGridItems);
+    if (C > table(W)) W = warps_for(kGridItemsBanded);
     const uint64_t want = C <= table(W) ? C : (uint64_t)std::min<uint32_t>(8, rows) * P1;
     while (W > 1 && table(W) < want) --W;
     uint64_t Ct = std::min<uint64_t>(table(W), C);
@@ -427,6 +432,42 @@ trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *gr
                                                              TRAX_DETAIL_PAIR_CAPACITY, st);
     CK(cudaGetLastError());
     return mark(ctx, "pair_offsets");
+}
+
+/* The pair stage's count passes alone (beam-spot generator): per outer hit
+ * the distinct pairs it makes, their scan, and the per-group offsets --
+ * what the chain would store, without storing it. */
+trax_status enqueue_pair_count(trax_ctx *ctx, const SortedCols &h, const uint32_t *grid,
+                               uint32_t *pair_offsets, uint32_t slot_cap, uint32_t max_groups)
+{
+    const KParams &kp = ctx->kp;
+    trax_status s = need_packed(ctx, h);
+    if (s != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->g_start, (size_t)max_groups * 4)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->g_base, (size_t)(max_groups + 1) * 4)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->slots, (size_t)slot_cap * 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->pexcl, (size_t)(slot_cap + 1) * 4)) != TRAX_OK) return s;
+    const uint32_t stile = tiles_for(slot_cap, kScanItems * kScanThreads);
+    if ((s = ensure(ctx, ctx->st0, (size_t)std::max(stile, tiles_for(slot_cap, kTileItems)) * 8)) != TRAX_OK)
+        return s;
+    uint32_t *g_start = (uint32_t *)ctx->g_start.p, *g_base = (uint32_t *)ctx->g_base.p;
+    uint2 *slots = (uint2 *)ctx->slots.p;
+    uint32_t *pexcl = (uint32_t *)ctx->pexcl.p;
+    DevState *st = ctx->d_state;
+    k_pair_groups<<<1, 1024, 0, ctx->stream>>>(kp, grid, g_start, g_base, st, false);
+    k_pair_slots<<<ctx->blk_small, 256, 0, ctx->stream>>>(kp, g_start, g_base, slots, slot_cap, st);
+    CK(cudaMemsetAsync(&st->tile_ctr[0], 0, 4, ctx->stream));
+    k_pair_count_lane<<<ctx->blk_pair_count, kFusedThreads, 0, ctx->stream>>>(
+        kp, grid, h.xyzp, h.zphi, slots, slot_cap, pexcl, nullptr, 0, st);
+    CK(cudaMemsetAsync(&st->tile_ctr[0], 0, 4, ctx->stream));
+    CK(cudaMemsetAsync(ctx->st0.p, 0, (size_t)stile * 8, ctx->stream));
+    k_scan<kScanItems><<<std::min<uint32_t>(ctx->blk_scan, stile), kScanThreads, 0, ctx->stream>>>(
+        pexcl, pexcl, &st->n_outer, slot_cap, &st->n_pairs, 0, (unsigned long long *)ctx->st0.p, st);
+    k_group_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(g_base, pexcl, pair_offsets, kp.n_lt,
+                                                             slot_cap, &st->n_pairs, 0xffffffffu,
+                                                             TRAX_DETAIL_PAIR_CAPACITY, st);
+    CK(cudaGetLastError());
+    return TRAX_OK;
 }
 
 /* Per-cell z index of the sorted hits (k_zindex) into ctx->zi. */
@@ -1718,6 +1759,41 @@ trax_status trax_stage_batch(trax_ctx *ctx, const trax_event_batch *in)
                                            cudaMemcpyHostToDevice, ctx->stream));
     ctx->staged_events = E;
     ctx->staged_hits = in->n_hits;
+    return TRAX_OK;
+}
+
+trax_status trax_count_pairs_batch(trax_ctx *ctx, const trax_event_batch *in,
+                                   uint32_t *event_pairs)
+{
+    if (!ctx || !in || !event_pairs) return TRAX_ERR_BAD_ARG;
+    if (ctx->pair_generator != TRAX_PAIRS_BEAMSPOT)
+        return fail(ctx, TRAX_ERR_BAD_ARG, "pair counts need the beam-spot pair generator");
+    trax_status s = trax_stage_batch(ctx, in);
+    if (s != TRAX_OK) return s;
+    fill_grid_params(ctx->kp, &ctx->r_grid);
+    const uint32_t T = ctx->kp.n_lt, E = in->n_events;
+    const uint32_t nseg = ctx->r_events * ctx->r_layers;
+    if ((s = grid_plan(ctx, ctx->kp.C, nseg ? ctx->r_hits / nseg : 0)) != TRAX_OK) return s;
+    const SortedCols sc = reserved_sorted(ctx);
+    uint32_t *grid = (uint32_t *)ctx->grid_buf.p;
+    const uint32_t *seg = (const uint32_t *)ctx->r_seg.p;
+    CK(cudaMemsetAsync(&ctx->d_state->n_outer, 0, sizeof(DevState) - 8, ctx->stream));
+    if ((s = enqueue_grid(ctx, in_cols_of(ctx->in_cols), sc, seg, seg + nseg, grid, nseg,
+                          ctx->r_hits)) != TRAX_OK)
+        return s;
+    if ((s = enqueue_pair_count(ctx, sc, grid, (uint32_t *)ctx->pair_off.p, ctx->r_hits * T + 1,
+                                ctx->r_events * T)) != TRAX_OK)
+        return s;
+    const size_t n_off = (size_t)E * T + 1;
+    if ((s = ensure_stage(ctx, n_off + 2)) != TRAX_OK) return s;
+    uint32_t *h = ctx->h_stage;
+    CK(cudaMemcpyAsync(h, ctx->pair_off.p, n_off * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(&ctx->h_state->status, &ctx->d_state->status, 8, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->h_state->status != TRAX_OK)
+        return fail(ctx, (trax_status)ctx->h_state->status, "device fault in the pair count");
+    for (uint32_t e = 0; e < E; ++e) event_pairs[e] = h[(size_t)(e + 1) * T] - h[(size_t)e * T];
     return TRAX_OK;
 }
 

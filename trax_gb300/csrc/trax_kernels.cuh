@@ -342,7 +342,8 @@ __device__ __forceinline__ uint32_t hit_cell(const KParams &kp, float x, float y
     return zs * (kp.nphi + 1) + ps;
 }
 
-constexpr int kGridItems = 4; /* hits per lane held in registers across passes */
+constexpr int kGridItems = 4;        /* hits per lane held in registers across passes */
+constexpr int kGridItemsBanded = 4;  /* the same in the banded instance */
 
 /*
  * One CTA per (event, layer) segment; W warps own contiguous sub-ranges.
@@ -373,6 +374,7 @@ __global__ void __maxnreg__(BANDED ? 64 : 48) k_grid_build(KParams kp, InCols in
                                                            uint32_t stage, uint32_t Ct,
                                                            DevState *st)
 {
+    constexpr int kItems = BANDED ? kGridItemsBanded : kGridItems;
     extern __shared__ uint32_t smem[];
     __shared__ uint32_t s_warp[33];
     const uint32_t C = kp.C, P1 = kp.nphi + 1;
@@ -407,9 +409,9 @@ __global__ void __maxnreg__(BANDED ? 64 : 48) k_grid_build(KParams kp, InCols in
         const uint32_t start = seg_start[seg], n = seg_n[seg];
         const uint32_t chunk = (n + W - 1) / W;
         const uint32_t lo = min(n, w * chunk), hi = min(n, lo + chunk);
-        /* chunks of at most kGridItems * 32 hits keep cell, phi and peer mask
+        /* chunks of at most kItems * 32 hits keep cell, phi and peer mask
          * in registers from pass 1 to pass 3 */
-        const bool cached = chunk <= (uint32_t)(kGridItems * 32);
+        const bool cached = chunk <= (uint32_t)(kItems * 32);
         const bool staged = n <= stage;
         uint32_t *gseg = grid + (size_t)seg * C;
 
@@ -441,12 +443,12 @@ __global__ void __maxnreg__(BANDED ? 64 : 48) k_grid_build(KParams kp, InCols in
             for (uint32_t c = (rhi + 1) * P1 + threadIdx.x; c < C; c += blockDim.x) gseg[c] = start + n;
         }
 
-        float cphi[kGridItems];
-        uint32_t ccell[kGridItems], cpeers[kGridItems];
+        float cphi[kItems];
+        uint32_t ccell[kItems], cpeers[kItems];
         if (cached) {
-            float cx[kGridItems], cy[kGridItems], cz[kGridItems];
+            float cx[kItems], cy[kItems], cz[kItems];
 #pragma unroll
-            for (int j = 0; j < kGridItems; ++j) {
+            for (int j = 0; j < kItems; ++j) {
                 const uint32_t i = lo + j * 32 + lane;
                 if (i < hi) {
                     const uint32_t h = start + i;
@@ -456,7 +458,7 @@ __global__ void __maxnreg__(BANDED ? 64 : 48) k_grid_build(KParams kp, InCols in
             /* independent atan2 chains first (ILP), then the warp votes */
             bool anybad = false;
 #pragma unroll
-            for (int j = 0; j < kGridItems; ++j) {
+            for (int j = 0; j < kItems; ++j) {
                 bool bad = false;
                 ccell[j] = 0;
                 cphi[j] = 0.f;
@@ -464,22 +466,26 @@ __global__ void __maxnreg__(BANDED ? 64 : 48) k_grid_build(KParams kp, InCols in
                 anybad |= bad;
             }
             if (anybad) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_OUTSIDE_GRID);
+            /* the peers of a hit (same cell, same warp step) do not depend on
+             * the band: with bands they are found once, here */
+            if (BANDED) {
 #pragma unroll
-            for (int j = 0; j < kGridItems; ++j) {
-                cpeers[j] = 0;
-                const uint32_t b = lo + j * 32;
-                if (b < hi) {  /* warp-uniform */
-                    const bool valid = b + lane < hi;
-                    const uint32_t act = __ballot_sync(kFull, valid);
-                    if (valid) cpeers[j] = __match_any_sync(act, ccell[j]);
+                for (int j = 0; j < kItems; ++j) {
+                    cpeers[j] = 0;
+                    const uint32_t b = lo + j * 32;
+                    if (b < hi) {  /* warp-uniform */
+                        const bool valid = b + lane < hi;
+                        const uint32_t act = __ballot_sync(kFull, valid);
+                        if (valid) cpeers[j] = __match_any_sync(act, ccell[j]);
+                    }
                 }
             }
         }
 
         uint32_t band_base = 0;  /* hits in the rows below the band */
         for (uint32_t rb = rlo; rb <= rhi; rb += R) {  /* block-uniform */
-            const uint32_t cb0 = rb * P1;
-            const uint32_t nb = min(R, rhi + 1 - rb) * P1;  /* the band's cells */
+            const uint32_t cb0 = BANDED ? rb * P1 : 0u;
+            const uint32_t nb = BANDED ? min(R, rhi + 1 - rb) * P1 : C;  /* the band's cells */
             {
                 const uint32_t nw = (uint32_t)W * Ct, n4 = nw >> 2;
                 for (uint32_t k = threadIdx.x; k < n4; k += blockDim.x)
@@ -491,11 +497,16 @@ __global__ void __maxnreg__(BANDED ? 64 : 48) k_grid_build(KParams kp, InCols in
             /* pass 1: per-warp counts of the band's cells */
             if (cached) {
 #pragma unroll
-                for (int j = 0; j < kGridItems; ++j) {
+                for (int j = 0; j < kItems; ++j) {
                     const uint32_t b = lo + j * 32;
                     if (b < hi) {  /* warp-uniform */
+                        const bool valid = b + lane < hi;
+                        if (!BANDED) {
+                            const uint32_t act = __ballot_sync(kFull, valid);
+                            if (valid) cpeers[j] = __match_any_sync(act, ccell[j]);
+                        }
                         const uint32_t lc = ccell[j] - cb0;
-                        if (b + lane < hi && lc < nb && lane == __ffs(cpeers[j]) - 1)
+                        if (valid && lc < nb && lane == __ffs(cpeers[j]) - 1)
                             s_cnt[w * Ct + lc] += __popc(cpeers[j]);
                         __syncwarp();
                     }
@@ -557,7 +568,7 @@ __global__ void __maxnreg__(BANDED ? 64 : 48) k_grid_build(KParams kp, InCols in
             /* pass 3: positions (segment-relative) */
             if (staged && cached) {
 #pragma unroll
-                for (int j = 0; j < kGridItems; ++j) {
+                for (int j = 0; j < kItems; ++j) {
                     const uint32_t b = lo + j * 32;
                     if (b < hi) {  /* warp-uniform */
                         const uint32_t lc = ccell[j] - cb0;
@@ -620,6 +631,7 @@ __global__ void __maxnreg__(BANDED ? 64 : 48) k_grid_build(KParams kp, InCols in
             }
             band_base += band_n;
             __syncthreads();
+            if (!BANDED) break;
         }
 
         /* pass 4: coalesced column writes of a staged segment */

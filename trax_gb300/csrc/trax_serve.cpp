@@ -10,11 +10,19 @@
  * frees first, so the slots' batches overlap on the device.
  *
  * Admission by memory budget: the budget is split over the slots and sized
- * into hit / pair / candidate / tracklet capacities.  The pair and candidate
- * totals are scanned on the device before anything is stored; when a batch
- * would exceed a capacity the device stores nothing beyond it, reports
- * TRAX_ERR_CAPACITY with the true size, and the worker splits the batch in
- * halves and reruns them.
+ * into hit / pair / candidate / tracklet capacities.  A worker admits the
+ * arrived requests into its batch while they fit the slot's event and hit
+ * capacity and -- the pair bound -- while their pair totals fit its pair
+ * capacity.  A request's pair total comes from the device before it is first
+ * admitted: the grid build and the pair stage's count passes run on the
+ * newly arrived requests as one batch and the scanned totals come back per
+ * event (trax_count_pairs_batch); they are exact, so a batch so admitted
+ * never overflows its pairs.  Requests that do not fit go back to the front
+ * of the queue with their totals and lead the next batch.  The candidate and
+ * tracklet totals are scanned on the device before anything is stored; when
+ * a batch would exceed one of those capacities the device stores nothing
+ * beyond it, reports TRAX_ERR_CAPACITY with the true size, and the worker
+ * splits the batch in halves and reruns them.
  *
  * Per-event results do not depend on the batch: every stage works inside its
  * (event, layer triplet) group and tracklets are returned as hit positions
@@ -44,10 +52,13 @@ uint64_t now_ns()
         .count();
 }
 
+constexpr uint32_t kPairsUnknown = 0xffffffffu;
+
 struct Request {
     uint64_t ticket = 0;
     uint64_t arrival_ns = 0;
     uint32_t n_hits = 0;
+    uint32_t pairs = kPairsUnknown;  /* the event's pair total, once counted */
     uint32_t layer_nhits[TRAX_MAX_LAYERS] = {};
     bool borrowed = false;
     const float *x = nullptr, *y = nullptr, *z = nullptr;
@@ -68,6 +79,8 @@ struct Result {
 struct Slot {
     trax_ctx *ctx = nullptr;
     uint32_t max_events = 0, max_hits = 0, trk_cap = 0;
+    uint64_t pair_cap = 0;
+    std::vector<uint32_t> event_pairs;  /* per event of an admission count */
     float *x = nullptr, *y = nullptr, *z = nullptr;
     uint32_t *layer = nullptr, *det = nullptr, *hitid = nullptr, *event = nullptr;
     uint32_t *layer_nhits = nullptr;
@@ -98,10 +111,11 @@ struct trax_server {
 
 namespace {
 
-void run_batch(trax_server *srv, Slot &slot, std::vector<Request *> &reqs, size_t lo, size_t hi,
-               uint64_t start_ns, std::vector<Result *> &out)
+/* Copies requests [lo, hi) into the slot's pinned staging as one batch. */
+trax_event_batch stage_requests(const trax_server *srv, Slot &slot,
+                                const std::vector<Request *> &reqs, size_t lo, size_t hi)
 {
-    const uint32_t L = srv->L, T = srv->T;
+    const uint32_t L = srv->L;
     const uint32_t E = (uint32_t)(hi - lo);
     uint32_t n = 0;
     for (size_t i = lo; i < hi; ++i) {
@@ -117,8 +131,34 @@ void run_batch(trax_server *srv, Slot &slot, std::vector<Request *> &reqs, size_
         std::memcpy(slot.layer_nhits + (size_t)e * L, r->layer_nhits, L * 4ull);
         n += r->n_hits;
     }
-    trax_event_batch b{E, L, n, slot.x, slot.y, slot.z, slot.layer, slot.det, slot.hitid,
-                       slot.event, slot.layer_nhits};
+    return trax_event_batch{E, L, n, slot.x, slot.y, slot.z, slot.layer, slot.det, slot.hitid,
+                            slot.event, slot.layer_nhits};
+}
+
+/* The pair totals of the requests not counted yet, from one device count
+ * pass over them as a batch. */
+trax_status count_pairs(trax_server *srv, Slot &slot, const std::vector<Request *> &reqs)
+{
+    std::vector<Request *> todo;
+    for (Request *r : reqs)
+        if (r->pairs == kPairsUnknown) todo.push_back(r);
+    if (todo.empty()) return TRAX_OK;
+    trax_event_batch b = stage_requests(srv, slot, todo, 0, todo.size());
+    slot.event_pairs.resize(todo.size());
+    const trax_status st = trax_count_pairs_batch(slot.ctx, &b, slot.event_pairs.data());
+    if (st != TRAX_OK) return st;
+    for (size_t i = 0; i < todo.size(); ++i) todo[i]->pairs = slot.event_pairs[i];
+    std::lock_guard<std::mutex> lock(srv->mu);
+    srv->stats.count_passes += 1;
+    return TRAX_OK;
+}
+
+void run_batch(trax_server *srv, Slot &slot, std::vector<Request *> &reqs, size_t lo, size_t hi,
+               uint64_t start_ns, std::vector<Result *> &out)
+{
+    const uint32_t T = srv->T;
+    const uint32_t E = (uint32_t)(hi - lo);
+    trax_event_batch b = stage_requests(srv, slot, reqs, lo, hi);
     trax_batch_result res{};
     res.hit1 = slot.h1; res.hit2 = slot.h2; res.hit3 = slot.h3; res.offsets = slot.off;
     res.capacity = slot.trk_cap;
@@ -198,15 +238,40 @@ void worker_main(trax_server *srv, size_t si)
             if (!srv->pending.empty()) srv->cv_work.notify_one();
         }
         const uint64_t start = now_ns();
-        if (batch.size() == 1 && batch[0]->n_hits > slot.max_hits) {
+        auto refuse = [&](Request *r) {
             Result *o = new Result();
-            o->ticket = batch[0]->ticket;
-            o->arrival_ns = batch[0]->arrival_ns;
+            o->ticket = r->ticket;
+            o->arrival_ns = r->arrival_ns;
             o->start_ns = o->done_ns = start;
             o->status = TRAX_ERR_CAPACITY;
             results.push_back(o);
+        };
+        if (batch.size() == 1 && batch[0]->n_hits > slot.max_hits) {
+            refuse(batch[0]);
         } else {
-            run_batch(srv, slot, batch, 0, batch.size(), start, results);
+            /* the pair bound: admit the longest prefix whose counted pairs
+             * fit the slot; the rest leads the next batch */
+            size_t k = batch.size();
+            if (count_pairs(srv, slot, batch) == TRAX_OK) {
+                uint64_t pairs = 0;
+                k = 0;
+                while (k < batch.size() && pairs + batch[k]->pairs <= slot.pair_cap)
+                    pairs += batch[k++]->pairs;
+                if (k < batch.size()) {
+                    std::lock_guard<std::mutex> lock(srv->mu);
+                    for (size_t i = batch.size(); i-- > std::max<size_t>(k, 1);)
+                        srv->pending.push_front(batch[i]);
+                    srv->stats.deferred += batch.size() - std::max<size_t>(k, 1);
+                }
+                if (k == 0) {  /* one event beyond the pair capacity: never fits */
+                    refuse(batch[0]);
+                    batch.resize(1);
+                } else {
+                    batch.resize(k);
+                }
+                srv->cv_work.notify_one();
+            }
+            if (k > 0) run_batch(srv, slot, batch, 0, batch.size(), start, results);
         }
         {
             std::lock_guard<std::mutex> lock(srv->mu);
@@ -333,6 +398,7 @@ trax_status trax_server_create(trax_server **out, int device, const trax_config 
         s.max_events = opts->max_batch_events;
         s.max_hits = (uint32_t)H;
         s.trk_cap = (uint32_t)(kt * H);
+        s.pair_cap = kp * H;
         st = trax_configure(s.ctx, cfg);
         if (st == TRAX_OK)
             st = trax_reserve(s.ctx, s.max_events, srv->L, s.max_hits, &g, (uint32_t)(kp * H),
@@ -353,6 +419,7 @@ trax_status trax_server_create(trax_server **out, int device, const trax_config 
         }
     }
     srv->stats.slot_max_hits = H;
+    srv->stats.slot_max_pairs = kp * H;
     for (size_t i = 0; i < srv->slots.size(); ++i) srv->workers.emplace_back(worker_main, srv, i);
     *out = srv;
     return TRAX_OK;
@@ -467,10 +534,11 @@ trax_status trax_server_reset_stats(trax_server *srv)
 {
     if (!srv) return TRAX_ERR_BAD_ARG;
     std::lock_guard<std::mutex> lock(srv->mu);
-    const uint64_t H = srv->stats.slot_max_hits;
+    const uint64_t H = srv->stats.slot_max_hits, PC = srv->stats.slot_max_pairs;
     const uint64_t sub = srv->stats.submitted, ev = srv->stats.events;
     srv->stats = trax_server_stats{};
     srv->stats.slot_max_hits = H;
+    srv->stats.slot_max_pairs = PC;
     srv->stats.submitted = sub - ev;
     srv->latencies_ns.clear();
     srv->first_arrival = UINT64_MAX;

@@ -93,6 +93,7 @@ _SIGS = {
                                           C.c_void_p]),
     "trax_prefix_sum_noalloc_error": (C.c_char_p, []),
     "trax_prefix_sum_noalloc_status": (C.c_int, [C.c_void_p]),
+    "trax_count_pairs_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "trax_selftest_lookback_timeout": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
                                                  C.c_uint32]),
     "trax_reset_counts": (C.c_int, [C.c_void_p]),
