@@ -78,8 +78,12 @@ def test_pair_bound_defers_instead_of_splitting(gpu_ctx):
 
 def test_candidate_overflow_still_splits(gpu_ctx):
     """The candidate capacity is only checked on the device: a batch whose
-    candidates overflow splits in halves and reruns, results unchanged."""
-    w = small_stream_workload()
+    candidates overflow splits in halves and reruns, results unchanged.
+    Pile-up up to 60 makes about 3 candidates per hit, against a capacity
+    of one per hit of the 12 events (which the densest event alone fits)."""
+    w0 = gen.WORKLOADS["stream-pileup-u200"]
+    w = gen.Workload("stream-pileup-u60", 5, w0.n_layers, w0.noise, w0.pt_range,
+                     w0.n_sectors_z, w0.n_sectors_phi, w0.n_triplets, pileup_uniform=60)
     events = [gen.generate_batch(w, 1, first_event=200 + i) for i in range(12)]
     cfg = w.config()
     p = Pipeline(gpu_ctx, cfg, w.grid(1), 1, max(e.n_hits for e in events) + 1,
