@@ -206,11 +206,17 @@ float trax_min_radius_curvature(float min_pt, float bz);
  * sweep each outer hit's candidates with the whole warp, replaying the count
  * sweep's ballots for the store (1) or sweeping twice (0).  Sparse events
  * favour walking and pair_record 3, dense (pile-up) events the index.
- * trax_configure installs run_walk 48, index_min 16, pair_record 3. */
+ * blocks_per_sm caps the resident blocks per SM of the candidate kernels
+ * (pairs, prediction, filter: grid-stride kernels launched one wave deep);
+ * 0 launches as many as fit -- the launch shape the reference sweeps as its
+ * work-group size (TripletBuilder.cpp:345, configs' `threads`).
+ * trax_configure installs run_walk 48, index_min 16, pair_record 3,
+ * blocks_per_sm 0. */
 typedef struct trax_tuning {
     uint32_t run_walk;
     uint32_t index_min;
     uint32_t pair_record;
+    uint32_t blocks_per_sm;
 } trax_tuning;
 trax_status trax_set_tuning(trax_ctx *ctx, const trax_tuning *t);
 
@@ -610,6 +616,7 @@ typedef struct trax_server_opts {
     uint32_t pairs_per_hit;        /* capacity ratios; 0: 24 pairs, 12 candidates, */
     uint32_t candidates_per_hit;   /*   4 tracklets per hit of the batch */
     uint32_t tracklets_per_hit;
+    trax_tuning tuning;            /* installed on every slot; all zero: the default */
 } trax_server_opts;
 
 typedef struct trax_server_result {

@@ -12,8 +12,8 @@ class _FakeCtx:
         self.tuning = None
         self.history = []
 
-    def set_tuning(self, run_walk, index_min, pair_record):
-        self.tuning = (run_walk, index_min, pair_record)
+    def set_tuning(self, run_walk, index_min, pair_record, blocks_per_sm=0):
+        self.tuning = (run_walk, index_min, pair_record, blocks_per_sm)
         self.history.append(self.tuning)
 
 
@@ -33,25 +33,39 @@ def _tune(monkeypatch, table, default=10.0):
     return ctx, p, best, timings
 
 
-def test_tune_walk_times_every_walk_then_the_pair_kernels_at_the_best(monkeypatch):
-    table = {(96, 32, 3): 2.0, (96, 32, 2): 1.5, (96, 32, 1): 3.0, (96, 32, 0): 4.0}
+def test_tune_walk_times_every_walk_then_the_pair_kernels_then_the_launch_shape(monkeypatch):
+    table = {(96, 32, 3, 0): 2.0, (96, 32, 2, 0): 1.5, (96, 32, 1, 0): 3.0,
+             (96, 32, 0, 0): 4.0, (96, 32, 2, 3): 1.2}
     ctx, p, best, timings = _tune(monkeypatch, table)
     assert p.staged == "b"
-    walks = [(*c, 3) for c in autotune.WALK_CANDIDATES]
+    walks = [(*c, 3, 0) for c in autotune.WALK_CANDIDATES]
     assert ctx.history[:len(walks)] == walks
     # the other pair kernels run only at the best walk, in the documented order
-    assert ctx.history[len(walks):len(walks) + 3] == [(96, 32, 2), (96, 32, 1), (96, 32, 0)]
-    assert best == (96, 32, 2)
+    n = len(walks)
+    assert ctx.history[n:n + 3] == [(96, 32, 2, 0), (96, 32, 1, 0), (96, 32, 0, 0)]
+    # then fewer resident blocks per SM at the best of those
+    assert ctx.history[n + 3:n + 3 + len(autotune.BLOCK_CAPS)] == \
+        [(96, 32, 2, c) for c in autotune.BLOCK_CAPS]
+    assert best == (96, 32, 2, 3)
     assert ctx.tuning == best  # installed last
-    assert len(timings) == len(walks) + 3
+    assert len(timings) == n + 3 + len(autotune.BLOCK_CAPS)
 
 
 def test_tune_walk_keeps_the_split_pair_stage_when_it_is_fastest(monkeypatch):
-    table = {(0, 16, 3): 1.0}
+    table = {(0, 16, 3, 0): 1.0}
     ctx, _, best, _ = _tune(monkeypatch, table)
-    assert best == (0, 16, 3)
-    assert ctx.tuning == (0, 16, 3)
-    assert ctx.history[-4:-1] == [(0, 16, 2), (0, 16, 1), (0, 16, 0)]
+    assert best == (0, 16, 3, 0)
+    assert ctx.tuning == (0, 16, 3, 0)
+    caps = len(autotune.BLOCK_CAPS)
+    assert ctx.history[-4 - caps:-1 - caps] == [(0, 16, 2, 0), (0, 16, 1, 0), (0, 16, 0, 0)]
+
+
+def test_tuning_for_picks_the_batch_class():
+    table = {"dense(>=20k)": [1 << 30, 256, 2, 3], "sparse(<5k hits/event)": [48, 16, 3, 0]}
+    assert autotune.tuning_for(table, 26_000.0) == (1 << 30, 256, 2, 3)
+    assert autotune.tuning_for(table, 3_000.0) == (48, 16, 3, 0)
+    assert autotune.tuning_for(table, 10_000.0) is None
+    assert autotune.tuning_for(None, 10_000.0) is None
 
 
 def test_density_classes():

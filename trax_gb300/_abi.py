@@ -39,7 +39,7 @@ class TraxConfig(C.Structure):
 
 class TraxTuning(C.Structure):
     _fields_ = [("run_walk", C.c_uint32), ("index_min", C.c_uint32),
-                ("pair_record", C.c_uint32)]
+                ("pair_record", C.c_uint32), ("blocks_per_sm", C.c_uint32)]
 
 
 class TraxHits(C.Structure):
@@ -118,7 +118,8 @@ class TraxServerOpts(C.Structure):
                 ("n_sectors_z", C.c_uint32), ("n_sectors_phi", C.c_uint32),
                 ("memory_budget_bytes", C.c_uint64), ("keep_results", C.c_int),
                 ("max_batch_hits", C.c_uint32), ("pairs_per_hit", C.c_uint32),
-                ("candidates_per_hit", C.c_uint32), ("tracklets_per_hit", C.c_uint32)]
+                ("candidates_per_hit", C.c_uint32), ("tracklets_per_hit", C.c_uint32),
+                ("tuning", TraxTuning)]
 
 
 class TraxServerResult(C.Structure):

@@ -1,10 +1,12 @@
 """Autotuner for the seeding pipeline.
 
-Two knobs, tuned differently:
-- how the candidate kernels visit a window (trax_set_tuning: walk runs of
-  cells or search a per-cell z index; replay the pair stage's count ballots or
-  sweep twice).  Results never depend on it, so tune_walk() simply times the
-  candidates on the resident batch and keeps the fastest.
+Two kinds of knob, tuned differently:
+- how the candidate kernels visit a window and how they are launched
+  (trax_set_tuning: walk runs of cells or search a per-cell z index; which
+  pair kernels run; how many blocks per SM the candidate kernels keep
+  resident -- the launch shape the reference sweeps as its work-group size).
+  Results never depend on them, so tune_walk() simply times the candidates on
+  the resident batch and keeps the fastest.
 - the grid granularity (z bins x phi bins).  It changes which candidates the
   reference visits first and therefore its truncation, so a tuned grid is a
   different (but equally reference-defined) configuration; sweep_grids()
@@ -22,6 +24,8 @@ from .ops import Pipeline
 from .runtime import Context
 
 WALK_CANDIDATES = ((1 << 30, 256), (96, 256), (96, 32), (48, 16), (24, 8), (0, 16), (0, 0))
+# resident blocks per SM of the candidate kernels (0: as many as fit)
+BLOCK_CAPS = (4, 3, 2)
 GRID_Z = (8, 16, 32, 64)
 GRID_PHI = (16, 32, 64, 128)
 TIMER_A, TIMER_B = 56, 57
@@ -41,24 +45,39 @@ def time_staged(ctx: Context, p: Pipeline, reps: int) -> float:
 
 
 def tune_walk(ctx: Context, p: Pipeline, batch: gen.EventBatch, reps=5,
-              candidates=WALK_CANDIDATES):
+              candidates=WALK_CANDIDATES, block_caps=BLOCK_CAPS):
     """Stages `batch`, times each (run_walk, index_min) with the split
     one-outer-hit-per-lane pair stage, then the best of them with the other
     pair kernels (one outer hit per lane with look-back, the warp sweep
-    replaying its ballots, the warp sweep twice), and installs the fastest
-    (run_walk, index_min, pair_record)."""
+    replaying its ballots, the warp sweep twice), then the best of those with
+    fewer resident blocks per SM, and installs the fastest
+    (run_walk, index_min, pair_record, blocks_per_sm)."""
     p.stage(batch)
     timings = {}
     for cand in candidates:
-        ctx.set_tuning(*cand, 3)
-        timings[(*cand, 3)] = time_staged(ctx, p, reps)
+        ctx.set_tuning(*cand, 3, 0)
+        timings[(*cand, 3, 0)] = time_staged(ctx, p, reps)
     best = min(timings, key=timings.get)
     for rec in (2, 1, 0):
-        ctx.set_tuning(best[0], best[1], rec)
-        timings[(best[0], best[1], rec)] = time_staged(ctx, p, reps)
+        ctx.set_tuning(best[0], best[1], rec, 0)
+        timings[(best[0], best[1], rec, 0)] = time_staged(ctx, p, reps)
+    best = min(timings, key=timings.get)
+    for cap in block_caps:
+        t = (best[0], best[1], best[2], cap)
+        ctx.set_tuning(*t)
+        timings[t] = time_staged(ctx, p, reps)
     best = min(timings, key=timings.get)
     ctx.set_tuning(*best)
     return best, timings
+
+
+def tuning_for(table, hits_per_event: float):
+    """The tuning `table` (density class -> tuning tuple, as autotune()
+    reports under "walk") holds for a batch of this density, or None."""
+    if not table:
+        return None
+    t = table.get(density_class(hits_per_event))
+    return tuple(t) if t is not None else None
 
 
 def density_class(hits_per_event: float) -> str:
@@ -99,11 +118,14 @@ def sweep_grids(ctx: Context, w: gen.Workload, batch: gen.EventBatch, grids=None
 
 
 def autotune(ctx: Context, w: gen.Workload, batches, grids=None, reps=3):
-    """Best grid per hit-density class over the given sample batches."""
+    """Best grid and tuning per hit-density class over the given sample
+    batches.  The "tuning" of each class is what Pipeline(tuning_by_class=)
+    and Server(tuning=) apply."""
     out = {}
     for b in batches:
         cls = density_class(b.n_hits / max(1, b.n_events))
         rows = sweep_grids(ctx, w, b, grids=grids, reps=reps)
         out[cls] = {"hits_per_event": round(b.n_hits / max(1, b.n_events), 1),
-                    "events": b.n_events, "best": rows[0] if rows else None, "sweep": rows}
+                    "events": b.n_events, "best": rows[0] if rows else None, "sweep": rows,
+                    "tuning": rows[0]["walk"] if rows else None}
     return out

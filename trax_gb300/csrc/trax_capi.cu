@@ -89,6 +89,11 @@ struct trax_ctx {
     DevBuf xyzp;  /* packed (x, y, z, phi) of the sorted hits */
     cudaEvent_t timers[kTimerSlots] = {};
     int blk_pair = 0, blk_pair0 = 0, blk_pair_lane = 0, blk_pair_count = 0, blk_pair_store = 0, blk_sector = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
+    /* resident blocks per SM that fit, per candidate kernel (occupancy), and
+     * the tuning's cap on them (0: none) */
+    int occ_pair = 0, occ_pair0 = 0, occ_pair_lane = 0, occ_pair_count = 0, occ_pair_store = 0,
+        occ_sector = 0, occ_pred = 0, occ_filter = 0, occ_pstore = 0, occ_fstore = 0;
+    uint32_t blocks_cap = 0;
     int blk_pstore = 0, blk_fstore = 0;  /* the store passes: their own occupancy */
 
     /* batched pipeline */
@@ -238,6 +243,27 @@ trax_status check_grid(trax_ctx *ctx, const trax_grid_cfg *g, bool need_cfg = tr
             return fail(ctx, TRAX_ERR_BAD_ARG, "layer triplet uses a layer outside the grid");
     }
     return TRAX_OK;
+}
+
+/* Grid sizes of the candidate kernels: the blocks per SM that fit, capped
+ * by the tuning's blocks_per_sm. */
+void apply_launch_cap(trax_ctx *ctx)
+{
+    auto grid = [&](int occ) {
+        int b = std::max(occ, 1);
+        if (ctx->blocks_cap) b = std::min<int>(b, (int)ctx->blocks_cap);
+        return ctx->sm_count * b;
+    };
+    ctx->blk_pair = grid(ctx->occ_pair);
+    ctx->blk_pair0 = grid(ctx->occ_pair0);
+    ctx->blk_pair_lane = grid(ctx->occ_pair_lane);
+    ctx->blk_pair_count = grid(ctx->occ_pair_count);
+    ctx->blk_pair_store = grid(ctx->occ_pair_store);
+    ctx->blk_sector = grid(ctx->occ_sector);
+    ctx->blk_pred = grid(ctx->occ_pred);
+    ctx->blk_filter = grid(ctx->occ_filter);
+    ctx->blk_pstore = grid(ctx->occ_pstore);
+    ctx->blk_fstore = grid(ctx->occ_fstore);
 }
 
 /* Launch plan of k_grid_build for C cells of nphi + 1 columns and segments
@@ -851,28 +877,19 @@ trax_status trax_ctx_create(trax_ctx **out, int device)
     if ((e = cudaFuncSetAttribute(k_grid_build<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)ctx->smem_optin)) != cudaSuccess) return bail(e);
     int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_fused<true>, kFusedThreads, 0);
-    ctx->blk_pair = ctx->sm_count * std::max(b, 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_fused<false>, kFusedThreads, 0);
-    ctx->blk_pair0 = ctx->sm_count * std::max(b, 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_lane, kFusedThreads, 0);
-    ctx->blk_pair_lane = ctx->sm_count * std::max(b, 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_count_lane, kFusedThreads, 0);
-    ctx->blk_pair_count = ctx->sm_count * std::max(b, 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_store_lane, kFusedThreads, 0);
-    ctx->blk_pair_store = ctx->sm_count * std::max(b, 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pair_sector, kFusedThreads, 0);
-    ctx->blk_sector = ctx->sm_count * std::max(b, 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_predict_count, kFusedThreads, 0);
-    ctx->blk_pred = ctx->sm_count * std::max(b, 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_filter_count, 256, 0);
-    ctx->blk_filter = ctx->sm_count * std::max(b, 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_pair, k_pair_fused<true>, kFusedThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_pair0, k_pair_fused<false>, kFusedThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_pair_lane, k_pair_lane, kFusedThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_pair_count, k_pair_count_lane, kFusedThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_pair_store, k_pair_store_lane, kFusedThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_sector, k_pair_sector, kFusedThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_pred, k_predict_count, kFusedThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_filter, k_filter_count, 256, 0);
     /* the store passes are bound by load latency and use fewer registers
      * than their count passes: a full complement of their own blocks */
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_predict_store, kFusedThreads, 0);
-    ctx->blk_pstore = ctx->sm_count * std::max(b, 1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_filter_store, 256, 0);
-    ctx->blk_fstore = ctx->sm_count * std::max(b, 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_pstore, k_predict_store, kFusedThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_fstore, k_filter_store, 256, 0);
+    apply_launch_cap(ctx);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_scan<kScanItems>, kScanThreads, 0);
     ctx->blk_scan = ctx->sm_count * std::max(b, 1);
     ctx->blk_small = ctx->sm_count * 2;
@@ -981,6 +998,8 @@ trax_status trax_set_tuning(trax_ctx *ctx, const trax_tuning *t)
     ctx->kp.run_walk = t->run_walk;
     ctx->kp.zi_min = t->index_min;
     ctx->kp.pair_record = t->pair_record;
+    ctx->blocks_cap = t->blocks_per_sm;
+    apply_launch_cap(ctx);
     drop_graphs(ctx);
     return TRAX_OK;
 }
@@ -1007,6 +1026,7 @@ trax_status trax_get_tuning(const trax_ctx *ctx, trax_tuning *t)
     t->run_walk = ctx->kp.run_walk;
     t->index_min = ctx->kp.zi_min;
     t->pair_record = ctx->kp.pair_record;
+    t->blocks_per_sm = ctx->blocks_cap;
     return TRAX_OK;
 }
 

@@ -400,6 +400,9 @@ trax_status trax_server_create(trax_server **out, int device, const trax_config 
         s.trk_cap = (uint32_t)(kt * H);
         s.pair_cap = kp * H;
         st = trax_configure(s.ctx, cfg);
+        const trax_tuning &tn = opts->tuning;
+        if (st == TRAX_OK && (tn.run_walk | tn.index_min | tn.pair_record | tn.blocks_per_sm))
+            st = trax_set_tuning(s.ctx, &tn);
         if (st == TRAX_OK)
             st = trax_reserve(s.ctx, s.max_events, srv->L, s.max_hits, &g, (uint32_t)(kp * H),
                               (uint32_t)(kc * H), s.trk_cap);

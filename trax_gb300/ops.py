@@ -346,10 +346,16 @@ class Pipeline:
     inside the chain (trax_reserve / trax_seed_batch)."""
 
     def __init__(self, ctx: Context, cfg: A.TraxConfig, grid: A.TraxGridCfg, max_events,
-                 max_hits, max_pairs, max_candidates, max_tracklets, pair_generator="beamspot"):
+                 max_hits, max_pairs, max_candidates, max_tracklets, pair_generator="beamspot",
+                 tuning_by_class=None):
+        """tuning_by_class: density class -> tuning (autotune.autotune()'s
+        per-class "tuning"); each batch then runs with its class's tuning,
+        which changes speed only."""
         self.ctx = ctx
         ctx.configure(cfg)
         ctx.set_pair_generator(pair_generator)
+        self.tuning_by_class = tuning_by_class
+        self._tuning = None
         self.n_triplets = cfg.n_layer_triplets
         self.max_tracklets = int(max_tracklets)
         self.n_layers = grid.n_layers
@@ -366,7 +372,15 @@ class Pipeline:
         self._stream_out = [None, None]
         self._inflight = {}
 
+    def _apply_tuning(self, b: EventBatch):
+        from .autotune import tuning_for
+        t = tuning_for(self.tuning_by_class, b.n_hits / max(1, b.n_events))
+        if t is not None and t != self._tuning:
+            self.ctx.set_tuning(*t)
+            self._tuning = t
+
     def _batch_struct(self, b: EventBatch):
+        self._apply_tuning(b)
         cols = [np.ascontiguousarray(c) for c in b.columns()]
         ln = np.ascontiguousarray(b.layer_nhits.reshape(-1), dtype=U32)
         self._keep = cols + [ln]
@@ -393,6 +407,8 @@ class Pipeline:
         """Streaming form (trax_submit_batch): queues `b` and returns a ticket
         at once; two batches may be in flight, each with its own pinned
         result buffers.  `b`'s arrays must stay unchanged until wait()."""
+        if not self._inflight:  # never change the tuning under a batch in flight
+            self._apply_tuning(b)
         busy = {v[3] for v in self._inflight.values()}
         free = [k for k in (0, 1) if k not in busy]
         if not free:

@@ -270,9 +270,10 @@ class Context:
         self.config = cfg
         return self
 
-    def set_tuning(self, run_walk: int, index_min: int, pair_record: int = 3):
+    def set_tuning(self, run_walk: int, index_min: int, pair_record: int = 3,
+                   blocks_per_sm: int = 0):
         self._check(self.lib.trax_set_tuning(
-            self.h, C.byref(A.TraxTuning(run_walk, index_min, pair_record))))
+            self.h, C.byref(A.TraxTuning(run_walk, index_min, pair_record, blocks_per_sm))))
 
     def set_pair_generator(self, name: str):
         """"beamspot" or "sector": the pair generator of the batched pipeline."""
@@ -281,7 +282,7 @@ class Context:
     def get_tuning(self):
         t = A.TraxTuning()
         self._check(self.lib.trax_get_tuning(self.h, C.byref(t)))
-        return int(t.run_walk), int(t.index_min), int(t.pair_record)
+        return int(t.run_walk), int(t.index_min), int(t.pair_record), int(t.blocks_per_sm)
 
     def alloc(self, n, dtype=np.uint32) -> DeviceBuffer:
         return DeviceBuffer(self, int(n) * np.dtype(dtype).itemsize, dtype)

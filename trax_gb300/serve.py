@@ -32,13 +32,17 @@ class Server:
     def __init__(self, cfg: A.TraxConfig, n_layers, n_sectors_z, n_sectors_phi, slots=2,
                  max_batch_events=256, max_event_hits=200_000, memory_budget_bytes=8 << 30,
                  keep_results=True, device=0, max_batch_hits=0, pairs_per_hit=0,
-                 candidates_per_hit=0, tracklets_per_hit=0):
+                 candidates_per_hit=0, tracklets_per_hit=0, tuning=None):
+        """tuning: (run_walk, index_min, pair_record[, blocks_per_sm]) for
+        every slot, e.g. the autotuner's pick for the stream's density class
+        (autotune.tuning_for); None keeps the default."""
         self.lib = load_library()
         self.T = cfg.n_layer_triplets
+        tn = A.TraxTuning(*[int(v) for v in tuning]) if tuning else A.TraxTuning()
         opts = A.TraxServerOpts(slots, max_batch_events, max_event_hits, n_layers, n_sectors_z,
                                 n_sectors_phi, int(memory_budget_bytes), 1 if keep_results else 0,
                                 int(max_batch_hits), int(pairs_per_hit), int(candidates_per_hit),
-                                int(tracklets_per_hit))
+                                int(tracklets_per_hit), tn)
         h = C.c_void_p()
         st = self.lib.trax_server_create(C.byref(h), device, C.byref(cfg), C.byref(opts))
         if st != 0:
