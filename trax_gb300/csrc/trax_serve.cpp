@@ -13,12 +13,16 @@
  * into hit / pair / candidate / tracklet capacities.  A worker admits the
  * arrived requests into its batch while they fit the slot's event and hit
  * capacity and -- the pair bound -- while their pair totals fit its pair
- * capacity.  A request's pair total comes from the device before it is first
- * admitted: the grid build and the pair stage's count passes run on the
- * newly arrived requests as one batch and the scanned totals come back per
- * event (trax_count_pairs_batch); they are exact, so a batch so admitted
- * never overflows its pairs.  Requests that do not fit go back to the front
- * of the queue with their totals and lead the next batch.  The candidate and
+ * capacity.  Pair totals come from the device: the grid build and the pair
+ * stage's count passes run on the requests not counted yet, as one batch,
+ * and the scanned totals come back per event (trax_count_pairs_batch); they
+ * are exact, so a batch so admitted never overflows its pairs.  Requests
+ * that do not fit go back to the front of the queue with their totals and
+ * lead the next batch.  The count costs a pass over the batch, so it runs
+ * only when the batch could come near the capacity: the counted events give
+ * kappa, the largest pairs / hits^2 seen (pairs grow with the square of an
+ * event's hit density), and a batch whose sum of 1.25 kappa hits^2 stays
+ * within the pair capacity is admitted without counting.  The candidate and
  * tracklet totals are scanned on the device before anything is stored; when
  * a batch would exceed one of those capacities the device stores nothing
  * beyond it, reports TRAX_ERR_CAPACITY with the true size, and the worker
@@ -104,6 +108,7 @@ struct trax_server {
     bool stop = false;
     uint64_t next_ticket = 1;
     std::vector<uint64_t> latencies_ns;
+    double kappa = 0.0;  /* largest pairs / hits^2 of a counted event */
     uint64_t first_arrival = UINT64_MAX, last_done = 0;
     trax_server_stats stats{};
     std::string err;
@@ -147,8 +152,14 @@ trax_status count_pairs(trax_server *srv, Slot &slot, const std::vector<Request 
     slot.event_pairs.resize(todo.size());
     const trax_status st = trax_count_pairs_batch(slot.ctx, &b, slot.event_pairs.data());
     if (st != TRAX_OK) return st;
-    for (size_t i = 0; i < todo.size(); ++i) todo[i]->pairs = slot.event_pairs[i];
+    double kappa = 0.0;
+    for (size_t i = 0; i < todo.size(); ++i) {
+        todo[i]->pairs = slot.event_pairs[i];
+        const double h = (double)todo[i]->n_hits;
+        if (h > 0) kappa = std::max(kappa, (double)todo[i]->pairs / (h * h));
+    }
     std::lock_guard<std::mutex> lock(srv->mu);
+    srv->kappa = std::max(srv->kappa, kappa);
     srv->stats.count_passes += 1;
     return TRAX_OK;
 }
@@ -252,7 +263,16 @@ void worker_main(trax_server *srv, size_t si)
             /* the pair bound: admit the longest prefix whose counted pairs
              * fit the slot; the rest leads the next batch */
             size_t k = batch.size();
-            if (count_pairs(srv, slot, batch) == TRAX_OK) {
+            double kappa, est = 0.0;
+            {
+                std::lock_guard<std::mutex> lock(srv->mu);
+                kappa = srv->kappa;
+            }
+            for (const Request *r : batch)
+                est += r->pairs != kPairsUnknown ? (double)r->pairs
+                                                 : 1.25 * kappa * (double)r->n_hits * r->n_hits;
+            const bool fits = kappa > 0.0 && est <= (double)slot.pair_cap;
+            if (!fits && count_pairs(srv, slot, batch) == TRAX_OK) {
                 uint64_t pairs = 0;
                 k = 0;
                 while (k < batch.size() && pairs + batch[k]->pairs <= slot.pair_cap)
