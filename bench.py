@@ -328,20 +328,24 @@ def parity_check(b, w, got_trk, got_off, n_events, threads):
             "tracklets_checked": int(k), "against": "CPU oracle (pinned to the reference kernels)"}
 
 
-def cpu_events_per_s(b, w, seconds, threads):
-    """The oracle on a bounded sample of b (about `seconds` of CPU work)."""
-    import oracle
-    cfg = w.config()
+def cpu_events_per_s(b, w, seconds, threads, runner=None):
+    """A CPU implementation on a bounded sample of b (about `seconds` of CPU
+    work): `runner(sample, w)` (the reference's kernels on the host, from
+    reference_runner), else the oracle."""
+    if runner is None:
+        import oracle
+        runner = lambda s, w_: oracle.run(s, w_.config(), w_.grid(s.n_events), 4, 256,
+                                          threads)["stats"]
     t0 = time.perf_counter()
     probe = b.slice_events(0, min(2, b.n_events))
-    oracle.run(probe, cfg, w.grid(probe.n_events), 4, 256, threads)
+    runner(probe, w)
     dt = max(time.perf_counter() - t0, 1e-3)
     n = int(max(1, min(b.n_events, probe.n_events * seconds / dt)))
     sample = b.slice_events(0, n)
     t0 = time.perf_counter()
-    r = oracle.run(sample, cfg, w.grid(n), 4, 256, threads)
+    stats = runner(sample, w)
     dt = time.perf_counter() - t0
-    return n / dt, n, dt, r["stats"]
+    return n / dt, n, dt, stats
 
 
 # --------------------------------------------------------------------------
@@ -792,12 +796,21 @@ def run_ours(args, dist):
     # ---- CPU baseline (rank 0, N=1 only) ----------------------------------
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        v, n, dt, _ = cpu_events_per_s(b, w, args.cpu_seconds, threads)
-        v1, n1, dt1, _ = cpu_events_per_s(b, w, max(2.0, args.cpu_seconds / 2), 1)
-        cpu = {"value": round(v, 3), "unit": "events/s", "cores": threads, "kind": "port",
-               "sample": f"first {n} events of the batch, {dt:.1f} s, OpenMP oracle",
+        kind, runner = reference_runner(threads)
+        v, n, dt, _ = cpu_events_per_s(b, w, args.cpu_seconds, threads, runner)
+        v1, n1, dt1, _ = cpu_events_per_s(b, w, max(2.0, args.cpu_seconds / 2), 1,
+                                          reference_runner(1)[1])
+        what = ("the reference's OpenCL kernels compiled for the host (oracle/_ref), "
+                "work-groups spread over the threads" if kind == "reference"
+                else "OpenMP oracle")
+        cpu = {"value": round(v, 3), "unit": "events/s", "cores": threads, "kind": kind,
+               "sample": f"first {n} events of the batch, {dt:.1f} s, {what}",
                "one_thread": {"value": round(v1, 3), "cores": 1,
                               "sample": f"first {n1} events, {dt1:.1f} s"}}
+        if kind == "reference":
+            vp, np_, dtp, _ = cpu_events_per_s(b, w, max(2.0, args.cpu_seconds / 2), threads)
+            cpu["port"] = {"value": round(vp, 3), "cores": threads,
+                           "sample": f"first {np_} events, {dtp:.1f} s, OpenMP oracle"}
 
     clocks = clk.summary()
     if dist.rank == 0:
