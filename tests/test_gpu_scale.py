@@ -133,3 +133,38 @@ def test_grid_build_in_row_bands_equals_oracle(gpu_ctx, zp, zscale):
     hits, g, _, _, _ = build_triplets(gpu_ctx, b, w.config(), zp[0], zp[1])
     assert np.array_equal(g.download(), r["grid"])
     assert np.array_equal(hits.download()["orig"], r["sorted_orig"])
+
+
+@pytest.mark.parametrize("name,n_ev,sigma_z", [("pileup200", 16, None),
+                                               ("multimuon-1000trk", 2, 4.0),
+                                               ("multimuon-1000trk", 2, 30.0)])
+def test_unindexed_walks_and_wide_windows_equal_oracle(gpu_ctx, name, n_ev, sigma_z):
+    """Walks that never search a cell's z index (index_min 256), contiguous
+    over whole runs or cell by cell.  A z window of 30 cm passes nearly every
+    hit of a 50 cm row through the half-precision screen, so every screen
+    step has 8 survivors and most pairs emit more candidates than a store
+    record carries (the store pass walks them); the counts, the truncation
+    and the tracklets equal the oracle's."""
+    w = gen.WORKLOADS[name]
+    b = gen.generate_batch(w, n_ev, first_event=4000)
+    cfg = w.config()
+    if sigma_z is not None:
+        for i in range(cfg.n_layer_triplets):
+            cfg.triplets[i].sigma_z = sigma_z
+    r = oracle.run(b, cfg, w.grid(n_ev), 4, n_threads=1, omp_threads=16)
+    assert r["stats"]["status"] == 0
+    want = oracle.canonical(r)["tracklets"]
+    N = b.n_hits
+    p = Pipeline(gpu_ctx, cfg, w.grid(n_ev), n_ev, N, 48 * N + 4096, 160 * N + 4096, 8 * N + 4096)
+    try:
+        for rw, rec in ((1 << 30, 2), (96, 3), (0, 1)):
+            gpu_ctx.set_tuning(rw, 256, rec)
+            trk, off, counts = p.seed(b)
+            assert counts["status"] == 0
+            assert np.array_equal(trk, want), rw
+            assert np.array_equal(off, r["trk_offsets"])
+            assert counts["n_candidates"] == r["stats"]["cands"]
+            assert counts["cand_slots"] == r["stats"]["cand_slots"]
+            assert counts["cand_truncated"] == r["stats"]["cand_truncated"]
+    finally:
+        gpu_ctx.set_tuning(48, 16, 3)
