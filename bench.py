@@ -54,7 +54,7 @@ HEADLINE = "pileup200"
 # the high-pile-up configuration the autotuner's choice (its sweep over
 # {8..64} x {16..128} on pile-up-200 events picks 64 x 128; the bench's
 # 'autotune' section repeats the sweep and reports whether it still does)
-TUNED_GRID = {"pileup200": (64, 128)}
+TUNED_GRID = {"pileup200": (256, 192)}
 # (workload, events per launch) measured beside the headline
 SECTIONS = (("pileup50-batch100", 100), ("multimuon-1000trk", 2048))
 # capacities per hit (pairs, candidates, tracklets) of the first sizing run
@@ -547,13 +547,14 @@ def measure_section(ctx, w, B, args, dist, threads):
 
 
 def run_autotune(args, ctx):
-    """Config 4: pile-up-200 events, grid sweep {8..64} x {16..128} with the
+    """Config 4: pile-up-200 events, grid sweep {8..256} x {16..192} with the
     walk tuned per grid, the plain per-event form at the best grid."""
     from trax_gb300 import gen
-    from trax_gb300.autotune import sweep_grids, density_class, GRID_Z, GRID_PHI
+    from trax_gb300.autotune import sweep_grids, density_class, GRID_Z, GRID_PHI, MAX_CELLS
     w = gen.WORKLOADS["pileup200"]
     b = gen.generate_batch(w, args.autotune_events)
-    grids = [(z, ph) for z in GRID_Z for ph in GRID_PHI] + [(12, 32)]
+    grids = [(z, ph) for z in GRID_Z for ph in GRID_PHI if (z + 1) * (ph + 1) <= MAX_CELLS]
+    grids.append((12, 32))
     t0 = time.perf_counter()
     rows = sweep_grids(ctx, w, b, grids=grids, reps=3)
     best = rows[0]

@@ -59,7 +59,7 @@ def test_pileup200_64_events_streaming_equals_oracle(gpu_ctx):
     assert np.array_equal(off1, want_off)
 
 
-@pytest.mark.parametrize("zp", [(64, 64), (64, 128), (32, 64)])
+@pytest.mark.parametrize("zp", [(64, 64), (64, 128), (32, 64), (256, 192), (128, 128)])
 def test_autotuned_grids_equal_oracle(gpu_ctx, zp):
     """The grids the autotuner selects on pile-up 200 (the truncated
     candidate set depends on the grid, so the oracle runs at the same one),

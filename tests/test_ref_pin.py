@@ -99,7 +99,7 @@ def test_sector_pair_generator(name, n_events, n_threads):
     assert_same(o, r)
 
 
-@pytest.mark.parametrize("zp", [(8, 16), (64, 128), (64, 64)])
+@pytest.mark.parametrize("zp", [(8, 16), (64, 128), (64, 64), (256, 192)])
 def test_other_grids(zp):
     """Grid granularities the autotuner searches."""
     w, b, cfg, _ = batch_for("multimuon-1000trk", 1)

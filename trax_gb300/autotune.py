@@ -26,8 +26,10 @@ from .runtime import Context
 WALK_CANDIDATES = ((1 << 30, 256), (96, 256), (96, 32), (48, 16), (24, 8), (0, 16), (0, 0))
 # resident blocks per SM of the candidate kernels (0: as many as fit)
 BLOCK_CAPS = (4, 3, 2)
-GRID_Z = (8, 16, 32, 64)
-GRID_PHI = (16, 32, 64, 128)
+GRID_Z = (8, 16, 32, 64, 128, 256)
+GRID_PHI = (16, 32, 64, 128, 192)
+# cells per layer the library accepts ((n_sectors_z + 1) * (n_sectors_phi + 1))
+MAX_CELLS = 65536
 TIMER_A, TIMER_B = 56, 57
 
 
@@ -92,7 +94,7 @@ def sweep_grids(ctx: Context, w: gen.Workload, batch: gen.EventBatch, grids=None
                 caps=(80, 80, 8)):
     """events/s of the batched pipeline at each grid, with the walk tuned per
     grid.  Returns a list of dicts sorted by events/s (best first)."""
-    grids = grids or [(z, p) for z in GRID_Z for p in GRID_PHI]
+    grids = grids or [(z, p) for z in GRID_Z for p in GRID_PHI if (z + 1) * (p + 1) <= MAX_CELLS]
     N = batch.n_hits
     rows = []
     for nz, nphi in grids:

@@ -969,6 +969,7 @@ trax_status trax_configure(trax_ctx *ctx, const trax_config *cfg)
         kp.sigma_phi[i] = t.sigma_phi; kp.tip[i] = t.tip_cut; kp.z0[i] = t.z0;
         kp.spread_z[i] = t.pair_spread_z;
         kp.spread_phi[i] = t.pair_spread_phi;
+        trax_dphi_screen_bounds(t.dphi_cut, &kp.dphi_tlo[i], &kp.dphi_thi[i]);
     }
     for (uint32_t l = 0; l < kMaxLayers; ++l) {
         kp.rmin[l] = l < cfg->n_geom_layers ? cfg->min_radius[l] : 0.0f;

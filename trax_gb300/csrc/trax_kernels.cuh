@@ -42,6 +42,8 @@ struct KParams {
     uint32_t l1[kMaxLT], l2[kMaxLT], l3[kMaxLT];
     float dtheta[kMaxLT], sigma_z[kMaxLT], dphi[kMaxLT], sigma_phi[kMaxLT];
     float tip[kMaxLT], z0[kMaxLT];
+    /* outward-rounded tan(dphi -/+ margin) of trax_dphi_screen; thi < 0: screen off */
+    float dphi_tlo[kMaxLT], dphi_thi[kMaxLT];
     uint32_t spread_z[kMaxLT], spread_phi[kMaxLT];
     float rmin[kMaxLayers], rmax[kMaxLayers];
     /* acos(r / (2 * minRadiusCurvature)) of each layer's min / max radius:
@@ -2003,6 +2005,9 @@ __device__ __forceinline__ bool filter_phi_cut(const KParams &kp, uint32_t lt, c
     const float x1 = h1.x, y1 = h1.y;
     const float x2 = h2.x, y2 = h2.y;
     const float x3 = h3.x, y3 = h3.y;
+    const int screened = trax_dphi_screen(x2 - x1, y2 - y1, x3 - x2, y3 - y2, kp.dphi_tlo[lt],
+                                          kp.dphi_thi[lt]);
+    if (screened >= 0) return screened != 0;
     const float angle1 = trax_atan2f((y2 - y1), (x2 - x1));
     const float angle2 = trax_atan2f((y3 - y2), (x3 - x2));
     float delta = angle2 - angle1;

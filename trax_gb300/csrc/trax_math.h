@@ -194,6 +194,59 @@ TRAX_HD float trax_floor_div(float x, float d, float inv_d)
     return floorf(x / d);
 }
 
+/*
+ * The filter's dphi cut (TripletThetaPhiFilter.h:86-99) decided without its
+ * two atan2 where the answer is certain.  The cut compares
+ *   delta = wrap(trax_atan2f(dy2, dx2) - trax_atan2f(dy1, dx1))
+ * with dphi.  The true angle phi from d1 = (dx1, dy1) to d2 = (dx2, dy2) is
+ * atan2(cross, dot), and |delta - phi| < 3e-6: trax_atan2f is within 5e-7 of
+ * atan2 (1.1 ulp polynomial on [0, 1], the division and the quadrant
+ * steps), and the subtraction, the wrap by 2 * (float)pi and their roundings
+ * add less than 8e-7.  cross and dot in float are each within
+ * 2^-22 |d1||d2| of exact, and (cross, dot) has length |d1||d2|, so the
+ * float pair's angle psi is within 4e-7 of phi.  With
+ *   tlo <= tan(dphi - mu), thi >= tan(dphi + mu), mu = 2e-5
+ * (each rounded outward on the host; set only for 4 mu < dphi <= 1, so that
+ * 2^-24 thi stays below 1e-7):
+ *   d <= 0                  |psi| >= pi/2: fails;
+ *   |c| <= RN(tlo * d)      |psi| <= dphi - mu + 2^-24 tlo: passes;
+ *   |c| >  RN(thi * d)      |psi| >= dphi + mu - 2^-24 thi: fails;
+ * and otherwise the caller evaluates the cut itself (-1), as it does when
+ * thi < 0 (screen off), for NaN or infinite input, and for vectors whose
+ * 1-norm is outside [2^-40, 2^60] (no product can overflow, and underflow
+ * errors stay far below 2^-22 |d1||d2|).  Returns 1 (passes), 0 (fails) or -1.
+ */
+#define TRAX_DPHI_SCREEN_MARGIN 2e-5
+TRAX_HD int trax_dphi_screen(float dx1, float dy1, float dx2, float dy2, float tlo, float thi)
+{
+    const float n1 = fabsf(dx1) + fabsf(dy1), n2 = fabsf(dx2) + fabsf(dy2);
+    if (!(thi >= 0.0f && n1 >= 0x1p-40f && n2 >= 0x1p-40f && n1 <= 0x1p60f && n2 <= 0x1p60f))
+        return -1;
+    const float c = dx1 * dy2 - dy1 * dx2;
+    const float d = dx1 * dx2 + dy1 * dy2;
+    if (d <= 0.0f) return 0;
+    const float ac = fabsf(c);
+    if (ac <= tlo * d) return 1;
+    if (ac > thi * d) return 0;
+    return -1;
+}
+
+/* Host side: the bounds of trax_dphi_screen for the cut dphi, from the
+ * double-precision tangent rounded outward to float (thi = -1: screen off). */
+static inline void trax_dphi_screen_bounds(float dphi, float *tlo, float *thi)
+{
+    const double mu = TRAX_DPHI_SCREEN_MARGIN;
+    *tlo = -1.0f;
+    *thi = -1.0f;
+    if (!(dphi > 4 * mu && dphi <= 1.0f)) return;
+    const double lo = tan((double)dphi - mu), hi = tan((double)dphi + mu);
+    float l = (float)lo, h = (float)hi;
+    if ((double)l > lo) l = nextafterf(l, 0.0f);
+    if ((double)h < hi) h = nextafterf(h, 2.0f);
+    *tlo = l;
+    *thi = h;
+}
+
 /* GridConfig::sectorSizeZ/Phi (Grid.h:9-15), evaluated in float. */
 TRAX_HD float trax_sector_size_z(uint32_t n_sectors_z)
 {
