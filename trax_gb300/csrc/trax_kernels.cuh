@@ -2136,21 +2136,50 @@ __global__ void __launch_bounds__(256) k_filter_store(const uint2 *pairs, const 
     const uint32_t words = st->n_ftile;
     if (blockIdx.x == 0 && threadIdx.x == 0 && st->n_trk > trk_cap)
         set_fault(st, TRAX_ERR_CAPACITY, TRAX_DETAIL_TRACKLET_CAPACITY);
-    /* one mask word per warp: lane b stores candidate 32 t + b if accepted,
-     * so the candidate reads and the tracklet writes are coalesced */
+    /* 32 mask words per warp, one per lane; the accepted candidates of the
+     * 32 words are then spread over the lanes in candidate order, so the
+     * tracklet writes are coalesced however sparse the words are (a few
+     * percent of the candidates pass on pile-up events, a quarter on
+     * isolated tracks) */
     const uint32_t lane = threadIdx.x & 31;
-    const uint32_t lt_mask = lanemask_lt();
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < words; t += nw) {
-        const uint32_t m = mask[t];
-        if (!((m >> lane) & 1u)) continue;
-        const uint32_t pos = word_pos[t] + __popc(m & lt_mask);
-        if (pos >= trk_cap) continue;
-        const uint2 c = cands[t * 32 + lane];
-        const uint2 pr = pairs[c.x];
-        t1[pos] = pr.x;
-        t2[pos] = pr.y;
-        t3[pos] = c.y;
+    for (uint32_t t0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; t0 < words;
+         t0 += nw * 32) {
+        const uint32_t t = t0 + lane;
+        const uint32_t m = t < words ? mask[t] : 0u;
+        const uint32_t base = m ? word_pos[t] : 0u;
+        const uint32_t cnt = __popc(m);
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFull, incl, d);
+            if (lane >= (uint32_t)d) incl += y;
+        }
+        const uint32_t total = __shfl_sync(kFull, incl, 31);
+        for (uint32_t k0 = 0; k0 < total; k0 += 32) {
+            const uint32_t k = k0 + lane;
+            /* the word holding accepted candidate k: the lanes whose
+             * inclusive count is <= k come before it */
+            uint32_t o = 0;
+#pragma unroll
+            for (uint32_t step = 16; step; step >>= 1)
+                if (__shfl_sync(kFull, incl, o + step - 1) <= k) o += step;
+            const uint32_t mo = __shfl_sync(kFull, m, o);
+            const uint32_t before = __shfl_sync(kFull, incl - cnt, o);
+            const uint32_t pos0 = __shfl_sync(kFull, base, o);
+            if (k < total) {
+                const uint32_t r = k - before;
+                const uint32_t pos = pos0 + r;
+                const uint32_t bit = __fns(mo, 0, (int)r + 1);
+                if (pos < trk_cap) {
+                    const uint2 c = cands[(t0 + o) * 32 + bit];
+                    const uint2 pr = pairs[c.x];
+                    t1[pos] = pr.x;
+                    t2[pos] = pr.y;
+                    t3[pos] = c.y;
+                }
+            }
+        }
     }
 }
 
