@@ -524,21 +524,26 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
     const uint32_t ntile = tiles_for(ptiles, kScanItems * kScanThreads);
     if ((s = ensure(ctx, ctx->st1, (size_t)ntile * 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->ptile, (size_t)ptiles * 4)) != TRAX_OK) return s;
-    const uint32_t rec_cap = cand_cap ? cand_cap : 1;
-    /* a walking record stands for more than kPredKeep candidates */
-    const uint32_t walk_cap = rec_cap / (kPredKeep + 1) + 1;
-    if ((s = ensure(ctx, ctx->prec, ((size_t)rec_cap + walk_cap) * sizeof(PredRec))) != TRAX_OK) return s;
+    /* staged accepts (at most one per candidate), the tiles' stage offsets
+     * and the walk records (each stands for more than kPredKeep candidates) */
+    const uint32_t stage_cap = cand_cap ? cand_cap : 1;
+    const uint32_t walk_cap = stage_cap / (kPredKeep + 1) + 1;
+    const size_t stage_off = (size_t)walk_cap * sizeof(PredRec);
+    const size_t sbase_off = stage_off + (((size_t)stage_cap * 4 + 255) & ~(size_t)255);
+    if ((s = ensure(ctx, ctx->prec, sbase_off + (size_t)ptiles * 4)) != TRAX_OK) return s;
     uint32_t *cexcl = (uint32_t *)ctx->cexcl.p;
     uint32_t *ptile = (uint32_t *)ctx->ptile.p;
-    PredRec *recs = (PredRec *)ctx->prec.p;
+    PredRec *walks = (PredRec *)ctx->prec.p;
+    uint32_t *stage = (uint32_t *)((char *)ctx->prec.p + stage_off);
+    uint32_t *tile_sbase = (uint32_t *)((char *)ctx->prec.p + sbase_off);
     DevState *st = ctx->d_state;
     /* the pair total is st->n_pairs: written by the pair stage, or copied
      * from pair_offsets[G] by trax_triplet_predict */
     CK(cudaMemsetAsync(&st->n_prec, 0, 8, ctx->stream));  /* n_prec, n_pwalk */
     k_predict_count<<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
         kp, grid, h.xyzp, h.zphi, h.zh, h.event, h.layer, (const float2 *)ctx->zi.p,
-        (const uint32_t *)ctx->zp.p, pairs, &st->n_pairs, pair_cap, cexcl, ptile, recs, rec_cap,
-        walk_cap, st);
+        (const uint32_t *)ctx->zp.p, pairs, &st->n_pairs, pair_cap, cexcl, ptile, stage, stage_cap,
+        tile_sbase, walks, walk_cap, st);
     if ((s = mark(ctx, "predict")) != TRAX_OK) return s;
     CK(cudaMemsetAsync(&st->tile_ctr[1], 0, 4, ctx->stream));
     CK(cudaMemsetAsync(ctx->st1.p, 0, (size_t)ntile * 8, ctx->stream));
@@ -546,8 +551,8 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
         ptile, ptile, &st->n_ptile, ptiles, &st->n_cands, 1, (unsigned long long *)ctx->st1.p, st);
     if ((s = mark(ctx, "predict_scan")) != TRAX_OK) return s;
     k_predict_store<<<ctx->blk_pstore, kFusedThreads, 0, ctx->stream>>>(
-        kp, grid, h.zphi, h.zh, recs,
-        rec_cap, walk_cap, cexcl, ptile, &st->n_pairs, pair_cap, &st->n_cands, cands, cand_cap, st);
+        kp, grid, h.zphi, h.zh, stage, stage_cap, tile_sbase, walks, walk_cap, cexcl, ptile,
+        &st->n_pairs, pair_cap, &st->n_cands, cands, cand_cap, st);
     if ((s = mark(ctx, "predict_store")) != TRAX_OK) return s;
     k_cand_offsets<<<ctx->blk_small, 256, 0, ctx->stream>>>(pair_offsets, cexcl, ptile,
                                                             cand_offsets, kp.n_lt, pair_cap,

@@ -69,7 +69,7 @@ struct DevState {
     unsigned long long cand_truncated;
     uint32_t tile_ctr[4];    /* decoupled look-back tile tickets */
     uint32_t aux_n;          /* element count of a standalone prefix sum */
-    uint32_t n_prec;         /* prediction store records carrying their accepts */
+    uint32_t n_prec;         /* accepts the prediction count staged for the store pass */
     uint32_t n_pwalk;        /* prediction store records that walk (after them) */
     uint32_t n_ptile;        /* 32-pair tiles of the prediction count pass */
     uint32_t n_ftile;        /* 32-candidate words of the filter's accept mask */
@@ -1686,31 +1686,30 @@ __device__ __forceinline__ PredWindow pred_window(const KParams &kp, uint32_t lt
  *                     count walk over layer-3 cells (window A = the
  *                     reference's predictCount, B = predictStore), the
  *                     emitted count min(A, B) per pair, its exclusive prefix
- *                     within the pair's 32-pair tile and the tile's total,
- *                     and for every pair that emits a 32-byte record of its
- *                     store window (warp-aggregated atomic append, any order);
+ *                     within the pair's 32-pair tile and the tile's total;
+ *                     the first kPredKeep window-B accepts of each pair that
+ *                     emits go to a stage (a tile's together, in candidate
+ *                     order, warp-aggregated atomic append), and a pair with
+ *                     more accepts leaves a 32-byte record of its store
+ *                     window;
  *   k_scan            exclusive scan of the tile totals (pair order);
- *   k_predict_store   one record per thread: the first `emitted` accepts of
- *                     window B in the reference's visit order at the pair's
- *                     position (tile prefix + in-tile prefix).
- * Only pairs with candidates are walked twice, and no window is recomputed.
+ *   k_predict_store   one warp per tile copies its staged accepts to their
+ *                     positions (tile prefix + in-tile prefix); the records
+ *                     walk window B for the accepts after the first
+ *                     kPredKeep, in the reference's visit order.
+ * Only pairs with more than kPredKeep candidates are walked twice, and no
+ * window is recomputed.
  */
-constexpr int kPredKeep = 7;  /* window-B accepts a store record carries */
+constexpr int kPredKeep = 7;  /* window-B accepts staged per pair */
 
-/* 32-byte store record of a pair that emits.  A pair emitting at most
- * kPredKeep candidates carries them; any other carries its store window.
- * The store pass tells the two apart by the pair's emitted count. */
+/* 32-byte record of a pair with more than kPredKeep candidates: its store
+ * window (window B). */
 struct PredRec {
     uint32_t pair;
-    union {
-        uint32_t hit[kPredKeep];  /* the first window-B accepts in visit order */
-        struct {
-            uint32_t grid_off;    /* layer-3 grid of the pair's event */
-            uint32_t zsec;        /* zLowSector | zHighSector << 16 */
-            uint32_t psec;        /* phiLowSector | phiHighSector << 16 | wrap << 31 */
-            float zLow, zHigh, phiLow, phiHigh;  /* window B */
-        } win;
-    };
+    uint32_t grid_off;    /* layer-3 grid of the pair's event */
+    uint32_t zsec;        /* zLowSector | zHighSector << 16 */
+    uint32_t psec;        /* phiLowSector | phiHighSector << 16 | wrap << 31 */
+    float zLow, zHigh, phiLow, phiHigh;  /* window B */
 };
 static_assert(sizeof(PredRec) == 32, "a store record is one 32-byte sector");
 
@@ -1813,7 +1812,8 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
     const uint32_t *n_pairs_ptr,
     uint32_t pair_cap,
     uint32_t *in_tile,
-    uint32_t *tile_sum, PredRec *recs, uint32_t rec_cap, uint32_t walk_cap, DevState *st)
+    uint32_t *tile_sum, uint32_t *stage, uint32_t stage_cap, uint32_t *tile_sbase,
+    PredRec *walks, uint32_t walk_cap, DevState *st)
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt_mask = lanemask_lt();
@@ -1863,39 +1863,46 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
         }
         if (p < n) in_tile[p] = incl - emitted;
         if (lane == 31) tile_sum[p0 >> 5] = incl;
-        /* records that carry their accepts go to recs[0, rec_cap), records
-         * that walk to recs[rec_cap, rec_cap + walk_cap): the store pass
-         * then runs the (rare) walks on warps of their own */
-        const bool copy = emitted != 0 && emitted <= (uint32_t)kPredKeep;
-        const bool walk = emitted > (uint32_t)kPredKeep;
-        const uint32_t want = __ballot_sync(kFull, copy), wwant = __ballot_sync(kFull, walk);
-        uint32_t base = 0, wbase = 0;
-        if (lane == 0 && want) base = atomicAdd(&st->n_prec, (uint32_t)__popc(want));
-        if (lane == 0 && wwant) wbase = atomicAdd(&st->n_pwalk, (uint32_t)__popc(wwant));
-        base = __shfl_sync(kFull, base, 0);
-        wbase = __shfl_sync(kFull, wbase, 0);
-        if (copy) {
-            const uint32_t r = base + __popc(want & lt_mask);
-            if (r < rec_cap) {
-                PredRec rec;
-                rec.pair = p;
+        /* the first kPredKeep accepts of every pair that emits go to the
+         * stage: a tile's together, in candidate order, at tile_sbase */
+        const uint32_t kept = emitted < (uint32_t)kPredKeep ? emitted : (uint32_t)kPredKeep;
+        uint32_t kincl = kept;
 #pragma unroll
-                for (int q = 0; q < kPredKeep; ++q) rec.hit[q] = (uint32_t)q < emitted ? keep[q] : 0u;
-                recs[r] = rec;
-            }
-        } else if (walk) {
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFull, kincl, d);
+            if (lane >= (uint32_t)d) kincl += y;
+        }
+        const uint32_t ktotal = __shfl_sync(kFull, kincl, 31);
+        uint32_t sbase = 0;
+        if (lane == 0) {
+            if (ktotal) sbase = atomicAdd(&st->n_prec, ktotal);
+            tile_sbase[p0 >> 5] = sbase;
+        }
+        sbase = __shfl_sync(kFull, sbase, 0);
+        const uint32_t at = sbase + kincl - kept;
+#pragma unroll
+        for (uint32_t q = 0; q < (uint32_t)kPredKeep; ++q)
+            if (q < kept && at + q < stage_cap) stage[at + q] = keep[q];
+        /* a pair with more accepts also leaves its store window, for the
+         * store pass to walk on warps of its own */
+        const bool walk = emitted > (uint32_t)kPredKeep;
+        const uint32_t wwant = __ballot_sync(kFull, walk);
+        uint32_t wbase = 0;
+        if (lane == 0 && wwant) wbase = atomicAdd(&st->n_pwalk, (uint32_t)__popc(wwant));
+        wbase = __shfl_sync(kFull, wbase, 0);
+        if (walk) {
             const uint32_t r = wbase + __popc(wwant & lt_mask);
             if (r < walk_cap) {
                 PredRec rec;
                 rec.pair = p;
-                rec.win.grid_off = goff;
-                rec.win.zsec = w.zLowSector[1] | (w.zHighSector[1] << 16);
-                rec.win.psec = w.phiLowSector | (w.phiHighSector << 16) | (w.wrap << 31);
-                rec.win.zLow = w.zLow[1];
-                rec.win.zHigh = w.zHigh[1];
-                rec.win.phiLow = w.phiLow;
-                rec.win.phiHigh = w.phiHigh;
-                recs[rec_cap + r] = rec;
+                rec.grid_off = goff;
+                rec.zsec = w.zLowSector[1] | (w.zHighSector[1] << 16);
+                rec.psec = w.phiLowSector | (w.phiHighSector << 16) | (w.wrap << 31);
+                rec.zLow = w.zLow[1];
+                rec.zHigh = w.zHigh[1];
+                rec.phiLow = w.phiLow;
+                rec.phiHigh = w.phiHigh;
+                walks[r] = rec;
             }
         }
     }
@@ -1912,51 +1919,102 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
 
 __global__ void __launch_bounds__(256) k_predict_store(
     KParams kp, const uint32_t *grid, const float2 *ZP, const uint16_t *ZH,
-    const PredRec *recs, uint32_t rec_cap, uint32_t walk_cap, const uint32_t *in_tile,
-    const uint32_t *tile_prefix, const uint32_t *n_pairs_ptr, uint32_t pair_cap,
-    const uint32_t *total_ptr, uint2 *cands, uint32_t cand_cap, DevState *st)
+    const uint32_t *stage, uint32_t stage_cap, const uint32_t *tile_sbase, const PredRec *walks,
+    uint32_t walk_cap, const uint32_t *in_tile, const uint32_t *tile_prefix,
+    const uint32_t *n_pairs_ptr, uint32_t pair_cap, const uint32_t *total_ptr, uint2 *cands,
+    uint32_t cand_cap, DevState *st)
 {
-    uint32_t ncopy = st->n_prec, nwalk = st->n_pwalk;
-    if (ncopy > rec_cap) ncopy = rec_cap;
+    uint32_t nwalk = st->n_pwalk;
     if (nwalk > walk_cap) nwalk = walk_cap;
     uint32_t n = *n_pairs_ptr;
     if (n > pair_cap) n = pair_cap;
+    const uint32_t ntiles = (n + 31) / 32;
+    const uint32_t total = *total_ptr;
     const uint32_t P1 = kp.nphi + 1;
-    /* the copy records, then the walk records: consecutive threads take
-     * records of one kind, so the walks share their warps only with walks */
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < ncopy + nwalk;
+    const uint32_t lane = threadIdx.x & 31;
+    /*
+     * A warp takes 32 tiles of 32 pairs; lane i reads tile i's prefix, total
+     * and stage offset (coalesced), and the warp then copies each non-empty
+     * tile: its candidates are one run of positions and its staged accepts
+     * one run of the stage in the same order (the first kPredKeep of each
+     * pair), so it copies them one candidate per lane with coalesced stage
+     * reads and candidate writes.  The stage reads do not wait for the
+     * counts: a tile stages at most 32 * kPredKeep accepts, and the first 32
+     * are read ahead.
+     */
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t t0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; t0 < ntiles;
+         t0 += nw * 32) {
+        const uint32_t tt = t0 + lane;
+        uint32_t tp = 0, sb = 0;
+        if (tt < ntiles) {
+            tp = tile_prefix[tt];
+            sb = tile_sbase[tt];
+        }
+        uint32_t tnext = __shfl_down_sync(kFull, tp, 1);
+        if (lane == 31 || tt + 1 >= ntiles) tnext = tt + 1 < ntiles ? tile_prefix[tt + 1] : total;
+        const uint32_t ttot = tt < ntiles ? tnext - tp : 0u;
+        for (uint32_t busy = __ballot_sync(kFull, ttot != 0); busy; busy &= busy - 1) {
+            const uint32_t i = __ffs(busy) - 1;
+            const uint32_t t = t0 + i;
+            const uint32_t tpi = __shfl_sync(kFull, tp, i);
+            const uint32_t ttotal = __shfl_sync(kFull, ttot, i);
+            const uint32_t sbase = __shfl_sync(kFull, sb, i);
+            const uint32_t p = t * 32 + lane;
+            const uint32_t ahead = sbase + lane < stage_cap ? stage[sbase + lane] : 0u;
+            const uint32_t it = p < n ? in_tile[p] : ttotal;
+            uint32_t next = __shfl_down_sync(kFull, it, 1);
+            if (lane == 31) next = ttotal;
+            const uint32_t emitted = p < n ? next - it : 0u;
+            const uint32_t kept = emitted < (uint32_t)kPredKeep ? emitted : (uint32_t)kPredKeep;
+            uint32_t kincl = kept;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t y = __shfl_up_sync(kFull, kincl, d);
+                if (lane >= (uint32_t)d) kincl += y;
+            }
+            const uint32_t ktotal = __shfl_sync(kFull, kincl, 31);
+            for (uint32_t k0 = 0; k0 < ktotal; k0 += 32) {
+                const uint32_t k = k0 + lane;
+                /* the pair of staged accept k: the lanes whose inclusive
+                 * count is <= k come before it */
+                uint32_t o = 0;
+#pragma unroll
+                for (uint32_t step = 16; step; step >>= 1)
+                    if (__shfl_sync(kFull, kincl, o + step - 1) <= k) o += step;
+                const uint32_t q = k - __shfl_sync(kFull, kincl - kept, o);
+                const uint32_t at = tpi + __shfl_sync(kFull, it, o) + q;
+                if (k < ktotal && at < cand_cap && sbase + k < stage_cap)
+                    cands[at] = make_uint2(t * 32 + o, k0 == 0 ? ahead : stage[sbase + k]);
+            }
+        }
+    }
+    /* the pairs with more than kPredKeep accepts, one per thread: accepts
+     * kPredKeep .. min(A, B) - 1 of window B in the reference's visit order */
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < nwalk;
          r += gridDim.x * blockDim.x) {
-        const PredRec r0 = recs[r < ncopy ? r : rec_cap + (r - ncopy)];
-        const uint32_t p = r0.pair;
+        const PredRec rec = walks[r];
+        const uint32_t p = rec.pair;
         if (p >= n) continue;
         const uint32_t pos = tile_prefix[p >> 5] + in_tile[p];
         const uint32_t emitted =
-            (p + 1 < n ? tile_prefix[(p + 1) >> 5] + in_tile[p + 1] : *total_ptr) - pos;
-        if (emitted <= (uint32_t)kPredKeep) {
-            /* the count pass kept them: the first window-B accepts in visit
-             * order (unrolled, so the record stays in registers) */
-#pragma unroll
-            for (uint32_t q = 0; q < (uint32_t)kPredKeep; ++q)
-                if (q < emitted && pos + q < cand_cap) cands[pos + q] = make_uint2(p, r0.hit[q]);
-            continue;
-        }
-        const auto &rec = r0.win;
+            (p + 1 < n ? tile_prefix[(p + 1) >> 5] + in_tile[p + 1] : total) - pos;
         const uint32_t *lGrid3 = grid + rec.grid_off;
         const uint32_t zLowSector = rec.zsec & 0xffffu, zHighSector = rec.zsec >> 16;
         const uint32_t phiLowSector = rec.psec & 0xffffu;
         const uint32_t phiHighSector = (rec.psec >> 16) & 0x7fffu;
         const uint32_t wrap = rec.psec >> 31;
         const ZScreen scr = zscreen_make(false, 0.f, 0.f, true, rec.zLow, rec.zHigh);
-        /* the first `emitted` accepts of window B in the reference's visit
-         * order: cells in run order, hits of a cell by position -- runs of
-         * whole cells walked in position order through the z screen (no
-         * z index: its accepts would come in z order) */
+        /* cells in run order, hits of a cell by position -- runs of whole
+         * cells walked in position order through the z screen (no z index:
+         * its accepts would come in z order) */
         uint32_t written = 0;
         /* a hit of a walk that passed the screen: the exact test */
         auto store = [&](uint32_t j) {
             const float2 v = ZP[j];
             if (rec.zLow <= v.x && v.x <= rec.zHigh && phi_in(v.y, rec.phiLow, rec.phiHigh, wrap)) {
-                if (pos + written < cand_cap) cands[pos + written] = make_uint2(p, j);
+                if (written >= (uint32_t)kPredKeep && pos + written < cand_cap)
+                    cands[pos + written] = make_uint2(p, j);
                 ++written;
             }
             return written < emitted;
