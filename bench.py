@@ -54,7 +54,12 @@ HEADLINE = "pileup200"
 # the high-pile-up configuration the autotuner's choice (its sweep over
 # {8..64} x {16..128} on pile-up-200 events picks 64 x 128; the bench's
 # 'autotune' section repeats the sweep and reports whether it still does)
-TUNED_GRID = {"pileup200": (256, 192)}
+TUNED_GRID = {"pileup200": (256, 192),
+              # the streaming mix (pile-up U{0..200}) served at the grid and walk
+              # the autotuner picks for its densest events
+              "stream-pileup-u200": (256, 192)}
+# walk tuning (run_walk, index_min, pair_record) recorded with a tuned grid
+TUNED_WALK = {"stream-pileup-u200": (1 << 30, 256, 2)}
 # (workload, events per launch) measured beside the headline
 SECTIONS = (("pileup50-batch100", 100), ("multimuon-1000trk", 2048))
 # capacities per hit (pairs, candidates, tracklets) of the first sizing run
@@ -79,6 +84,11 @@ def parse(argv=None):
                     help="Poisson arrival rates (events/s) for the streaming measurement")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--serve-pool", type=int, default=128)
+    ap.add_argument("--serve-grid", default="tuned",
+                    help="ZxP bins of the serving measurement, 'tuned' or 'workload'")
+    ap.add_argument("--serve-walk", default=None,
+                    help="run_walk,index_min,pair_record of the serving slots (default: the "
+                         "tuned one where a grid is recorded, else the library default)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--autotune-events", type=int, default=32)
     ap.add_argument("--walk", default=None,
@@ -580,16 +590,22 @@ def run_serving(args):
     continuous-batching server; p50/p99 arrival-to-result latency."""
     from trax_gb300 import gen
     from trax_gb300.serve import Server, poisson_arrivals
-    w = gen.WORKLOADS["stream-pileup-u200"]
+    w = workload_at_grid(gen.WORKLOADS["stream-pileup-u200"], args.serve_grid)
+    tuning = None
+    if args.serve_walk:
+        tuning = [int(v) for v in args.serve_walk.split(",")]
+    elif args.serve_grid == "tuned" and w.name in TUNED_WALK:
+        tuning = list(TUNED_WALK[w.name])
     pool = [gen.generate_batch(w, 1, first_event=i) for i in range(args.serve_pool)]
     hits = np.array([e.n_hits for e in pool])
     out = {"workload": w.name, "grid": f"{w.n_sectors_z}x{w.n_sectors_phi}",
            "pool_events": len(pool), "hits_per_event_mean": round(float(hits.mean()), 1),
            "hits_per_event_max": int(hits.max()), "slots": 3, "max_batch_events": 256,
            "rates": []}
+    out["tuning"] = tuning
     with Server(w.config(), w.n_layers, w.n_sectors_z, w.n_sectors_phi, slots=3,
                 max_batch_events=256, max_event_hits=int(hits.max()) + 1,
-                memory_budget_bytes=24 << 30, keep_results=False) as srv:
+                memory_budget_bytes=24 << 30, keep_results=False, tuning=tuning) as srv:
         # warm-up: every slot captures its graph
         srv.replay(pool, np.arange(len(pool)) % len(pool),
                    np.full(len(pool), srv.now_ns(), dtype=np.uint64))

@@ -82,16 +82,21 @@ def test_autotuned_grids_equal_oracle(gpu_ctx, zp):
     gpu_ctx.set_tuning(48, 16, 3)
 
 
-def test_serving_stream_equals_oracle(gpu_ctx):
+@pytest.mark.parametrize("zp,tuning", [(None, None), ((256, 192), (1 << 30, 256, 2))])
+def test_serving_stream_equals_oracle(gpu_ctx, zp, tuning):
     """Events of the streaming workload (pile-up ~ U{0..200}) arriving as a
-    Poisson stream through the continuous-batching server: every event's
-    tracklets equal the oracle's for that event alone."""
+    Poisson stream through the continuous-batching server, at the workload's
+    grid and at the tuned grid and walk the benchmark serves with: every
+    event's tracklets equal the oracle's for that event alone."""
     from trax_gb300.serve import Server, poisson_arrivals
     w = gen.WORKLOADS["stream-pileup-u200"]
+    if zp is not None:
+        w = gen.Workload(w.name, w.config_id, w.n_layers, w.noise, w.pt_range, zp[0], zp[1],
+                         w.n_triplets, pileup_uniform=w.pileup_uniform)
     events = [gen.generate_batch(w, 1, first_event=300 + i) for i in range(24)]
     cfg = w.config()
     with Server(cfg, w.n_layers, w.n_sectors_z, w.n_sectors_phi, slots=3,
-                max_batch_events=8, memory_budget_bytes=6 << 30) as srv:
+                max_batch_events=8, memory_budget_bytes=6 << 30, tuning=tuning) as srv:
         t0 = srv.now_ns() + 20_000_000
         arrivals = poisson_arrivals(len(events), 2000.0, t0, seed=5)
         tickets = [srv.submit(e, int(a)) for e, a in zip(events, arrivals)]

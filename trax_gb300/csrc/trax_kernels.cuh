@@ -2123,9 +2123,14 @@ __device__ __forceinline__ bool filter_theta_fit_cut(const KParams &kp, uint32_t
  */
 /* Two phases per warp and 64 candidates: the dphi cut for all of them
  * (most candidates fail it), then the dtheta cut and the circle fit for the
- * survivors only, gathered onto consecutive lanes through shared memory so
- * that the expensive part runs on full warps.  Accept bits land in the two
- * mask words by shared-memory atomics. */
+ * survivors only, queued in shared memory and taken 32 at a time so that
+ * the expensive part runs on full warps: survivors left over from one chunk
+ * wait for the next chunk's, and a chunk's two mask words are written once
+ * its last survivor is done (at most kFiltRing chunks wait).  Accept bits
+ * land in the mask words by shared-memory atomics. */
+constexpr uint32_t kFiltRing = 4;     /* chunks whose survivors may wait in the queue */
+constexpr uint32_t kFiltQueue = 96;   /* survivors waiting: < 32 left over + one chunk */
+
 __global__ void __launch_bounds__(256) k_filter_count(KParams kp, const float4 *XYZP,
                                                       const uint32_t *LAYER,
                                                       const uint2 *pairs, const uint2 *cands,
@@ -2133,8 +2138,8 @@ __global__ void __launch_bounds__(256) k_filter_count(KParams kp, const float4 *
                                                       uint32_t cand_cap, uint32_t *mask,
                                                       uint32_t *word_count, DevState *st)
 {
-    __shared__ uint4 s_q[kFusedThreads / 32][64];
-    __shared__ uint32_t s_w[kFusedThreads / 32][2];
+    __shared__ uint4 s_q[kFusedThreads / 32][kFiltQueue];
+    __shared__ uint32_t s_w[kFusedThreads / 32][kFiltRing][2];
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt_mask = lanemask_lt();
     const uint32_t wib = threadIdx.x >> 5;
@@ -2143,9 +2148,59 @@ __global__ void __launch_bounds__(256) k_filter_count(KParams kp, const float4 *
     if (blockIdx.x == 0 && threadIdx.x == 0) st->n_ftile = (n + 31) / 32;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    /* warp-uniform bookkeeping: survivors queued [0, qn); chunks in the ring
+     * slots [oldest, oldest + pending), each with its first candidate and
+     * the running index one past its last survivor; done = survivors
+     * finished so far (running index) */
+    uint32_t qn = 0, pending = 0, oldest = 0, done = 0, queued = 0;
+    uint32_t ring_i0 = 0, ring_end = 0;  /* lane r < kFiltRing holds slot r */
+    /* the dtheta cut and circle fit for the first m queued survivors */
+    auto round = [&](uint32_t m) {
+        if (lane < m) {
+            const uint4 e = s_q[wib][lane];
+            const uint32_t lt = e.w & 0xffu, slot = (e.w >> 8) & 0xffu, r = e.w >> 16;
+            if (filter_theta_fit_cut(kp, lt, XYZP[e.x], XYZP[e.y], XYZP[e.z]))
+                atomicOr(&s_w[wib][r][slot >> 5], 1u << (slot & 31));
+        }
+        __syncwarp();
+        /* move the rest to the front */
+        const uint32_t rest = qn - m;
+        uint4 keep0 = make_uint4(0, 0, 0, 0), keep1 = keep0;
+        if (lane < rest) keep0 = s_q[wib][m + lane];
+        if (lane + 32 < rest) keep1 = s_q[wib][m + 32 + lane];
+        __syncwarp();
+        if (lane < rest) s_q[wib][lane] = keep0;
+        if (lane + 32 < rest) s_q[wib][32 + lane] = keep1;
+        __syncwarp();
+        qn = rest;
+        done += m;
+    };
+    /* writes the mask words of the finished chunks, oldest first */
+    auto retire = [&]() {
+        while (pending) {
+            const uint32_t end = __shfl_sync(kFull, ring_end, oldest);
+            if (end > done) break;
+            const uint32_t i0 = __shfl_sync(kFull, ring_i0, oldest);
+            if (lane < 2 && i0 + lane * 32 < n) {
+                const uint32_t m = s_w[wib][oldest][lane];
+                mask[(i0 >> 5) + lane] = m;
+                word_count[(i0 >> 5) + lane] = __popc(m);
+            }
+            oldest = (oldest + 1) % kFiltRing;
+            --pending;
+        }
+        __syncwarp();
+    };
     for (uint32_t i0 = gw * 64; i0 < n; i0 += nw * 64) {
-        if (lane < 2) s_w[wib][lane] = 0;
-        uint32_t nsurv = 0;
+        /* a free ring slot for this chunk: finish queued survivors until the
+         * oldest chunk retires */
+        while (pending == kFiltRing) {
+            round(qn < 32 ? qn : 32);
+            retire();
+        }
+        const uint32_t r = (oldest + pending) % kFiltRing;
+        if (lane < 2) s_w[wib][r][lane] = 0;
+        __syncwarp();
 #pragma unroll
         for (int half = 0; half < 2; ++half) {
             const uint32_t i = i0 + half * 32 + lane;
@@ -2159,29 +2214,27 @@ __global__ void __launch_bounds__(256) k_filter_count(KParams kp, const float4 *
                     set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_BAD_TRIPLET_INDEX);
                 } else {
                     pass = filter_phi_cut(kp, lt, XYZP[pr.x], XYZP[pr.y], XYZP[c.y]);
-                    e = make_uint4(pr.x, pr.y, c.y, lt | ((uint32_t)(half * 32) + lane) << 8);
+                    e = make_uint4(pr.x, pr.y, c.y,
+                                   lt | ((uint32_t)(half * 32) + lane) << 8 | r << 16);
                 }
             }
             const uint32_t b = __ballot_sync(kFull, pass);
-            if (pass) s_q[wib][nsurv + __popc(b & lt_mask)] = e;
-            nsurv += __popc(b);
+            if (pass) s_q[wib][qn + __popc(b & lt_mask)] = e;
+            qn += __popc(b);
+            queued += __popc(b);
         }
         __syncwarp();
-        for (uint32_t r = 0; r < nsurv; r += 32) {
-            if (r + lane < nsurv) {
-                const uint4 e = s_q[wib][r + lane];
-                const uint32_t lt = e.w & 0xffu, slot = e.w >> 8;
-                if (filter_theta_fit_cut(kp, lt, XYZP[e.x], XYZP[e.y], XYZP[e.z]))
-                    atomicOr(&s_w[wib][slot >> 5], 1u << (slot & 31));
-            }
+        if (lane == r) {
+            ring_i0 = i0;
+            ring_end = queued;
         }
-        __syncwarp();
-        if (lane < 2 && i0 + lane * 32 < n) {
-            const uint32_t m = s_w[wib][lane];
-            mask[(i0 >> 5) + lane] = m;
-            word_count[(i0 >> 5) + lane] = __popc(m);
-        }
-        __syncwarp();
+        ++pending;
+        while (qn >= 32) round(32);
+        retire();
+    }
+    while (pending) {
+        round(qn);
+        retire();
     }
 }
 
