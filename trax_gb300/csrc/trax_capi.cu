@@ -540,7 +540,8 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
     /* the pair total is st->n_pairs: written by the pair stage, or copied
      * from pair_offsets[G] by trax_triplet_predict */
     CK(cudaMemsetAsync(&st->n_prec, 0, 8, ctx->stream));  /* n_prec, n_pwalk */
-    k_predict_count<<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
+    (kp.zi_min >= kZiMax ? k_predict_count<true> : k_predict_count<false>)
+        <<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
         kp, grid, h.xyzp, h.zphi, h.zh, h.event, h.layer, (const float2 *)ctx->zi.p,
         (const uint32_t *)ctx->zp.p, pairs, &st->n_pairs, pair_cap, cexcl, ptile, stage, stage_cap,
         tile_sbase, walks, walk_cap, st);
@@ -888,7 +889,7 @@ trax_status trax_ctx_create(trax_ctx **out, int device)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_pair_count, k_pair_count_lane, kFusedThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_pair_store, k_pair_store_lane, kFusedThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_sector, k_pair_sector, kFusedThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_pred, k_predict_count, kFusedThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_pred, k_predict_count<false>, kFusedThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_filter, k_filter_count, 256, 0);
     /* the store passes are bound by load latency and use fewer registers
      * than their count passes: a full complement of their own blocks */

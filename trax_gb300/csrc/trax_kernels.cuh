@@ -1733,6 +1733,7 @@ __device__ __forceinline__ void pred_keep(uint32_t *keep, uint32_t n, uint32_t c
 
 /* Count walk of one pair: accepts of window A (cA) and B (cB), and the first
  * kPredKeep window-B accepts in the reference's visit order. */
+template <bool NOINDEX>
 __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_t *lGrid3,
                                                 const float2 *ZP, const uint16_t *ZH,
                                                 const float2 *zi, const uint32_t *zpos,
@@ -1767,12 +1768,16 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
          * c0..c1-1 (with wrap-around pLow..P, then 0..pHigh-1) */
         auto run = [&](uint32_t c0, uint32_t c1) {
             const uint32_t ra = row[c0], rb = row[c1];
+            if (NOINDEX) {
+                zscreen_walk(ZH, ra, rb, scr, exact);
+                return;
+            }
             if (rb - ra <= kp.run_walk) {
                 /* a small run: walk its contiguous hits */
                 zscreen_walk(ZH, ra, rb, scr, exact);
                 return;
             }
-            for (uint32_t c = c0; c < c1; ++c) {
+            for (uint32_t c = c0; NOINDEX ? false : c < c1; ++c) {
                 const uint32_t ca = row[c], cb = row[c + 1];
                 if (cb - ca <= kp.zi_min || cb - ca > kZiMax) {
                     zscreen_walk(ZH, ca, cb, scr, exact);
@@ -1805,6 +1810,9 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
     }
 }
 
+/* NOINDEX: the tuning never searches a cell's z index (index_min >= kZiMax),
+ * so every run is walked and the search code is left out. */
+template <bool NOINDEX>
 __global__ void __launch_bounds__(256, 5) k_predict_count(
     KParams kp, const uint32_t *grid, const float4 *XYZP, const float2 *ZP,
     const uint16_t *ZH, const uint32_t *EVENT,
@@ -1850,7 +1858,7 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
         uint32_t keep[kPredKeep];
         if (live) {
             uint32_t cA, cB;
-            pred_count_walk(kp, grid + goff, ZP, ZH, zi, zpos, w, cA, cB, keep);
+            pred_count_walk<NOINDEX>(kp, grid + goff, ZP, ZH, zi, zpos, w, cA, cB, keep);
             emitted = cA < cB ? cA : cB;
             my_slots += cA;
             my_trunc += cB - emitted;
