@@ -639,12 +639,15 @@ def run_ours(args, dist):
     B = args.events
     b = gen.generate_batch(w, B, first_event=replica_first_event(dist.rank, B))
     N = b.n_hits
+    if args.walk:
+        # a given walk runs from the sizing chains on, so that every chain a
+        # profiler sees is the measured one
+        best_walk = tuple(int(v) for v in args.walk.split(","))
+        ctx.set_tuning(*best_walk)
     p, counts = sized_pipeline(ctx, w, b)
 
     # ---- result-neutral walk tuning on the resident batch ------------------
     if args.walk:
-        best_walk = tuple(int(v) for v in args.walk.split(","))
-        ctx.set_tuning(*best_walk)
         walk_ms = {}
     else:
         best_walk, walk_ms = tune_walk(ctx, p, b, reps=3)
