@@ -52,7 +52,7 @@ FALLBACK_HBM_GBS = 6800.0
 HEADLINE = "pileup200"
 # grid (z x phi bins) each workload is timed at: the workload's own, or for
 # the high-pile-up configuration the autotuner's choice (its sweep over
-# {8..64} x {16..128} on pile-up-200 events picks 64 x 128; the bench's
+# {8..256} x {16..192} on pile-up-200 events picks 256 x 192; the bench's
 # 'autotune' section repeats the sweep and reports whether it still does)
 TUNED_GRID = {"pileup200": (256, 192),
               # the streaming mix (pile-up U{0..200}) served at the grid and walk

@@ -2139,7 +2139,9 @@ __device__ __forceinline__ bool filter_theta_fit_cut(const KParams &kp, uint32_t
 constexpr uint32_t kFiltRing = 4;     /* chunks whose survivors may wait in the queue */
 constexpr uint32_t kFiltQueue = 96;   /* survivors waiting: < 32 left over + one chunk */
 
-__global__ void __launch_bounds__(256) k_filter_count(KParams kp, const float4 *XYZP,
+/* 7 blocks per SM (32 registers, a few spilled): the gathers wait on memory, and
+ * more resident warps hide it better than the registers saved would. */
+__global__ void __launch_bounds__(256, 7) k_filter_count(KParams kp, const float4 *XYZP,
                                                       const uint32_t *LAYER,
                                                       const uint2 *pairs, const uint2 *cands,
                                                       const uint32_t *n_cands_ptr,
