@@ -580,6 +580,11 @@ def run_autotune(args, ctx):
             "batched_over_per_event_at_best": round(best["events_per_s"] / pe["value"], 2),
             "headline_grid": "x".join(map(str, TUNED_GRID["pileup200"])),
             "headline_grid_is_best": best["grid"] == "x".join(map(str, TUNED_GRID["pileup200"])),
+            # the headline grid's own sweep rate against the best one (grids within
+            # a percent or two trade places between sweeps)
+            "headline_over_best": next((round(r["events_per_s"] / best["events_per_s"], 4)
+                                        for r in rows if r.get("grid") ==
+                                        "x".join(map(str, TUNED_GRID["pileup200"]))), None),
             "sweep_s": round(time.perf_counter() - t0, 1),
             "sweep": [{k: r[k] for k in ("grid", "events_per_s", "walk") if k in r}
                       for r in rows]}
