@@ -86,6 +86,7 @@ struct trax_ctx {
     DevBuf zphi;  /* packed (z, phi) of the sorted hits */
     DevBuf zh;    /* half-precision z of the sorted hits (candidate screen) */
     DevBuf pkeep; /* per outer hit: its first kept pair accepts (split pair stage) */
+    DevBuf gscr;  /* grid build: each hit's cell and phi, for segments beyond the registers */
     DevBuf xyzp;  /* packed (x, y, z, phi) of the sorted hits */
     cudaEvent_t timers[kTimerSlots] = {};
     int blk_pair = 0, blk_pair0 = 0, blk_pair_lane = 0, blk_pair_count = 0, blk_pair_store = 0, blk_sector = 0, blk_pred = 0, blk_filter = 0, blk_scan = 0, blk_small = 0;
@@ -367,15 +368,17 @@ trax_status enqueue_grid(trax_ctx *ctx, const InCols &in, const SortedCols &out,
     if (s != TRAX_OK) return s;
     const int W = ctx->gb_warps, per_sm = ctx->gb_per_sm;
     const size_t smem = ((size_t)(W + 1) * ctx->gb_cells + 2ull * ctx->gb_stage) * 4;
+    if ((s = ensure(ctx, ctx->gscr, (size_t)n_hits * 8 + 8)) != TRAX_OK) return s;
+    uint2 *cscr = (uint2 *)ctx->gscr.p;
     uint32_t blocks = std::min<uint32_t>(max_segs, (uint32_t)(ctx->sm_count * per_sm));
     if (blocks == 0) blocks = 1;
     CK(cudaMemsetAsync(&ctx->d_state->gb_next, 0, 4, ctx->stream));  /* segment counter */
     if (ctx->gb_cells < kp.C)
         k_grid_build<true><<<blocks, W * 32, smem, ctx->stream>>>(
-            kp, in, out, seg_start, seg_n, grid, ctx->gb_stage, ctx->gb_cells, ctx->d_state);
+            kp, in, out, seg_start, seg_n, grid, ctx->gb_stage, ctx->gb_cells, cscr, ctx->d_state);
     else
         k_grid_build<false><<<blocks, W * 32, smem, ctx->stream>>>(
-            kp, in, out, seg_start, seg_n, grid, ctx->gb_stage, ctx->gb_cells, ctx->d_state);
+            kp, in, out, seg_start, seg_n, grid, ctx->gb_stage, ctx->gb_cells, cscr, ctx->d_state);
     CK(cudaGetLastError());
     return mark(ctx, "grid_build");
 }
@@ -916,7 +919,7 @@ void trax_ctx_destroy(trax_ctx *ctx)
                       &ctx->conn_keys, &ctx->conn_sums, &ctx->grid_buf,
                       &ctx->pairs_buf, &ctx->pair_off, &ctx->cands_buf, &ctx->cand_off, &ctx->trk_off,
                       &ctx->r_seg, &ctx->ing, &ctx->phys, &ctx->prec, &ctx->zp, &ctx->ptile,
-                      &ctx->fmask, &ctx->zphi, &ctx->zh, &ctx->xyzp, &ctx->pkeep};
+                      &ctx->fmask, &ctx->zphi, &ctx->zh, &ctx->xyzp, &ctx->pkeep, &ctx->gscr};
     for (DevBuf *b : bufs) if (b->p) cudaFree(b->p);
     for (auto &b : ctx->in_cols) if (b.p) cudaFree(b.p);
     for (auto &b : ctx->srt_cols) if (b.p) cudaFree(b.p);
@@ -1612,6 +1615,7 @@ trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers
     if ((s = ensure(ctx, ctx->zphi, (size_t)max_hits * 8 + 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->zh, (size_t)max_hits * 2 + 32)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->xyzp, (size_t)max_hits * 16 + 16)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->gscr, (size_t)max_hits * 8 + 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->g_start, G * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->g_base, (G + 1) * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->slots, slot_cap * 8)) != TRAX_OK) return s;

@@ -374,7 +374,7 @@ __global__ void __maxnreg__(BANDED ? 64 : 48) k_grid_build(KParams kp, InCols in
                                                            const uint32_t *seg_start,
                                                            const uint32_t *seg_n, uint32_t *grid,
                                                            uint32_t stage, uint32_t Ct,
-                                                           DevState *st)
+                                                           uint2 *cscr, DevState *st)
 {
     constexpr int kItems = BANDED ? kGridItemsBanded : kGridItems;
     extern __shared__ uint32_t smem[];
@@ -417,15 +417,39 @@ __global__ void __maxnreg__(BANDED ? 64 : 48) k_grid_build(KParams kp, InCols in
         const bool staged = n <= stage;
         uint32_t *gseg = grid + (size_t)seg * C;
 
-        /* pass 0: the z rows the segment's hits occupy */
+        /* pass 0: with bands, segments too large for the registers compute
+         * every hit's cell and phi once, into cscr (read back by the same
+         * thread in passes 1 and 3 of every band, instead of an atan2 per
+         * hit per band), and the z rows the segment's hits occupy */
+        const bool scratch = BANDED && !cached && cscr != nullptr;
+        if (scratch) {
+            bool anybad = false;
+            for (uint32_t i = lo + lane; i < hi; i += 32) {
+                const uint32_t h = start + i;
+                float phi;
+                bool bad;
+                const uint32_t cell = hit_cell(kp, in.x[h], in.y[h], in.z[h], &phi, &bad);
+                anybad |= bad;
+                cscr[h] = make_uint2(cell, __float_as_uint(phi));
+            }
+            if (anybad) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_OUTSIDE_GRID);
+        }
         uint32_t rlo = 0, rhi = kp.nz;
         if (banded) {
             uint32_t mn = 0xffffffffu, mx = 0u;
-            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-                uint32_t zs = trax_f2u(trax_floor_div(in.z[start + i] - TRAX_MIN_Z, kp.sz_z, kp.inv_sz_z));
-                if (zs > kp.nz) zs = kp.nz;
-                mn = min(mn, zs);
-                mx = max(mx, zs);
+            if (scratch) {
+                for (uint32_t i = lo + lane; i < hi; i += 32) {
+                    const uint32_t zs = cscr[start + i].x / P1;
+                    mn = min(mn, zs);
+                    mx = max(mx, zs);
+                }
+            } else {
+                for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+                    uint32_t zs = trax_f2u(trax_floor_div(in.z[start + i] - TRAX_MIN_Z, kp.sz_z, kp.inv_sz_z));
+                    if (zs > kp.nz) zs = kp.nz;
+                    mn = min(mn, zs);
+                    mx = max(mx, zs);
+                }
             }
 #pragma unroll
             for (int d = 16; d; d >>= 1) {
@@ -520,10 +544,14 @@ __global__ void __maxnreg__(BANDED ? 64 : 48) k_grid_build(KParams kp, InCols in
                     uint32_t cell = 0;
                     if (valid) {
                         const uint32_t h = start + i;
-                        float phi;
-                        bool bad;
-                        cell = hit_cell(kp, in.x[h], in.y[h], in.z[h], &phi, &bad);
-                        if (bad && rb == rlo) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_OUTSIDE_GRID);
+                        if (scratch) {
+                            cell = cscr[h].x;
+                        } else {
+                            float phi;
+                            bool bad;
+                            cell = hit_cell(kp, in.x[h], in.y[h], in.z[h], &phi, &bad);
+                            if (bad && rb == rlo) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_OUTSIDE_GRID);
+                        }
                         valid = cell - cb0 < nb;
                     }
                     const uint32_t act = __ballot_sync(kFull, valid);
@@ -595,9 +623,20 @@ __global__ void __maxnreg__(BANDED ? 64 : 48) k_grid_build(KParams kp, InCols in
                     uint32_t h = 0;
                     if (valid) {
                         h = start + i;
-                        x = in.x[h]; y = in.y[h]; z = in.z[h];
-                        bool bad;
-                        cell = hit_cell(kp, x, y, z, &phi, &bad);
+                        if (!staged) {
+                            x = in.x[h]; y = in.y[h]; z = in.z[h];
+                        }
+                        if (scratch) {
+                            const uint2 cp = cscr[h];
+                            cell = cp.x;
+                            phi = __uint_as_float(cp.y);
+                        } else {
+                            if (staged) {
+                                x = in.x[h]; y = in.y[h]; z = in.z[h];
+                            }
+                            bool bad;
+                            cell = hit_cell(kp, x, y, z, &phi, &bad);
+                        }
                         valid = cell - cb0 < nb;
                     }
                     const uint32_t act = __ballot_sync(kFull, valid);
