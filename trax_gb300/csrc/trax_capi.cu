@@ -543,6 +543,7 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
     /* the pair total is st->n_pairs: written by the pair stage, or copied
      * from pair_offsets[G] by trax_triplet_predict */
     CK(cudaMemsetAsync(&st->n_prec, 0, 8, ctx->stream));  /* n_prec, n_pwalk */
+    CK(cudaMemsetAsync(&st->tile_ctr[0], 0, 4, ctx->stream));  /* work tickets */
     (kp.zi_min >= kZiMax ? k_predict_count<true> : k_predict_count<false>)
         <<<ctx->blk_pred, kFusedThreads, 0, ctx->stream>>>(
         kp, grid, h.xyzp, h.zphi, h.zh, h.event, h.layer, (const float2 *)ctx->zi.p,
@@ -584,6 +585,7 @@ trax_status enqueue_filter(trax_ctx *ctx, const SortedCols &h, const uint2 *pair
     uint32_t *mask = (uint32_t *)ctx->fmask.p, *wpos = mask + words;
     DevState *st = ctx->d_state;
     CK(cudaMemsetAsync(trk_offsets, 0, (size_t)(max_groups + 1) * 4, ctx->stream));
+    CK(cudaMemsetAsync(&st->tile_ctr[0], 0, 4, ctx->stream));  /* work tickets */
     k_filter_count<<<ctx->blk_filter, 256, 0, ctx->stream>>>(kp, h.xyzp, h.layer, pairs,
                                                              cands, &st->n_cands, cand_cap, mask,
                                                              wpos, st);

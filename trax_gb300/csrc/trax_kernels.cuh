@@ -67,7 +67,7 @@ struct DevState {
     unsigned long long pair_slots;
     unsigned long long cand_slots;
     unsigned long long cand_truncated;
-    uint32_t tile_ctr[4];    /* decoupled look-back tile tickets */
+    uint32_t tile_ctr[4];    /* decoupled look-back tile tickets; [0] also the count passes' work tickets */
     uint32_t aux_n;          /* element count of a standalone prefix sum */
     uint32_t n_prec;         /* accepts the prediction count staged for the store pass */
     uint32_t n_pwalk;        /* prediction store records that walk (after them) */
@@ -1740,6 +1740,7 @@ __device__ __forceinline__ PredWindow pred_window(const KParams &kp, uint32_t lt
  * window is recomputed.
  */
 constexpr int kPredKeep = 7;  /* window-B accepts staged per pair */
+constexpr uint32_t kPredTicket = 4;  /* 32-pair tiles per work ticket of the count pass */
 
 /* 32-byte record of a pair with more than kPredKeep candidates: its store
  * window (window B). */
@@ -1807,16 +1808,15 @@ __device__ __forceinline__ void pred_count_walk(const KParams &kp, const uint32_
          * c0..c1-1 (with wrap-around pLow..P, then 0..pHigh-1) */
         auto run = [&](uint32_t c0, uint32_t c1) {
             const uint32_t ra = row[c0], rb = row[c1];
-            if (NOINDEX) {
+            /* a small run (every run without the index): walk its contiguous hits */
+            if (NOINDEX || rb - ra <= kp.run_walk) {
                 zscreen_walk(ZH, ra, rb, scr, exact);
                 return;
             }
-            if (rb - ra <= kp.run_walk) {
-                /* a small run: walk its contiguous hits */
-                zscreen_walk(ZH, ra, rb, scr, exact);
-                return;
-            }
-            for (uint32_t c = c0; NOINDEX ? false : c < c1; ++c) {
+            /* the run's cells one by one; NOINDEX never gets here, and its
+             * loop bound of zero keeps the compiler from warning about it */
+            const uint32_t cend = NOINDEX ? c0 : c1;
+            for (uint32_t c = c0; c < cend; ++c) {
                 const uint32_t ca = row[c], cb = row[c + 1];
                 if (cb - ca <= kp.zi_min || cb - ca > kZiMax) {
                     zscreen_walk(ZH, ca, cb, scr, exact);
@@ -1869,8 +1869,20 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
     const uint32_t E = st->n_events;
     if (blockIdx.x == 0 && threadIdx.x == 0) st->n_ptile = (n + 31) / 32;
     unsigned long long my_slots = 0, my_trunc = 0;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t p0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; p0 < n; p0 += stride) {
+    /* warps take kPredTicket consecutive 32-pair tiles at a time from a device
+     * counter: tiles cost very different amounts (dense rows, long walks),
+     * and a warp's consecutive tiles share outer hits and layer-3 cells */
+    uint32_t tile = 0, left = 0;
+    for (;;) {
+        if (left == 0) {
+            if (lane == 0) tile = atomicAdd(&st->tile_ctr[0], 1u);
+            tile = __shfl_sync(kFull, tile, 0) * kPredTicket;
+            left = kPredTicket;
+        }
+        const uint32_t p0 = tile * 32;
+        ++tile;
+        --left;
+        if (p0 >= n) break;
         const uint32_t p = p0 + lane;
         bool live = p < n;
         PredWindow w{};
@@ -2240,7 +2252,24 @@ __global__ void __launch_bounds__(256, 7) k_filter_count(KParams kp, const float
         }
         __syncwarp();
     };
-    for (uint32_t i0 = gw * 64; i0 < n; i0 += nw * 64) {
+    /* with many chunks per warp, warps take 4 consecutive chunks at a time
+     * from a device counter (chunks cost different amounts, and consecutive
+     * ones share pairs and hits); with few, a fixed stride spreads them over
+     * every warp and spares the counter */
+    const bool tickets = (n + 63) / 64 >= nw * 64;
+    uint32_t ticket = 0, left = 0;
+    for (uint32_t i0 = gw * 64;;) {
+        if (tickets) {
+            if (left == 0) {
+                if (lane == 0) ticket = atomicAdd(&st->tile_ctr[0], 1u);
+                ticket = __shfl_sync(kFull, ticket, 0) * 4;
+                left = 4;
+            }
+            i0 = ticket * 64;
+            ++ticket;
+            --left;
+        }
+        if (i0 >= n) break;
         /* a free ring slot for this chunk: finish queued survivors until the
          * oldest chunk retires */
         while (pending == kFiltRing) {
@@ -2280,6 +2309,7 @@ __global__ void __launch_bounds__(256, 7) k_filter_count(KParams kp, const float
         ++pending;
         while (qn >= 32) round(32);
         retire();
+        if (!tickets) i0 += nw * 64;
     }
     while (pending) {
         round(qn);
