@@ -555,6 +555,7 @@ trax_status enqueue_predict(trax_ctx *ctx, const SortedCols &h, const uint32_t *
     k_scan<kScanItems><<<std::min<uint32_t>(ctx->blk_scan, ntile), kScanThreads, 0, ctx->stream>>>(
         ptile, ptile, &st->n_ptile, ptiles, &st->n_cands, 1, (unsigned long long *)ctx->st1.p, st);
     if ((s = mark(ctx, "predict_scan")) != TRAX_OK) return s;
+    CK(cudaMemsetAsync(&st->tile_ctr[0], 0, 4, ctx->stream));  /* work tickets */
     k_predict_store<<<ctx->blk_pstore, kFusedThreads, 0, ctx->stream>>>(
         kp, grid, h.zphi, h.zh, stage, stage_cap, tile_sbase, walks, walk_cap, cexcl, ptile,
         &st->n_pairs, pair_cap, &st->n_cands, cands, cand_cap, st);

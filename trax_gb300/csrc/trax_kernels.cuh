@@ -1992,7 +1992,7 @@ __global__ void __launch_bounds__(256) k_predict_store(
     const uint32_t P1 = kp.nphi + 1;
     const uint32_t lane = threadIdx.x & 31;
     /*
-     * A warp takes 32 tiles of 32 pairs; lane i reads tile i's prefix, total
+     * A warp takes 32 tiles of 32 pairs at a time; lane i reads tile i's prefix, total
      * and stage offset (coalesced), and the warp then copies each non-empty
      * tile: its candidates are one run of positions and its staged accepts
      * one run of the stage in the same order (the first kPredKeep of each
@@ -2001,9 +2001,12 @@ __global__ void __launch_bounds__(256) k_predict_store(
      * counts: a tile stages at most 32 * kPredKeep accepts, and the first 32
      * are read ahead.
      */
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t t0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; t0 < ntiles;
-         t0 += nw * 32) {
+    /* the 32-tile groups come from a device counter (their costs differ) */
+    for (;;) {
+        uint32_t group = 0;
+        if (lane == 0) group = atomicAdd(&st->tile_ctr[0], 1u);
+        const uint32_t t0 = __shfl_sync(kFull, group, 0) * 32;
+        if (t0 >= ntiles) break;
         const uint32_t tt = t0 + lane;
         uint32_t tp = 0, sb = 0;
         if (tt < ntiles) {
