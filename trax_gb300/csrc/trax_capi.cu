@@ -276,8 +276,11 @@ void apply_launch_cap(trax_ctx *ctx)
  *   warps    enough for 1.5x the average segment at kGridItems * 32 hits a
  *            warp (kGridItemsBanded with bands; at most 32);
  *   tables   per-warp cell tables of Ct cells: the whole grid when it fits,
- *            else whole z rows -- at least min(8, Z + 1) of them, with fewer
- *            warps if need be -- and the kernel works in bands of rows. */
+ *            else whole z rows -- at least min(4, Z + 1) of them, with fewer
+ *            warps if need be -- and the kernel works in bands of rows (the
+ *            table work of a segment grows with the warps times the cells its
+ *            rows occupy, not with the number of bands, so more warps and
+ *            narrower bands win: 8 rows 0.75 ms, 4 rows 0.72 ms at 256 x 192). */
 trax_status grid_plan(trax_ctx *ctx, uint32_t C, uint32_t avg_seg)
 {
     const uint32_t P1 = ctx->kp.nphi + 1, rows = C / P1;
@@ -295,7 +298,7 @@ trax_status grid_plan(trax_ctx *ctx, uint32_t C, uint32_t avg_seg)
     /* the banded instance holds more hits per lane */
     long W = warps_for(kGridItems);
     if (C > table(W)) W = warps_for(kGridItemsBanded);
-    const uint64_t want = C <= table(W) ? C : (uint64_t)std::min<uint32_t>(8, rows) * P1;
+    const uint64_t want = C <= table(W) ? C : (uint64_t)std::min<uint32_t>(4, rows) * P1;
     while (W > 1 && table(W) < want) --W;
     uint64_t Ct = std::min<uint64_t>(table(W), C);
     if (Ct < C) Ct = Ct / P1 * P1;
