@@ -202,7 +202,9 @@ float trax_min_radius_curvature(float min_pt, float bz);
  * than index_min (<= 256) hits is searched through a per-cell z index.
  * pair_record selects the pair kernels: 3 walks one outer hit per lane in a
  * count pass, scans the counts and copies the kept accepts in a store pass;
- * 2 walks one outer hit per lane with a look-back in one kernel; 1 and 0
+ * 2 walks one outer hit per lane with a look-back in one kernel, keeping 16
+ * accepts per outer hit for the store (4: the same keeping 48, for outer hits
+ * with a few dozen pairs each); 1 and 0
  * sweep each outer hit's candidates with the whole warp, replaying the count
  * sweep's ballots for the store (1) or sweeping twice (0).  Sparse events
  * favour walking and pair_record 3, dense (pile-up) events the index.

@@ -215,7 +215,8 @@ def test_tuning_does_not_change_results(gpu_ctx):
     try:
         for walk, imin, rec in ((0, 0, 1), (0, 16, 0), (48, 16, 1), (96, 32, 0),
                                 (1 << 30, 256, 1), (1 << 30, 256, 0), (0, 16, 2),
-                                (1 << 30, 256, 2), (0, 16, 3), (1 << 30, 256, 3)):
+                                (1 << 30, 256, 2), (0, 16, 3), (1 << 30, 256, 3),
+                                (1 << 30, 256, 4), (0, 16, 4)):
             gpu_ctx.set_tuning(walk, imin, rec)
             trk, off, counts = p.seed(b)
             assert counts["status"] == 0

@@ -73,7 +73,7 @@ def test_autotuned_grids_equal_oracle(gpu_ctx, zp):
     want, want_off, _ = oracle_trk(b, g, grid)
     p = pipeline_for(gpu_ctx, g, b, grid)
     for rw, zi in WALK_CANDIDATES[:4]:
-        for rec in (3, 1):
+        for rec in (3, 4, 1):
             gpu_ctx.set_tuning(rw, zi, rec)
             trk, off, counts = p.seed(b)
             assert counts["status"] == 0

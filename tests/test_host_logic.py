@@ -42,13 +42,14 @@ def test_tune_walk_times_every_walk_then_the_pair_kernels_then_the_launch_shape(
     assert ctx.history[:len(walks)] == walks
     # the other pair kernels run only at the best walk, in the documented order
     n = len(walks)
-    assert ctx.history[n:n + 3] == [(96, 32, 2, 0), (96, 32, 1, 0), (96, 32, 0, 0)]
+    assert ctx.history[n:n + 4] == [(96, 32, 2, 0), (96, 32, 4, 0), (96, 32, 1, 0),
+                                    (96, 32, 0, 0)]
     # then fewer resident blocks per SM at the best of those
-    assert ctx.history[n + 3:n + 3 + len(autotune.BLOCK_CAPS)] == \
+    assert ctx.history[n + 4:n + 4 + len(autotune.BLOCK_CAPS)] == \
         [(96, 32, 2, c) for c in autotune.BLOCK_CAPS]
     assert best == (96, 32, 2, 3)
     assert ctx.tuning == best  # installed last
-    assert len(timings) == n + 3 + len(autotune.BLOCK_CAPS)
+    assert len(timings) == n + 4 + len(autotune.BLOCK_CAPS)
 
 
 def test_tune_walk_keeps_the_split_pair_stage_when_it_is_fastest(monkeypatch):
@@ -57,7 +58,8 @@ def test_tune_walk_keeps_the_split_pair_stage_when_it_is_fastest(monkeypatch):
     assert best == (0, 16, 3, 0)
     assert ctx.tuning == (0, 16, 3, 0)
     caps = len(autotune.BLOCK_CAPS)
-    assert ctx.history[-4 - caps:-1 - caps] == [(0, 16, 2, 0), (0, 16, 1, 0), (0, 16, 0, 0)]
+    assert ctx.history[-5 - caps:-1 - caps] == [(0, 16, 2, 0), (0, 16, 4, 0), (0, 16, 1, 0),
+                                                (0, 16, 0, 0)]
 
 
 def test_tuning_for_picks_the_batch_class():

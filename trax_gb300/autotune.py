@@ -60,7 +60,7 @@ def tune_walk(ctx: Context, p: Pipeline, batch: gen.EventBatch, reps=5,
         ctx.set_tuning(*cand, 3, 0)
         timings[(*cand, 3, 0)] = time_staged(ctx, p, reps)
     best = min(timings, key=timings.get)
-    for rec in (2, 1, 0):
+    for rec in (2, 4, 1, 0):
         ctx.set_tuning(best[0], best[1], rec, 0)
         timings[(best[0], best[1], rec, 0)] = time_staged(ctx, p, reps)
     best = min(timings, key=timings.get)

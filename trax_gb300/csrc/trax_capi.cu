@@ -445,8 +445,9 @@ trax_status enqueue_pairs(trax_ctx *ctx, const SortedCols &h, const uint32_t *gr
         k_pair_sector<<<ctx->blk_sector, kFusedThreads, 0, ctx->stream>>>(
             kp, grid, h.zphi, slots, slot_cap, pexcl, pairs, pair_cap,
             (unsigned long long *)ctx->st0.p, st);
-    else if (kp.pair_record == 2)
-        k_pair_lane<<<ctx->blk_pair_lane, kFusedThreads, 0, ctx->stream>>>(
+    else if (kp.pair_record == 2 || kp.pair_record == 4)
+        (kp.pair_record == 2 ? k_pair_lane<kPairKeep> : k_pair_lane<kPairKeepWide>)
+            <<<ctx->blk_pair_lane, kFusedThreads, 0, ctx->stream>>>(
             kp, grid, h.xyzp, h.zphi, slots, slot_cap, pexcl, pairs, pair_cap,
             (unsigned long long *)ctx->st0.p, st);
     else if (kp.pair_record)
@@ -894,7 +895,7 @@ trax_status trax_ctx_create(trax_ctx **out, int device)
     int b = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_pair, k_pair_fused<true>, kFusedThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_pair0, k_pair_fused<false>, kFusedThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_pair_lane, k_pair_lane, kFusedThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_pair_lane, k_pair_lane<kPairKeep>, kFusedThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_pair_count, k_pair_count_lane, kFusedThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_pair_store, k_pair_store_lane, kFusedThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_sector, k_pair_sector, kFusedThreads, 0);
@@ -1009,7 +1010,7 @@ trax_status trax_set_tuning(trax_ctx *ctx, const trax_tuning *t)
 {
     if (!ctx || !t) return TRAX_ERR_BAD_ARG;
     if (t->index_min > 256) return fail(ctx, TRAX_ERR_BAD_ARG, "index_min must be <= 256");
-    if (t->pair_record > 3) return fail(ctx, TRAX_ERR_BAD_ARG, "pair_record must be 0 to 3");
+    if (t->pair_record > 4) return fail(ctx, TRAX_ERR_BAD_ARG, "pair_record must be 0 to 4");
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->kp.run_walk = t->run_walk;
     ctx->kp.zi_min = t->index_min;
