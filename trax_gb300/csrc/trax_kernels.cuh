@@ -1996,16 +1996,15 @@ __global__ void __launch_bounds__(256) k_predict_store(
     const uint32_t P1 = kp.nphi + 1;
     const uint32_t lane = threadIdx.x & 31;
     /*
-     * A warp takes 32 tiles of 32 pairs at a time; lane i reads tile i's prefix, total
-     * and stage offset (coalesced), and the warp then copies each non-empty
-     * tile: its candidates are one run of positions and its staged accepts
-     * one run of the stage in the same order (the first kPredKeep of each
-     * pair), so it copies them one candidate per lane with coalesced stage
-     * reads and candidate writes.  The stage reads do not wait for the
-     * counts: a tile stages at most 32 * kPredKeep accepts, and the first 32
-     * are read ahead.
+     * A warp takes groups of 32 tiles of 32 pairs from a device counter (the
+     * groups' costs differ); lane i reads tile i's prefix, total and stage
+     * offset (coalesced), and the warp then copies each non-empty tile: its
+     * candidates are one run of positions and its staged accepts one run of
+     * the stage in the same order (the first kPredKeep of each pair), so it
+     * copies them one candidate per lane with coalesced stage reads and
+     * candidate writes.  The stage reads do not wait for the counts: a tile
+     * stages at most 32 * kPredKeep accepts, and the first 32 are read ahead.
      */
-    /* the 32-tile groups come from a device counter (their costs differ) */
     for (;;) {
         uint32_t group = 0;
         if (lane == 0) group = atomicAdd(&st->tile_ctr[0], 1u);
