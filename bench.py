@@ -361,16 +361,49 @@ def cpu_events_per_s(b, w, seconds, threads, runner=None):
 # --------------------------------------------------------------------------
 # reference arm
 
+# the reference sizes and indexes its pair bitmap (n1 * n2 bits per event and
+# layer triplet) in 32-bit counts (PairGeneratorBeamspot.cpp:9-27): event groups
+# stay below this many bits, as its own event grouping would keep them
+REF_GROUP_BITS = 1 << 31
+
+
+def reference_groups(b, w):
+    """Consecutive event groups of batch b whose pair bitmaps stay within
+    REF_GROUP_BITS (at least one event each)."""
+    cfg = w.config()
+    ln = b.layer_nhits.astype(np.int64)
+    bits = np.zeros(b.n_events, dtype=np.int64)
+    for t in range(cfg.n_layer_triplets):
+        tr = cfg.triplets[t]
+        bits += ln[:, tr.layer1 - 1] * ln[:, tr.layer2 - 1]
+    groups, first, acc = [], 0, 0
+    for e in range(b.n_events):
+        if e > first and acc + bits[e] > REF_GROUP_BITS:
+            groups.append((first, e - first))
+            first, acc = e, 0
+        acc += int(bits[e])
+    groups.append((first, b.n_events - first))
+    return groups
+
+
 def reference_runner(threads):
-    """The reference's own kernels on the host when oracle/_ref builds here,
-    else the CPU restatement of its algorithm."""
+    """The reference's own kernels on the host when oracle/_ref builds here
+    (run per event group, see REF_GROUP_BITS), else the CPU restatement of its
+    algorithm."""
     from oracle import ref
     try:
         if ref.available():
             ref.lib()
-            return "reference", lambda s, w: ref.run(s, w.config(), w.grid(s.n_events), 4,
-                                                     n_threads=256, grid_threads=1,
-                                                     workers=threads)["stats"]
+
+            def run_groups(s, w):
+                total = None
+                for first, count in reference_groups(s, w):
+                    g = s.slice_events(first, count) if count != s.n_events else s
+                    st = ref.run(g, w.config(), w.grid(g.n_events), 4, n_threads=256,
+                                 grid_threads=1, workers=threads)["stats"]
+                    total = dict(st) if total is None else {k: total[k] + st[k] for k in st}
+                return total
+            return "reference", run_groups
     except (OSError, FileNotFoundError, subprocess.CalledProcessError):
         pass
     import oracle

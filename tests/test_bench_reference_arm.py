@@ -55,3 +55,26 @@ def test_gpus_flag_must_match_the_launcher():
                        env=env)
     assert p.returncode == 2
     assert "disagrees" in p.stderr
+
+
+def test_reference_runs_in_event_groups_its_bitmap_counts_can_hold():
+    """The reference sizes its pair bitmap in 32-bit bit counts, so the arm
+    runs it on event groups whose n1 * n2 bits stay below 2^31; pile-up 200
+    events (~84 M bits each) go in groups of at most 25, every event once and
+    in order."""
+    sys.path.insert(0, ROOT)
+    import numpy as np
+    import bench
+    from trax_gb300 import gen
+    w = bench.workload_at_grid(gen.WORKLOADS["pileup200"], "tuned")
+
+    class Batch:  # layer hit counts are all the grouping reads
+        n_events = 200
+        layer_nhits = np.tile(np.array([[6500, 6500, 6500, 6500]], dtype=np.uint32), (200, 1))
+
+    groups = bench.reference_groups(Batch, w)
+    assert groups[0][0] == 0 and sum(c for _, c in groups) == 200
+    assert all(f2 == f1 + c1 for (f1, c1), (f2, _) in zip(groups, groups[1:]))
+    per_event = 2 * 6500 * 6500
+    assert all(c * per_event <= bench.REF_GROUP_BITS for _, c in groups)
+    assert max(c for _, c in groups) == bench.REF_GROUP_BITS // per_event
