@@ -99,6 +99,13 @@ __device__ __forceinline__ void set_fault(DevState *st, uint32_t status, uint32_
     if (atomicCAS(&st->status, 0u, status) == 0u) atomicExch(&st->detail, detail);
 }
 
+/* A hint to bring the 128-byte line holding `a` into L2; `a` must lie inside
+ * an allocation. */
+__device__ __forceinline__ void prefetch_l2(const void *a)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt()
 {
     uint32_t m;
@@ -1875,12 +1882,21 @@ __global__ void __launch_bounds__(256, 5) k_predict_count(
     unsigned long long my_slots = 0, my_trunc = 0;
     /* warps take kPredTicket consecutive 32-pair tiles at a time from a device
      * counter: tiles cost very different amounts (dense rows, long walks),
-     * and a warp's consecutive tiles share outer hits and layer-3 cells */
+     * and a warp's consecutive tiles share outer hits and layer-3 cells.
+     * With each ticket a warp has the pairs of the ticket one round of warps
+     * ahead (one 128-byte line per 16) brought into L2: some warp takes that
+     * ticket about when this one is done (a warp holding a ticket ahead
+     * would stretch the tail of small batches). */
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     uint32_t tile = 0, left = 0;
     for (;;) {
         if (left == 0) {
             if (lane == 0) tile = atomicAdd(&st->tile_ctr[0], 1u);
-            tile = __shfl_sync(kFull, tile, 0) * kPredTicket;
+            tile = __shfl_sync(kFull, tile, 0);
+            const unsigned long long q =
+                ((unsigned long long)tile + nw) * (kPredTicket * 32) + lane * 16;
+            if (lane < kPredTicket * 2 && q < n) prefetch_l2(pairs + q);
+            tile *= kPredTicket;
             left = kPredTicket;
         }
         const uint32_t p0 = tile * 32;
@@ -2261,14 +2277,19 @@ __global__ void __launch_bounds__(256, 7) k_filter_count(KParams kp, const float
     /* with many chunks per warp, warps take 4 consecutive chunks at a time
      * from a device counter (chunks cost different amounts, and consecutive
      * ones share pairs and hits); with few, a fixed stride spreads them over
-     * every warp and spares the counter */
+     * every warp and spares the counter.  With each ticket a warp has the
+     * candidates of the ticket one round of warps ahead (8 bytes each, one
+     * 128-byte line per 16) brought into L2 for the warp that takes it. */
     const bool tickets = (n + 63) / 64 >= nw * 64;
     uint32_t ticket = 0, left = 0;
     for (uint32_t i0 = gw * 64;;) {
         if (tickets) {
             if (left == 0) {
                 if (lane == 0) ticket = atomicAdd(&st->tile_ctr[0], 1u);
-                ticket = __shfl_sync(kFull, ticket, 0) * 4;
+                ticket = __shfl_sync(kFull, ticket, 0);
+                const unsigned long long q = ((unsigned long long)ticket + nw) * 256 + lane * 16;
+                if (lane < 16 && q < n) prefetch_l2(cands + q);
+                ticket *= 4;
                 left = 4;
             }
             i0 = ticket * 64;
