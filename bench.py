@@ -788,7 +788,9 @@ def run_ours(args, dist):
     e2e_s = dist.max(time.perf_counter() - t0)
     if sc2["n_tracklets"] != c2["n_tracklets"] or not np.array_equal(strk[0], trk[0]):
         raise SystemExit("streaming result differs from the synchronous one")
-    h2d = sum(c.nbytes for c in cols) + b.layer_nhits.nbytes
+    # the batched calls upload x, y, z, layer and event (the detector and hit
+    # ids are not read on that path) and the segment starts and counts
+    h2d = sum(c.nbytes for c in (b.x, b.y, b.z, b.layer, b.event)) + 2 * b.layer_nhits.nbytes + 8
     d2h = int(sum(t.nbytes for t in trk) + off.nbytes + 72)
     e2e = {"value": round(events_all * args.steps / e2e_s, 2), "unit": "events/s",
            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h,

@@ -513,7 +513,12 @@ trax_status trax_reset_counts(trax_ctx *ctx);
  * addEvent, uploads, the four stages, the result downloads) as one call on
  * reserved buffers and one CUDA graph. */
 
-/* Host-side batch of events, bucketed as HitCollection::addEvent does. */
+/* Host-side batch of events, bucketed as HitCollection::addEvent does.  The
+ * batched calls (trax_stage_batch, trax_seed_batch, trax_submit_batch,
+ * trax_count_pairs_batch, the server) upload and read x, y, z, layer and
+ * event only: detector_id and hit_id are not used on that path (tracklets
+ * come back as input positions, or sorted positions whose hits are never
+ * returned) and may be null. */
 typedef struct trax_event_batch {
     uint32_t n_events;
     uint32_t n_layers;

@@ -59,6 +59,29 @@ def test_pileup200_64_events_streaming_equals_oracle(gpu_ctx):
     assert np.array_equal(off1, want_off)
 
 
+def test_batched_calls_do_not_read_detector_and_hit_ids(gpu_ctx):
+    """The batched calls upload x, y, z, layer and event only: null detector
+    and hit id columns, or columns of garbage, give the oracle's tracklets
+    through trax_seed_batch and trax_submit_batch alike."""
+    import dataclasses
+    w = gen.WORKLOADS["pileup200"]
+    b = gen.generate_batch(w, 8, first_event=77)
+    want, want_off, _ = oracle_trk(b, w)
+    p = pipeline_for(gpu_ctx, w, b)
+    junk = np.full(b.n_hits, 0xDEADBEEF, dtype=np.uint32)
+    for ids in (None, junk):
+        nb = dataclasses.replace(b, detector_id=ids, hit_id=ids)
+        trk, off, counts = p.seed(nb)
+        assert counts["status"] == 0
+        assert np.array_equal(trk, want) and np.array_equal(off, want_off)
+        t1 = p.submit(nb)
+        t2 = p.submit(nb)
+        for t in (t1, t2):
+            trk, off, counts = p.wait(t)
+            assert counts["status"] == 0
+            assert np.array_equal(trk, want) and np.array_equal(off, want_off)
+
+
 @pytest.mark.parametrize("zp", [(64, 64), (64, 128), (32, 64), (256, 192), (128, 128)])
 def test_autotuned_grids_equal_oracle(gpu_ctx, zp):
     """The grids the autotuner selects on pile-up 200 (the truncated
@@ -94,12 +117,16 @@ def test_serving_stream_equals_oracle(gpu_ctx, zp, tuning):
         w = gen.Workload(w.name, w.config_id, w.n_layers, w.noise, w.pt_range, zp[0], zp[1],
                          w.n_triplets, pileup_uniform=w.pileup_uniform)
     events = [gen.generate_batch(w, 1, first_event=300 + i) for i in range(24)]
+    # the server never reads the detector and hit ids: half the requests leave them out
+    import dataclasses
+    reqs = [dataclasses.replace(e, detector_id=None, hit_id=None) if i % 2 else e
+            for i, e in enumerate(events)]
     cfg = w.config()
     with Server(cfg, w.n_layers, w.n_sectors_z, w.n_sectors_phi, slots=3,
                 max_batch_events=8, memory_budget_bytes=6 << 30, tuning=tuning) as srv:
         t0 = srv.now_ns() + 20_000_000
         arrivals = poisson_arrivals(len(events), 2000.0, t0, seed=5)
-        tickets = [srv.submit(e, int(a)) for e, a in zip(events, arrivals)]
+        tickets = [srv.submit(e, int(a)) for e, a in zip(reqs, arrivals)]
         got = {}
         while len(got) < len(events):
             r = srv.poll(timeout_ms=20_000)

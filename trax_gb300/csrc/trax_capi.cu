@@ -43,6 +43,13 @@ struct DevBuf {
     size_t bytes = 0;
 };
 
+/* The input columns (x, y, z, layer, detector id, hit id, event) the batched
+ * chain reads: x, y, z, layer and event.  The detector and hit ids stay on
+ * the host -- the chain's tracklets come back as input positions and its
+ * sorted hits are never returned -- so their buffers are neither allocated
+ * nor uploaded. */
+constexpr int kChainCols[5] = {0, 1, 2, 3, 6};
+
 /* One of the two batches a context can have in flight
  * (trax_submit_batch / trax_wait_batch): its own inputs, upload staging,
  * graph and result counts. */
@@ -1603,7 +1610,8 @@ trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers
     const uint64_t slot_cap = (uint64_t)max_hits * T + 1;
     if (slot_cap > 0xF0000000ull || (uint64_t)max_events * max_layers * C > 0xF0000000ull)
         return fail(ctx, TRAX_ERR_BAD_ARG, "reservation too large");
-    for (int i = 0; i < 7; ++i) if ((s = ensure(ctx, ctx->in_cols[i], (size_t)max_hits * 4)) != TRAX_OK) return s;
+    for (int i : kChainCols)
+        if ((s = ensure(ctx, ctx->in_cols[i], (size_t)max_hits * 4)) != TRAX_OK) return s;
     /* the chain keeps only layer, event and input position of the sorted
      * hits (plus the packed columns below) */
     for (int i : {4, 7, 8}) if ((s = ensure(ctx, ctx->srt_cols[i], (size_t)max_hits * 4)) != TRAX_OK) return s;
@@ -1792,7 +1800,7 @@ trax_status trax_stage_batch(trax_ctx *ctx, const trax_event_batch *in)
     CK(cudaMemcpyAsync(ctx->d_state, hs + 2 * nseg_r, 8, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaEventRecord(ctx->stage_free, ctx->stream));
     const void *src[7] = {in->x, in->y, in->z, in->layer, in->detector_id, in->hit_id, in->event};
-    for (int i = 0; i < 7; ++i)
+    for (int i : kChainCols)
         if (in->n_hits) CK(cudaMemcpyAsync(ctx->in_cols[i].p, src[i], (size_t)in->n_hits * 4,
                                            cudaMemcpyHostToDevice, ctx->stream));
     ctx->staged_events = E;
@@ -1981,7 +1989,7 @@ trax_status trax_seed_batch(trax_ctx *ctx, const trax_event_batch *in, trax_batc
     b2.n_events = E - E1;
     b2.n_hits = in->n_hits - (uint32_t)n1;
     b2.x += n1; b2.y += n1; b2.z += n1;
-    b2.layer += n1; b2.detector_id += n1; b2.hit_id += n1; b2.event += n1;
+    b2.layer += n1; b2.event += n1;  /* the ids are not read (and may be null) */
     b2.layer_nhits += (size_t)E1 * L;
     uint32_t t1 = 0, t2 = 0;
     trax_status s = submit_slot(ctx, &b1, out, 0, 0, &t1);
@@ -2025,7 +2033,8 @@ static trax_status ensure_slot(trax_ctx *ctx, AsyncSlot &a)
     if (a.h_meta) return TRAX_OK;
     const size_t nseg_r = (size_t)ctx->r_events * ctx->r_layers;
     /* plain allocations: the slot's graph is captured after them */
-    for (auto &b : a.in_cols) {
+    for (int i : kChainCols) {
+        DevBuf &b = a.in_cols[i];
         b.bytes = std::max<size_t>((size_t)ctx->r_hits * 4, 16);
         CK(cudaMalloc(&b.p, b.bytes));
     }
@@ -2070,7 +2079,7 @@ static trax_status submit_slot(trax_ctx *ctx, const trax_event_batch *in,
     CK(cudaMemcpyAsync(seg + 2 * nseg_r, a.h_meta + 2 * nseg_r, 8, cudaMemcpyHostToDevice,
                        ctx->copy_stream));
     const void *src[7] = {in->x, in->y, in->z, in->layer, in->detector_id, in->hit_id, in->event};
-    for (int i = 0; i < 7; ++i)
+    for (int i : kChainCols)
         if (in->n_hits)
             CK(cudaMemcpyAsync(a.in_cols[i].p, src[i], (size_t)in->n_hits * 4,
                                cudaMemcpyHostToDevice, ctx->copy_stream));

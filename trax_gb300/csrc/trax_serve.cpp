@@ -65,10 +65,12 @@ struct Request {
     uint32_t pairs = kPairsUnknown;  /* the event's pair total, once counted */
     uint32_t layer_nhits[TRAX_MAX_LAYERS] = {};
     bool borrowed = false;
+    /* the columns the batched chain reads (not the detector and hit ids:
+     * tracklets come back as positions in the request's own columns) */
     const float *x = nullptr, *y = nullptr, *z = nullptr;
-    const uint32_t *layer = nullptr, *det = nullptr, *hitid = nullptr;
+    const uint32_t *layer = nullptr;
     std::vector<float> own_f;      /* x | y | z when copied */
-    std::vector<uint32_t> own_u;   /* layer | det | hitid when copied */
+    std::vector<uint32_t> own_u;   /* layer when copied */
 };
 
 struct Result {
@@ -86,7 +88,7 @@ struct Slot {
     uint64_t pair_cap = 0;
     std::vector<uint32_t> event_pairs;  /* per event of an admission count */
     float *x = nullptr, *y = nullptr, *z = nullptr;
-    uint32_t *layer = nullptr, *det = nullptr, *hitid = nullptr, *event = nullptr;
+    uint32_t *layer = nullptr, *event = nullptr;
     uint32_t *layer_nhits = nullptr;
     uint32_t *h1 = nullptr, *h2 = nullptr, *h3 = nullptr, *off = nullptr;
 };
@@ -130,13 +132,11 @@ trax_event_batch stage_requests(const trax_server *srv, Slot &slot,
         std::memcpy(slot.y + n, r->y, r->n_hits * 4ull);
         std::memcpy(slot.z + n, r->z, r->n_hits * 4ull);
         std::memcpy(slot.layer + n, r->layer, r->n_hits * 4ull);
-        std::memcpy(slot.det + n, r->det, r->n_hits * 4ull);
-        std::memcpy(slot.hitid + n, r->hitid, r->n_hits * 4ull);
         std::fill(slot.event + n, slot.event + n + r->n_hits, e);
         std::memcpy(slot.layer_nhits + (size_t)e * L, r->layer_nhits, L * 4ull);
         n += r->n_hits;
     }
-    return trax_event_batch{E, L, n, slot.x, slot.y, slot.z, slot.layer, slot.det, slot.hitid,
+    return trax_event_batch{E, L, n, slot.x, slot.y, slot.z, slot.layer, nullptr, nullptr,
                             slot.event, slot.layer_nhits};
 }
 
@@ -318,8 +318,7 @@ void destroy_slots(trax_server *srv)
 {
     for (Slot &s : srv->slots) {
         if (!s.ctx) continue;
-        void *bufs[] = {s.x, s.y, s.z, s.layer, s.det, s.hitid, s.event, s.layer_nhits,
-                        s.h1, s.h2, s.h3, s.off};
+        void *bufs[] = {s.x, s.y, s.z, s.layer, s.event, s.layer_nhits, s.h1, s.h2, s.h3, s.off};
         for (void *b : bufs) if (b) trax_host_free_pinned(s.ctx, b);
         trax_ctx_destroy(s.ctx);
         s.ctx = nullptr;
@@ -336,20 +335,17 @@ Request *make_request(trax_server *srv, const trax_event_batch *ev, uint64_t arr
     r->borrowed = borrow != 0;
     if (borrow) {
         r->x = ev->x; r->y = ev->y; r->z = ev->z;
-        r->layer = ev->layer; r->det = ev->detector_id; r->hitid = ev->hit_id;
+        r->layer = ev->layer;
     } else {
         const size_t n = ev->n_hits;
         r->own_f.resize(3 * n);
-        r->own_u.resize(3 * n);
+        r->own_u.resize(n);
         std::memcpy(r->own_f.data(), ev->x, n * 4);
         std::memcpy(r->own_f.data() + n, ev->y, n * 4);
         std::memcpy(r->own_f.data() + 2 * n, ev->z, n * 4);
         std::memcpy(r->own_u.data(), ev->layer, n * 4);
-        std::memcpy(r->own_u.data() + n, ev->detector_id, n * 4);
-        std::memcpy(r->own_u.data() + 2 * n, ev->hit_id, n * 4);
         r->x = r->own_f.data(); r->y = r->own_f.data() + n; r->z = r->own_f.data() + 2 * n;
-        r->layer = r->own_u.data(); r->det = r->own_u.data() + n;
-        r->hitid = r->own_u.data() + 2 * n;
+        r->layer = r->own_u.data();
     }
     return r;
 }
@@ -427,7 +423,7 @@ trax_status trax_server_create(trax_server **out, int device, const trax_config 
             st = trax_reserve(s.ctx, s.max_events, srv->L, s.max_hits, &g, (uint32_t)(kp * H),
                               (uint32_t)(kc * H), s.trk_cap);
         void **f[] = {(void **)&s.x, (void **)&s.y, (void **)&s.z, (void **)&s.layer,
-                      (void **)&s.det, (void **)&s.hitid, (void **)&s.event};
+                      (void **)&s.event};
         for (void **p : f)
             if (st == TRAX_OK) st = pinned(s.ctx, p, H * 4);
         if (st == TRAX_OK) st = pinned(s.ctx, (void **)&s.layer_nhits, (size_t)s.max_events * srv->L * 4);

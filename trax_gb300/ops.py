@@ -341,6 +341,16 @@ def build_triplets(ctx: Context, batch: EventBatch, cfg: A.TraxConfig, n_sectors
     return hits, grid, pairs, cands, trk
 
 
+def _host_cols(b: EventBatch):
+    """The batch's columns, contiguous; a column given as None (the detector
+    and hit ids, which the batched calls do not read) stays None."""
+    return [None if c is None else np.ascontiguousarray(c) for c in b.columns()]
+
+
+def _col_ptrs(cols):
+    return [None if c is None else c.ctypes.data for c in cols]
+
+
 class Pipeline:
     """Batched form: reserved buffers, one CUDA graph per run, no host sync
     inside the chain (trax_reserve / trax_seed_batch)."""
@@ -381,11 +391,10 @@ class Pipeline:
 
     def _batch_struct(self, b: EventBatch):
         self._apply_tuning(b)
-        cols = [np.ascontiguousarray(c) for c in b.columns()]
+        cols = _host_cols(b)
         ln = np.ascontiguousarray(b.layer_nhits.reshape(-1), dtype=U32)
         self._keep = cols + [ln]
-        return A.TraxEventBatch(b.n_events, b.n_layers, b.n_hits,
-                                *[c.ctypes.data for c in cols], ln.ctypes.data)
+        return A.TraxEventBatch(b.n_events, b.n_layers, b.n_hits, *_col_ptrs(cols), ln.ctypes.data)
 
     def seed(self, b: EventBatch, input_indices=False, copy=True):
         """Host arrays in, tracklets out (synchronous).  With copy=False the
@@ -419,10 +428,9 @@ class Pipeline:
             self._stream_out[k] = ([PinnedBuffer(self.ctx, 4 * cap, U32) for _ in range(3)],
                                    PinnedBuffer(self.ctx, 4 * self._off_len, U32))
         outs, off = self._stream_out[k]
-        cols = [np.ascontiguousarray(c) for c in b.columns()]
+        cols = _host_cols(b)
         ln = np.ascontiguousarray(b.layer_nhits.reshape(-1), dtype=U32)
-        bs = A.TraxEventBatch(b.n_events, b.n_layers, b.n_hits, *[c.ctypes.data for c in cols],
-                              ln.ctypes.data)
+        bs = A.TraxEventBatch(b.n_events, b.n_layers, b.n_hits, *_col_ptrs(cols), ln.ctypes.data)
         r = A.TraxBatchResult(outs[0].ptr, outs[1].ptr, outs[2].ptr, off.ptr, self.max_tracklets,
                               1 if input_indices else 0, 0, A.TraxCounts())
         t = C.c_uint32()

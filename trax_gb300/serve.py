@@ -21,11 +21,12 @@ U32 = np.uint32
 def _event_struct(ev: EventBatch, keep: list):
     if ev.n_events != 1:
         raise ValueError("a request is exactly one event")
-    cols = [np.ascontiguousarray(c) for c in ev.columns()]
+    # the detector and hit ids are not read by the server and may be None
+    cols = [None if c is None else np.ascontiguousarray(c) for c in ev.columns()]
     ln = np.ascontiguousarray(ev.layer_nhits.reshape(-1), dtype=U32)
     keep.extend(cols + [ln])
-    return A.TraxEventBatch(1, ev.n_layers, ev.n_hits, *[c.ctypes.data for c in cols],
-                            ln.ctypes.data)
+    return A.TraxEventBatch(1, ev.n_layers, ev.n_hits,
+                            *[None if c is None else c.ctypes.data for c in cols], ln.ctypes.data)
 
 
 class Server:
