@@ -372,7 +372,10 @@ constexpr int kGridItemsBanded = 4;  /* the same in the banded instance */
  * them; a band covers the whole occupied range in one go for hits within a
  * few z rows, as barrel layers give), and the grid rows outside that range
  * get the segment's start or end.  Cells are row-major, so a band's hits are
- * one contiguous part of the sorted segment.
+ * one contiguous part of the sorted segment.  Block-wide bands visit every
+ * hit once per band; staged segments whose cells sit in the scratch column
+ * (dense layers on fine grids) instead bucket their hits by band once and
+ * let each warp sort whole bands (the warp bands below).
  * Dynamic shared memory: (W + 1) * Ct + 2 * stage words.  BANDED is Ct < C
  * (the instance with bands has 64 registers, the other 48).
  */
@@ -515,8 +518,142 @@ __global__ void __maxnreg__(BANDED ? 64 : 48) k_grid_build(KParams kp, InCols in
             }
         }
 
+        /* Warp bands (BANDED, staged, cells in the scratch column): the hits
+         * are bucketed once by band of R2 z rows (a stable counting sort over
+         * (band, warp)), and each warp then sorts whole bands on its own:
+         * count the band's hits per cell in a warp-private table, scan it,
+         * write the band's grid rows and place its hits -- every hit is
+         * visited a fixed number of times and no band waits for a block
+         * barrier.  The band list (one word per hit) takes the last `stage`
+         * words of the per-warp tables, and each warp's table the R2 rows
+         * that fit in front of it.  Otherwise the block-wide bands below. */
+        const uint32_t tab_words = BANDED ? ((uint32_t)W * Ct > stage ? (uint32_t)W * Ct - stage : 0u) : 0u;
+        const uint32_t R2 = tab_words / ((uint32_t)W * P1);
+        const uint32_t nb2 = R2 ? (rhi - rlo) / R2 + 1 : 0u;
+        const bool wband = BANDED && scratch && staged && R2 >= 1 &&
+                           nb2 * (uint32_t)W <= tab_words && nb2 + 1 <= Ct;
+        if (wband) {
+            uint32_t *s_bc = s_cnt;                       /* [nb2][W] hits per band and warp */
+            uint32_t *s_bstart = s_tot;                   /* [nb2 + 1] first position of each band */
+            uint32_t *s_blist = s_cnt + (uint32_t)W * Ct - stage;  /* [n] hits in band order */
+            const uint32_t m = nb2 * (uint32_t)W;
+            for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) s_bc[k] = 0;
+            __syncthreads();
+            /* bucket counts per (band, warp) over each warp's sub-range */
+            for (uint32_t b = lo; b < hi; b += 32) {  /* warp-uniform */
+                const uint32_t i = b + lane;
+                const bool valid = i < hi;
+                const uint32_t band = valid ? (cscr[start + i].x / P1 - rlo) / R2 : 0u;
+                const uint32_t act = __ballot_sync(kFull, valid);
+                if (valid) {
+                    const uint32_t peers = __match_any_sync(act, band);
+                    if (lane == __ffs(peers) - 1) s_bc[band * W + w] += __popc(peers);
+                }
+                __syncwarp();
+            }
+            __syncthreads();
+            {
+                const uint32_t per = (m + blockDim.x - 1) / blockDim.x;
+                const uint32_t c0 = min(m, threadIdx.x * per), c1 = min(m, c0 + per);
+                uint32_t sum = 0, total;
+                for (uint32_t c = c0; c < c1; ++c) sum += s_bc[c];
+                uint32_t run = block_exclusive_scan(sum, s_warp, &total);
+                for (uint32_t c = c0; c < c1; ++c) {
+                    const uint32_t t = s_bc[c];
+                    s_bc[c] = run;
+                    run += t;
+                }
+            }
+            __syncthreads();
+            for (uint32_t k = threadIdx.x; k <= nb2; k += blockDim.x) s_bstart[k] = k < nb2 ? s_bc[k * W] : n;
+            __syncthreads();
+            /* the band list, stable: warps in order, each sub-range in order */
+            for (uint32_t b = lo; b < hi; b += 32) {  /* warp-uniform */
+                const uint32_t i = b + lane;
+                const bool valid = i < hi;
+                const uint32_t band = valid ? (cscr[start + i].x / P1 - rlo) / R2 : 0u;
+                const uint32_t act = __ballot_sync(kFull, valid);
+                uint32_t peers = 0, pos = 0;
+                if (valid) {
+                    peers = __match_any_sync(act, band);
+                    pos = s_bc[band * W + w] + __popc(peers & lt_mask);
+                }
+                __syncwarp();
+                if (valid && lane == __ffs(peers) - 1) s_bc[band * W + w] += __popc(peers);
+                __syncwarp();
+                if (valid) s_blist[pos] = i;
+            }
+            __syncthreads();
+            /* each warp sorts whole bands */
+            uint32_t *tab = s_cnt + (uint32_t)w * R2 * P1;
+            for (uint32_t bb = w; bb < nb2; bb += W) {  /* warp-uniform */
+                const uint32_t rb = rlo + bb * R2;
+                const uint32_t cb0 = rb * P1, nb = min(R2, rhi + 1 - rb) * P1;
+                const uint32_t bs = s_bstart[bb], be = s_bstart[bb + 1];
+                for (uint32_t c = lane; c < nb; c += 32) tab[c] = 0;
+                __syncwarp();
+                for (uint32_t kb = bs; kb < be; kb += 32) {
+                    const uint32_t k = kb + lane;
+                    const bool valid = k < be;
+                    const uint32_t lc = valid ? cscr[start + s_blist[k]].x - cb0 : 0u;
+                    const uint32_t act = __ballot_sync(kFull, valid);
+                    if (valid) {
+                        const uint32_t peers = __match_any_sync(act, lc);
+                        if (lane == __ffs(peers) - 1) tab[lc] += __popc(peers);
+                    }
+                    __syncwarp();
+                }
+                /* exclusive scan of the band's cells, lane-contiguous blocks */
+                const uint32_t per = (nb + 31) / 32;
+                const uint32_t c0 = min(nb, lane * per), c1 = min(nb, c0 + per);
+                uint32_t sum = 0;
+                for (uint32_t c = c0; c < c1; ++c) sum += tab[c];
+                uint32_t incl = sum;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const uint32_t y = __shfl_up_sync(kFull, incl, d);
+                    if (lane >= (uint32_t)d) incl += y;
+                }
+                uint32_t run = incl - sum;
+                for (uint32_t c = c0; c < c1; ++c) {
+                    const uint32_t t = tab[c];
+                    tab[c] = run;
+                    run += t;
+                }
+                __syncwarp();
+                for (uint32_t c = lane; c < nb; c += 32) gseg[cb0 + c] = start + bs + tab[c];
+                /* place: the band's hits in list order, cursor per cell */
+                for (uint32_t kb = bs; kb < be; kb += 32) {
+                    const uint32_t k = kb + lane;
+                    const bool valid = k < be;
+                    uint32_t i = 0, lc = 0, peers = 0, pos = 0;
+                    float phi = 0.f;
+                    if (valid) {
+                        i = s_blist[k];
+                        const uint2 cp = cscr[start + i];
+                        lc = cp.x - cb0;
+                        phi = __uint_as_float(cp.y);
+                    }
+                    const uint32_t act = __ballot_sync(kFull, valid);
+                    if (valid) {
+                        peers = __match_any_sync(act, lc);
+                        pos = bs + tab[lc] + __popc(peers & lt_mask);
+                    }
+                    __syncwarp();
+                    if (valid && lane == __ffs(peers) - 1) tab[lc] += __popc(peers);
+                    __syncwarp();
+                    if (valid) {
+                        s_src[pos] = i;
+                        s_phi[pos] = phi;
+                    }
+                }
+                __syncwarp();
+            }
+            __syncthreads();
+        }
+
         uint32_t band_base = 0;  /* hits in the rows below the band */
-        for (uint32_t rb = rlo; rb <= rhi; rb += R) {  /* block-uniform */
+        for (uint32_t rb = rlo; !wband && rb <= rhi; rb += R) {  /* block-uniform */
             const uint32_t cb0 = BANDED ? rb * P1 : 0u;
             const uint32_t nb = BANDED ? min(R, rhi + 1 - rb) * P1 : C;  /* the band's cells */
             {
