@@ -558,6 +558,22 @@ def resident_rate(ctx, p, b, steps, warmup, dist, clocks=None):
     return aggregate_rate(dist, b.n_events, steps, ctx.timer_elapsed_ms(62, 63))
 
 
+def pinned_copy(ctx, b):
+    """The batch's columns the batched calls upload (x, y, z, layer, event) in
+    pinned host memory, the detector and hit ids left out (they are never
+    read on that path); returns (batch, buffers to free)."""
+    from trax_gb300.gen import EventBatch
+    from trax_gb300.runtime import PinnedBuffer
+    bufs, cols = [], {}
+    for name in ("x", "y", "z", "layer", "event"):
+        c = getattr(b, name)
+        buf = PinnedBuffer(ctx, c.nbytes, c.dtype)
+        buf.array[:] = c
+        bufs.append(buf)
+        cols[name] = buf.array
+    return EventBatch(detector_id=None, hit_id=None, layer_nhits=b.layer_nhits, **cols), bufs
+
+
 def measure_section(ctx, w, B, args, dist, threads):
     """A further workload: resident value, one-at-a-time e2e, the per-event
     form, and parity of its tracklets against the oracle."""
@@ -568,12 +584,16 @@ def measure_section(ctx, w, B, args, dist, threads):
     best_walk, _ = tune_walk(ctx, p, b, reps=3)
     steps = max(3, args.steps // 2)
     value, ms_total, events_all = resident_rate(ctx, p, b, steps, args.warmup, dist)
-    trk, off, _ = p.seed(b, input_indices=True)
+    pb, bufs = pinned_copy(ctx, b)
+    p.seed(pb, input_indices=True, copy=False)
     ctx.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
-        trk, off, _ = p.seed(b, input_indices=True)
+        p.seed(pb, input_indices=True, copy=False)
     sync_s = dist.max(time.perf_counter() - t0)
+    for x in bufs:
+        x.free()
+    trk, off, _ = p.seed(b, input_indices=True)
     par = parity_check(b, w, trk, off, B if B <= 128 else args.parity_events, threads)
     del p
     pe = per_event_form(ctx, w, b, args.per_event_sample)
@@ -668,7 +688,6 @@ def run_serving(args):
 
 def run_ours(args, dist):
     from trax_gb300 import Context, gen
-    from trax_gb300.runtime import PinnedBuffer
     from trax_gb300.autotune import tune_walk
 
     threads = os.cpu_count() or 1
@@ -753,15 +772,7 @@ def run_ours(args, dist):
                             "bound by instruction issue and load latency (sm_issue_active from ncu)"}
 
     # ---- e2e through the streaming API with pinned host buffers -----------
-    cols = b.columns()
-    pinned, pb_cols = [], []
-    for c in cols:
-        buf = PinnedBuffer(ctx, c.nbytes, c.dtype)
-        buf.array[:] = c
-        pinned.append(buf)
-        pb_cols.append(buf.array)
-    from trax_gb300.gen import EventBatch
-    pinned_batch = EventBatch(*pb_cols, b.layer_nhits)
+    pinned_batch, pinned = pinned_copy(ctx, b)
     for _ in range(args.warmup):
         p.seed(pinned_batch, copy=False)
     dist.barrier()
