@@ -114,6 +114,11 @@ struct trax_ctx {
     int gb_warps = 0, gb_per_sm = 0;
     uint32_t gb_stage = 0;                /* k_grid_build staged-segment capacity */
     uint32_t gb_cells = 0;                /* k_grid_build per-warp table cells */
+    /* dense segments on fine grids: k_grid_build_wb with gb_wb_warps warps,
+     * bands of gb_R2 z rows, gb_wb_smem bytes of shared memory */
+    bool gb_wb = false;
+    uint32_t gb_R2 = 0, gb_wb_warps = 0;
+    size_t gb_wb_smem = 0;
     cudaGraphExec_t graph = nullptr;
     uint32_t staged_events = 0, staged_hits = 0;
     /* streaming submission: two slots, uploads on their own stream */
@@ -288,6 +293,13 @@ void apply_launch_cap(trax_ctx *ctx)
  *            table work of a segment grows with the warps times the cells its
  *            rows occupy, not with the number of bands, so more warps and
  *            narrower bands win: 8 rows 0.75 ms, 4 rows 0.72 ms at 256 x 192). */
+/* The grid build's scratch: each hit's (cell, phi), then the warp-band
+ * kernel's band list (one word per hit). */
+size_t gscr_bytes(size_t n_hits) { return (n_hits + 1) * 8 + n_hits * 4 + 16; }
+
+constexpr uint32_t kWbWarps = 16;  /* k_grid_build_wb: warps per CTA */
+constexpr uint32_t kWbRows = 2;    /* k_grid_build_wb: z rows per band */
+
 trax_status grid_plan(trax_ctx *ctx, uint32_t C, uint32_t avg_seg)
 {
     const uint32_t P1 = ctx->kp.nphi + 1, rows = C / P1;
@@ -329,6 +341,28 @@ trax_status grid_plan(trax_ctx *ctx, uint32_t C, uint32_t avg_seg)
     ctx->gb_warps = (int)W;
     ctx->gb_cells = (uint32_t)Ct;
     ctx->gb_per_sm = per_sm < 1 ? 1 : per_sm;
+    /* a fine grid (bands) whose average segment is beyond the registers of
+     * k_grid_build (each hit's cell would go through the scratch column):
+     * warp bands in k_grid_build_wb, two or more CTAs per SM */
+    ctx->gb_wb = false;
+    if (Ct < C && avg_seg > (uint32_t)W * 32u * (uint32_t)kGridItemsBanded) {
+        const uint32_t Wb = kWbWarps, R2 = kWbRows, nbm = (rows + R2 - 1) / R2;
+        const uint32_t stage_b = std::max<uint32_t>(512, (3 * avg_seg / 2 + 255) / 256 * 256);
+        const size_t tabw = std::max<size_t>((size_t)nbm * Wb, (size_t)Wb * R2 * P1);
+        const size_t smem_b = ((size_t)stage_b + tabw + nbm + 1) * 4;
+        int per_sm_b = 0;
+        if (smem_b <= ctx->smem_optin)
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_b, k_grid_build_wb,
+                                                             (int)Wb * 32, smem_b));
+        if (per_sm_b >= 2) {
+            ctx->gb_wb = true;
+            ctx->gb_R2 = R2;
+            ctx->gb_wb_warps = Wb;
+            ctx->gb_wb_smem = smem_b;
+            ctx->gb_stage = stage_b;
+            ctx->gb_per_sm = per_sm_b;
+        }
+    }
     return TRAX_OK;
 }
 
@@ -378,12 +412,16 @@ trax_status enqueue_grid(trax_ctx *ctx, const InCols &in, const SortedCols &out,
     if (s != TRAX_OK) return s;
     const int W = ctx->gb_warps, per_sm = ctx->gb_per_sm;
     const size_t smem = ((size_t)(W + 1) * ctx->gb_cells + 2ull * ctx->gb_stage) * 4;
-    if ((s = ensure(ctx, ctx->gscr, (size_t)n_hits * 8 + 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->gscr, gscr_bytes(n_hits))) != TRAX_OK) return s;
     uint2 *cscr = (uint2 *)ctx->gscr.p;
     uint32_t blocks = std::min<uint32_t>(max_segs, (uint32_t)(ctx->sm_count * per_sm));
     if (blocks == 0) blocks = 1;
     CK(cudaMemsetAsync(&ctx->d_state->gb_next, 0, 4, ctx->stream));  /* segment counter */
-    if (ctx->gb_cells < kp.C)
+    if (ctx->gb_wb)
+        k_grid_build_wb<<<blocks, ctx->gb_wb_warps * 32, ctx->gb_wb_smem, ctx->stream>>>(
+            kp, in, out, seg_start, seg_n, grid, ctx->gb_stage, ctx->gb_R2, cscr,
+            (uint32_t *)(cscr + (size_t)n_hits + 1), ctx->d_state);
+    else if (ctx->gb_cells < kp.C)
         k_grid_build<true><<<blocks, W * 32, smem, ctx->stream>>>(
             kp, in, out, seg_start, seg_n, grid, ctx->gb_stage, ctx->gb_cells, cscr, ctx->d_state);
     else
@@ -898,6 +936,8 @@ trax_status trax_ctx_create(trax_ctx **out, int device)
     if ((e = cudaFuncSetAttribute(k_grid_build<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)ctx->smem_optin)) != cudaSuccess) return bail(e);
     if ((e = cudaFuncSetAttribute(k_grid_build<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)ctx->smem_optin)) != cudaSuccess) return bail(e);
+    if ((e = cudaFuncSetAttribute(k_grid_build_wb, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)ctx->smem_optin)) != cudaSuccess) return bail(e);
     int b = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->occ_pair, k_pair_fused<true>, kFusedThreads, 0);
@@ -1630,7 +1670,7 @@ trax_status trax_reserve(trax_ctx *ctx, uint32_t max_events, uint32_t max_layers
     if ((s = ensure(ctx, ctx->zphi, (size_t)max_hits * 8 + 8)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->zh, (size_t)max_hits * 2 + 32)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->xyzp, (size_t)max_hits * 16 + 16)) != TRAX_OK) return s;
-    if ((s = ensure(ctx, ctx->gscr, (size_t)max_hits * 8 + 8)) != TRAX_OK) return s;
+    if ((s = ensure(ctx, ctx->gscr, gscr_bytes(max_hits))) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->g_start, G * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->g_base, (G + 1) * 4)) != TRAX_OK) return s;
     if ((s = ensure(ctx, ctx->slots, slot_cap * 8)) != TRAX_OK) return s;

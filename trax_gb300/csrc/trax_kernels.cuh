@@ -846,6 +846,255 @@ __global__ void __maxnreg__(BANDED ? 64 : 48) k_grid_build(KParams kp, InCols in
     }
 }
 
+/* One sorted hit written to every output column at position d. */
+__device__ __forceinline__ void grid_write_hit(const InCols &in, const SortedCols &out, uint32_t h,
+                                               uint32_t d, float x, float y, float z, float phi,
+                                               uint32_t ly, uint32_t ev)
+{
+    if (out.x) {
+        out.x[d] = x; out.y[d] = y; out.z[d] = z; out.phi[d] = phi;
+        out.det[d] = in.det[h]; out.hitid[d] = in.hitid[h];
+    }
+    out.layer[d] = ly; out.event[d] = ev; out.orig[d] = h;
+    if (out.zphi) {
+        out.zphi[d] = make_float2(z, phi);
+        out.zh[d] = __half_as_ushort(__float2half_rn(z));
+        out.xyzp[d] = make_float4(x, y, z, phi);
+    }
+}
+
+/*
+ * Grid build for dense segments on fine grids (the average segment beyond the
+ * registers of k_grid_build, its grid beyond one cell table): warp bands,
+ * with shared memory small enough for two CTAs per SM, so that one
+ * segment's barriers and loads overlap another's.  A CTA takes (event, layer)
+ * segments from a device counter:
+ *   pass 0  each hit's cell and phi into the scratch column `cscr`, and the
+ *           z rows the segment occupies;
+ *   pass 1  hits per (band of R2 rows, warp) over each warp's sub-range; an
+ *           exclusive scan over (band, warp) gives every band's first
+ *           position and every warp's cursor in it;
+ *   pass 2  the band list `blist` (segment-relative input indices in band
+ *           order; stable: warps in order, each sub-range in order);
+ *   pass 3  each warp sorts whole bands: per-cell counts in a warp-private
+ *           table, their scan, the band's grid rows, and each hit's position,
+ *           recorded in shared memory (segments of at most `stage` hits) or
+ *           the columns written there at once;
+ *   pass 4  staged segments write every column coalesced.
+ * Within a cell hits keep input order, as in k_grid_build.  Dynamic shared
+ * memory: stage + tabw + nbm + 1 words (nbm = the bands of Z + 1 rows,
+ * tabw = max(nbm * W, W * R2 * (P + 1))).
+ */
+__global__ void __launch_bounds__(512, 2) k_grid_build_wb(KParams kp, InCols in, SortedCols out,
+                                                          const uint32_t *seg_start,
+                                                          const uint32_t *seg_n, uint32_t *grid,
+                                                          uint32_t stage, uint32_t R2, uint2 *cscr,
+                                                          uint32_t *blist, DevState *st)
+{
+    extern __shared__ uint32_t smem[];
+    __shared__ uint32_t s_warp[33];
+    __shared__ uint32_t s_seg, s_rlo, s_rhi;
+    const uint32_t C = kp.C, P1 = kp.nphi + 1;
+    const uint32_t W = blockDim.x >> 5;
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t lt_mask = lanemask_lt();
+    const uint32_t nbm = (kp.nz + R2) / R2;  /* bands of the Z + 1 rows */
+    const uint32_t tabw = max(nbm * W, W * R2 * P1);
+    uint32_t *s_src = smem;              /* [stage] segment-relative input index per position */
+    uint32_t *s_tab = smem + stage;      /* [tabw] (band, warp) counts, then the warps' cell tables */
+    uint32_t *s_bstart = s_tab + tabw;   /* [nbm + 1] first position of each band */
+    const uint32_t nseg = st->n_events * kp.n_layers;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_seg = atomicAdd(&st->gb_next, 1u);
+            s_rlo = 0xffffffffu;
+            s_rhi = 0u;
+        }
+        __syncthreads();
+        const uint32_t seg = s_seg;
+        if (seg >= nseg) break;  /* block-uniform */
+        const uint32_t e = seg / kp.n_layers, l = seg % kp.n_layers;
+        const uint32_t start = seg_start[seg], n = seg_n[seg];
+        const uint32_t chunk = (n + W - 1) / W;
+        const uint32_t lo = min(n, w * chunk), hi = min(n, lo + chunk);
+        const bool staged = n <= stage;
+        uint32_t *gseg = grid + (size_t)seg * C;
+        uint32_t *bl = blist + start;
+
+        /* pass 0 */
+        {
+            bool anybad = false;
+            uint32_t mn = 0xffffffffu, mx = 0u;
+            for (uint32_t i = lo + lane; i < hi; i += 32) {
+                const uint32_t h = start + i;
+                float phi;
+                bool bad;
+                const uint32_t cell = hit_cell(kp, in.x[h], in.y[h], in.z[h], &phi, &bad);
+                anybad |= bad;
+                cscr[h] = make_uint2(cell, __float_as_uint(phi));
+                const uint32_t zs = cell / P1;
+                mn = min(mn, zs);
+                mx = max(mx, zs);
+            }
+            if (anybad) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_OUTSIDE_GRID);
+#pragma unroll
+            for (int d = 16; d; d >>= 1) {
+                mn = min(mn, __shfl_xor_sync(kFull, mn, d));
+                mx = max(mx, __shfl_xor_sync(kFull, mx, d));
+            }
+            if (lane == 0) {
+                atomicMin(&s_rlo, mn);
+                atomicMax(&s_rhi, mx);
+            }
+        }
+        __syncthreads();
+        uint32_t rlo = s_rlo, rhi = s_rhi;
+        if (rlo > rhi) rlo = rhi = 0;  /* no hits */
+        /* rows below the occupied range start at the segment start, rows
+         * above it at its end */
+        for (uint32_t c = threadIdx.x; c < rlo * P1; c += blockDim.x) gseg[c] = start;
+        for (uint32_t c = (rhi + 1) * P1 + threadIdx.x; c < C; c += blockDim.x) gseg[c] = start + n;
+        const uint32_t nb2 = (rhi - rlo) / R2 + 1;  /* <= nbm */
+        const uint32_t m = nb2 * W;
+        for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) s_tab[k] = 0;
+        __syncthreads();
+
+        /* pass 1 */
+        for (uint32_t b = lo; b < hi; b += 32) {  /* warp-uniform */
+            const uint32_t i = b + lane;
+            const bool valid = i < hi;
+            const uint32_t band = valid ? (cscr[start + i].x / P1 - rlo) / R2 : 0u;
+            const uint32_t act = __ballot_sync(kFull, valid);
+            if (valid) {
+                const uint32_t peers = __match_any_sync(act, band);
+                if (lane == __ffs(peers) - 1) s_tab[band * W + w] += __popc(peers);
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        {
+            const uint32_t per = (m + blockDim.x - 1) / blockDim.x;
+            const uint32_t c0 = min(m, threadIdx.x * per), c1 = min(m, c0 + per);
+            uint32_t sum = 0, total;
+            for (uint32_t c = c0; c < c1; ++c) sum += s_tab[c];
+            uint32_t run = block_exclusive_scan(sum, s_warp, &total);
+            for (uint32_t c = c0; c < c1; ++c) {
+                const uint32_t t = s_tab[c];
+                s_tab[c] = run;
+                run += t;
+            }
+        }
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k <= nb2; k += blockDim.x) s_bstart[k] = k < nb2 ? s_tab[k * W] : n;
+        __syncthreads();
+
+        /* pass 2 */
+        for (uint32_t b = lo; b < hi; b += 32) {  /* warp-uniform */
+            const uint32_t i = b + lane;
+            const bool valid = i < hi;
+            const uint32_t band = valid ? (cscr[start + i].x / P1 - rlo) / R2 : 0u;
+            const uint32_t act = __ballot_sync(kFull, valid);
+            uint32_t peers = 0, pos = 0;
+            if (valid) {
+                peers = __match_any_sync(act, band);
+                pos = s_tab[band * W + w] + __popc(peers & lt_mask);
+            }
+            __syncwarp();
+            if (valid && lane == __ffs(peers) - 1) s_tab[band * W + w] += __popc(peers);
+            __syncwarp();
+            if (valid) bl[pos] = i;
+        }
+        __syncthreads();
+
+        /* pass 3 */
+        uint32_t *tab = s_tab + w * R2 * P1;
+        bool mismatch = false;
+        for (uint32_t bb = w; bb < nb2; bb += W) {  /* warp-uniform */
+            const uint32_t rb = rlo + bb * R2;
+            const uint32_t cb0 = rb * P1, nb = min(R2, rhi + 1 - rb) * P1;
+            const uint32_t bs = s_bstart[bb], be = s_bstart[bb + 1];
+            for (uint32_t c = lane; c < nb; c += 32) tab[c] = 0;
+            __syncwarp();
+            for (uint32_t kb = bs; kb < be; kb += 32) {
+                const uint32_t k = kb + lane;
+                const bool valid = k < be;
+                const uint32_t lc = valid ? cscr[start + bl[k]].x - cb0 : 0u;
+                const uint32_t act = __ballot_sync(kFull, valid);
+                if (valid) {
+                    const uint32_t peers = __match_any_sync(act, lc);
+                    if (lane == __ffs(peers) - 1) tab[lc] += __popc(peers);
+                }
+                __syncwarp();
+            }
+            const uint32_t per = (nb + 31) / 32;
+            const uint32_t c0 = min(nb, lane * per), c1 = min(nb, c0 + per);
+            uint32_t sum = 0;
+            for (uint32_t c = c0; c < c1; ++c) sum += tab[c];
+            uint32_t incl = sum;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t y = __shfl_up_sync(kFull, incl, d);
+                if (lane >= (uint32_t)d) incl += y;
+            }
+            uint32_t run = incl - sum;
+            for (uint32_t c = c0; c < c1; ++c) {
+                const uint32_t t = tab[c];
+                tab[c] = run;
+                run += t;
+            }
+            __syncwarp();
+            for (uint32_t c = lane; c < nb; c += 32) gseg[cb0 + c] = start + bs + tab[c];
+            for (uint32_t kb = bs; kb < be; kb += 32) {
+                const uint32_t k = kb + lane;
+                const bool valid = k < be;
+                uint32_t i = 0, lc = 0, peers = 0, pos = 0;
+                float phi = 0.f;
+                if (valid) {
+                    i = bl[k];
+                    const uint2 cp = cscr[start + i];
+                    lc = cp.x - cb0;
+                    phi = __uint_as_float(cp.y);
+                }
+                const uint32_t act = __ballot_sync(kFull, valid);
+                if (valid) {
+                    peers = __match_any_sync(act, lc);
+                    pos = bs + tab[lc] + __popc(peers & lt_mask);
+                }
+                __syncwarp();
+                if (valid && lane == __ffs(peers) - 1) tab[lc] += __popc(peers);
+                __syncwarp();
+                if (valid) {
+                    if (staged) {
+                        s_src[pos] = i;
+                    } else {
+                        const uint32_t h = start + i;
+                        const uint32_t ly = in.layer[h], ev = in.event[h];
+                        mismatch |= ly != l + 1 || ev != e;
+                        grid_write_hit(in, out, h, start + pos, in.x[h], in.y[h], in.z[h], phi, ly, ev);
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        if (mismatch) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_LAYER_MISMATCH);
+        __syncthreads();
+
+        /* pass 4 */
+        if (staged) {
+            bool mm = false;
+            for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+                const uint32_t h = start + s_src[k];
+                const uint32_t ly = in.layer[h], ev = in.event[h];
+                mm |= ly != l + 1 || ev != e;
+                grid_write_hit(in, out, h, start + k, in.x[h], in.y[h], in.z[h],
+                               __uint_as_float(cscr[h].y), ly, ev);
+            }
+            if (mm) set_fault(st, TRAX_ERR_BAD_INPUT, TRAX_DETAIL_HIT_LAYER_MISMATCH);
+            __syncthreads();
+        }
+    }
+}
+
 /* (z, phi) of the sorted hits packed for the candidate loops, z in half
  * precision for the candidate screen, and (x, y, z, phi) packed. */
 __global__ void __launch_bounds__(256) k_pack_zphi(const float *X, const float *Y, const float *Z,
