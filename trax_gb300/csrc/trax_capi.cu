@@ -298,7 +298,7 @@ void apply_launch_cap(trax_ctx *ctx)
 size_t gscr_bytes(size_t n_hits) { return (n_hits + 1) * 8 + n_hits * 4 + 16; }
 
 constexpr uint32_t kWbWarps = 16;  /* k_grid_build_wb: warps per CTA */
-constexpr uint32_t kWbRows = 2;    /* k_grid_build_wb: z rows per band */
+constexpr uint32_t kWbRows = 1;    /* k_grid_build_wb: z rows per band */
 
 trax_status grid_plan(trax_ctx *ctx, uint32_t C, uint32_t avg_seg)
 {
