@@ -52,9 +52,9 @@ FALLBACK_HBM_GBS = 6800.0
 HEADLINE = "pileup200"
 # grid (z x phi bins) each workload is timed at: the workload's own, or for
 # the high-pile-up configuration the autotuner's choice (its sweep over
-# {8..256} x {16..192} on pile-up-200 events picks 256 x 192; the bench's
+# {8..320} x {16..192} on pile-up-200 events picks 320 x 192; the bench's
 # 'autotune' section repeats the sweep and reports whether it still does)
-TUNED_GRID = {"pileup200": (256, 192),
+TUNED_GRID = {"pileup200": (320, 192),
               # the streaming mix (pile-up U{0..200}) served at the grid and walk
               # the autotuner picks for its densest events
               "stream-pileup-u200": (256, 192)}
@@ -610,7 +610,7 @@ def measure_section(ctx, w, B, args, dist, threads):
 
 
 def run_autotune(args, ctx):
-    """Config 4: pile-up-200 events, grid sweep {8..256} x {16..192} with the
+    """Config 4: pile-up-200 events, grid sweep {8..320} x {16..192} with the
     walk tuned per grid, the plain per-event form at the best grid."""
     from trax_gb300 import gen
     from trax_gb300.autotune import sweep_grids, density_class, GRID_Z, GRID_PHI, MAX_CELLS

@@ -82,7 +82,7 @@ def test_batched_calls_do_not_read_detector_and_hit_ids(gpu_ctx):
             assert np.array_equal(trk, want) and np.array_equal(off, want_off)
 
 
-@pytest.mark.parametrize("zp", [(64, 64), (64, 128), (32, 64), (256, 192), (128, 128)])
+@pytest.mark.parametrize("zp", [(64, 64), (64, 128), (32, 64), (256, 192), (320, 192), (128, 128)])
 def test_autotuned_grids_equal_oracle(gpu_ctx, zp):
     """The grids the autotuner selects on pile-up 200 (the truncated
     candidate set depends on the grid, so the oracle runs at the same one),

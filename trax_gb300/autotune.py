@@ -26,7 +26,7 @@ from .runtime import Context
 WALK_CANDIDATES = ((1 << 30, 256), (96, 256), (96, 32), (48, 16), (24, 8), (0, 16), (0, 0))
 # resident blocks per SM of the candidate kernels (0: as many as fit)
 BLOCK_CAPS = (4, 3, 2)
-GRID_Z = (8, 16, 32, 64, 128, 256)
+GRID_Z = (8, 16, 32, 64, 128, 256, 320)
 GRID_PHI = (16, 32, 64, 128, 192)
 # cells per layer the library accepts ((n_sectors_z + 1) * (n_sectors_phi + 1))
 MAX_CELLS = 65536
