@@ -88,3 +88,32 @@ def test_poisson_arrivals_are_a_seeded_increasing_stream_at_the_rate():
     assert not np.array_equal(a, poisson_arrivals(20_000, 5_000.0, start, seed=8))
     mean_gap_s = (int(a[-1]) - start) / 1e9 / len(a)
     assert abs(mean_gap_s * 5_000.0 - 1.0) < 0.03
+
+
+def test_batch_struct_passes_null_id_columns():
+    """The batched calls never read the detector and hit ids: a batch that
+    leaves them out (None) reaches the C-ABI with null pointers there and
+    the five columns it uploads intact."""
+    import dataclasses
+    from trax_gb300 import gen
+    from trax_gb300 import _abi as A
+    from trax_gb300.ops import _col_ptrs, _host_cols
+    b = gen.generate_batch(gen.WORKLOADS["multimuon-1000trk"], 2)
+    nb = dataclasses.replace(b, detector_id=None, hit_id=None)
+    cols = _host_cols(nb)
+    assert cols[4] is None and cols[5] is None
+    ln = np.ascontiguousarray(nb.layer_nhits.reshape(-1), dtype=np.uint32)
+    s = A.TraxEventBatch(nb.n_events, nb.n_layers, nb.n_hits, *_col_ptrs(cols), ln.ctypes.data)
+    assert s.detector_id is None and s.hit_id is None
+    for name, c in zip(("x", "y", "z", "layer", "event"), (cols[0], cols[1], cols[2], cols[3], cols[6])):
+        assert getattr(s, name) == c.ctypes.data
+    assert s.n_hits == b.n_hits and s.n_events == 2
+
+
+def test_grid_sweep_includes_the_headline_grid():
+    """The bench's headline grid for pile-up 200 lies inside the autotuner's
+    sweep, within the cell limit."""
+    import bench
+    z, p = bench.TUNED_GRID["pileup200"]
+    assert z in autotune.GRID_Z and p in autotune.GRID_PHI
+    assert (z + 1) * (p + 1) <= autotune.MAX_CELLS
